@@ -1,0 +1,41 @@
+#!/usr/bin/env bash
+# build_ref.sh -- compile the reference's own host ADI path into oracle/_ref/ref_driver.
+#
+# TEST INFRASTRUCTURE ONLY.  Reads the reference sources where they lie (default
+# /root/reference, override with LSS_REFERENCE_DIR), copies the headers it needs into
+# oracle/_ref/src (git-ignored, never committed), applies four mechanical portability
+# patches (MSVC-only std::exception(const char*) ctor; two shadowed template-template
+# parameter names; one decltype on a non-class), and compiles oracle/ref_driver.cu
+# against them.  Host code only runs; nvcc is used because the reference headers pull in
+# thrust device headers.  -ffp-contract=off keeps the reference's two-rounding a*b+c.
+set -euo pipefail
+HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
+REF="${LSS_REFERENCE_DIR:-/root/reference}"
+OUT="$HERE/_ref"
+if [ ! -d "$REF/pde_solvers" ]; then
+    echo "build_ref.sh: reference not found at $REF (skipping)" >&2
+    exit 0
+fi
+mkdir -p "$OUT"
+if [ -x "$OUT/ref_driver" ] && [ "$OUT/ref_driver" -nt "$HERE/ref_driver.cu" ] && [ "$OUT/ref_driver" -nt "$0" ]; then
+    echo "build_ref.sh: $OUT/ref_driver is up to date"
+    exit 0
+fi
+rm -rf "$OUT/src"
+mkdir -p "$OUT/src"
+( cd "$REF" && find . \( -name '*.hpp' -o -name '*.cu' \) ! -path './.git/*' -print0 | \
+    while IFS= read -r -d '' f; do mkdir -p "$OUT/src/$(dirname "$f")"; cp "$f" "$OUT/src/$f"; done )
+cd "$OUT/src"
+find . -name '*.hpp' -print0 | xargs -0 sed -i 's/std::exception(/std::runtime_error(/g'
+for f in sparse_solvers/general/core_sor_solver/lss_core_sor_solver.hpp \
+         sparse_solvers/general/core_sor_solver_cuda/lss_core_sor_solver_cuda.hpp; do
+    sed -i 's/template <typename fp_type, typename allocator> typename container/template <typename, typename> typename container/' "$f"
+    sed -i 's/template <template <typename fp_type> typename traits>/template <template <typename> typename traits>/' "$f"
+done
+sed -i 's/decltype(errors)::value_type(0.0)/fp_type(0.0)/' sparse_solvers/general/core_sor_solver_cuda/lss_core_sor_solver_cuda.hpp
+CUS=$(find . -name '*.cu' ! -name main.cu | sort)
+ARCH="${LSS_REF_ARCH:-sm_100}"
+nvcc -std=c++17 -O2 -arch="$ARCH" -Xcompiler -ffp-contract=off \
+    -include cmath -include stdexcept -I"$OUT/src" \
+    "$HERE/ref_driver.cu" $CUS -o "$OUT/ref_driver" -lcusolver -lcusparse -lcublas
+echo "build_ref.sh: built $OUT/ref_driver"
