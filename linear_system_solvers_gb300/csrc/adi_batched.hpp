@@ -1,0 +1,26 @@
+// adi_batched.hpp -- batched persistent-kernel solver and the adjoint solver.
+#pragma once
+
+#include <memory>
+#include <vector>
+
+#include "adi_common.hpp"
+#include "adi_device.cuh"
+#include "adi_tables.hpp"
+
+namespace lss_gb300 {
+
+struct batch_impl;   // defined in adi_batched.cu
+struct adjoint_impl; // defined in adi_adjoint.cu
+
+// Forward + adjoint of one parametric FP64 Heston problem (behind lss_adi_adjoint).
+struct adjoint_solver {
+    std::unique_ptr<adjoint_impl> impl;
+    adjoint_solver();
+    ~adjoint_solver();
+    int init(const lss_adi_problem &p);
+    int run(const void *payoff, double *out_value, double *dv_dparams, void *dv_dpayoff, int checkpoint_every, int flags,
+            void *stream);
+};
+
+} // namespace lss_gb300

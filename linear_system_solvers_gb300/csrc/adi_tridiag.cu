@@ -1,0 +1,88 @@
+// adi_tridiag.cu -- batched Thomas LU line solver (lss_tridiag_thomas_lu).
+//
+// The reference's thomas_lu_solver with a Dirichlet boundary_pair
+// (sparse_solvers/tridiagonal/thomas_lu_solver/lss_thomas_lu_solver.hpp:125-191,
+// lss_thomas_lu_boundary.hpp:114-205), one thread per line, lines fastest in memory so
+// every access of a warp is one coalesced row.  Reference operation order, no FMA
+// contraction (bit-identical to the host policy).
+#include "adi_common.hpp"
+#include "adi_device.cuh"
+
+namespace lss_gb300 {
+
+template <typename T>
+__global__ void k_thomas_lu_lines(int n, int lines, const T *__restrict__ lo, const T *__restrict__ dg,
+                                  const T *__restrict__ up, const T *__restrict__ rhs, const T *__restrict__ blo,
+                                  const T *__restrict__ bhi, T *__restrict__ x, T *__restrict__ gam_scratch)
+{
+    using R = ar<true>;
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= lines) return;
+    const size_t L = static_cast<size_t>(lines);
+    const int e = n - 2;
+    const T bl = blo[l], bh = bhi[l];
+    T gam = T(0), y = T(0);
+    for (int t = 1; t <= e; ++t) {
+        const size_t o = static_cast<size_t>(t) * L + l;
+        const T a = lo[o], b = dg[o], c = up[o], f = rhs[o];
+        if (t == 1) {
+            gam = R::div(c, b);
+            y = R::div(R::sub(f, R::mul(a, bl)), b);
+        } else if (t < e) {
+            const T beta = R::sub(b, R::mul(a, gam));
+            y = R::div(R::sub(f, R::mul(a, y)), beta);
+            gam = R::div(c, beta);
+        } else {
+            const T beta = R::sub(b, R::mul(a, gam));
+            y = R::div(R::sub(R::sub(f, R::mul(c, bh)), R::mul(a, y)), beta);
+        }
+        gam_scratch[o] = gam;
+        x[o] = y;
+    }
+    T xv = y;
+    for (int t = e - 1; t >= 1; --t) {
+        const size_t o = static_cast<size_t>(t) * L + l;
+        xv = R::sub(x[o], R::mul(gam_scratch[o], xv));
+        x[o] = xv;
+    }
+    x[l] = bl;
+    x[static_cast<size_t>(n - 1) * L + l] = bh;
+}
+
+} // namespace lss_gb300
+
+using namespace lss_gb300;
+
+extern "C" int lss_tridiag_thomas_lu(int precision, int n, int lines, const void *lo, const void *diag, const void *up,
+                                     const void *rhs, const void *bnd_lo, const void *bnd_hi, void *x, void *stream)
+{
+    clear_error();
+    if (n < 4) return set_error(LSS_ADI_EINVAL, "lss_tridiag_thomas_lu: n must be >= 4");
+    if (lines < 0) return set_error(LSS_ADI_EINVAL, "lss_tridiag_thomas_lu: lines must be >= 0");
+    if (lines == 0) return LSS_ADI_OK;
+    if (!lo || !diag || !up || !rhs || !bnd_lo || !bnd_hi || !x)
+        return set_error(LSS_ADI_EINVAL, "lss_tridiag_thomas_lu: null pointer");
+    if (precision != LSS_ADI_FP64 && precision != LSS_ADI_FP32)
+        return set_error(LSS_ADI_EINVAL, "lss_tridiag_thomas_lu: unknown precision");
+    const size_t elem = precision == LSS_ADI_FP64 ? sizeof(double) : sizeof(float);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // stream-ordered scratch for the gamma factors: concurrent calls on other streams
+    // get their own buffer
+    void *scratch = nullptr;
+    LSS_CUDA_TRY(cudaMallocAsync(&scratch, static_cast<size_t>(n) * lines * elem, s), "allocating line-solver scratch");
+    const int bs = 128;
+    if (precision == LSS_ADI_FP64)
+        k_thomas_lu_lines<double><<<grid_for(lines, bs), bs, 0, s>>>(
+            n, lines, static_cast<const double *>(lo), static_cast<const double *>(diag), static_cast<const double *>(up),
+            static_cast<const double *>(rhs), static_cast<const double *>(bnd_lo), static_cast<const double *>(bnd_hi),
+            static_cast<double *>(x), static_cast<double *>(scratch));
+    else
+        k_thomas_lu_lines<float><<<grid_for(lines, bs), bs, 0, s>>>(
+            n, lines, static_cast<const float *>(lo), static_cast<const float *>(diag), static_cast<const float *>(up),
+            static_cast<const float *>(rhs), static_cast<const float *>(bnd_lo), static_cast<const float *>(bnd_hi),
+            static_cast<float *>(x), static_cast<float *>(scratch));
+    const cudaError_t launch = cudaGetLastError();
+    cudaFreeAsync(scratch, s);
+    LSS_CUDA_TRY(launch, "launching k_thomas_lu_lines");
+    return LSS_ADI_OK;
+}

@@ -1,0 +1,135 @@
+"""GPU parity of the single-instance device path (C-ABI lss_adi_create / lss_adi_forward)
+against the CPU oracle, which is bit-exact with the reference's host Thomas-LU path."""
+import numpy as np
+import pytest
+
+from cases import CONFIG1, SMALL
+from conftest import problem_pair, rel_err
+
+pytestmark = pytest.mark.gpu
+
+NU = dict(nonuniform=True, acc_point=100.0, alpha_scale=10.0, beta_scale=24.0)
+CASES = {k: v for k, v in SMALL.items() if v[0].get("solver", "tlu") == "tlu"}
+CASES.update({
+    "config1_dr_f64": (dict(CONFIG1), "f64"),
+    "config1_dr_f32": (dict(CONFIG1), "f32"),
+    "cs_f32": (dict(CONFIG1, scheme="cs", nx=64, ny=32, nt=51, **NU), "f32"),
+    "hv_f32": (dict(CONFIG1, scheme="hv", nx=45, ny=33, nt=41, **NU), "f32"),
+    "mcs_odd_f64": (dict(CONFIG1, scheme="mcs", nx=97, ny=35, nt=61, **NU), "f64"),
+    "mcs_z08_f32": (dict(CONFIG1, scheme="mcs", zeta=0.8, nx=70, ny=30, nt=31, **NU), "f32"),
+    "dr_euler_f64": (dict(CONFIG1, theta_scheme="euler", nx=129, ny=65, nt=21), "f64"),
+    "hv_theta80_fwd_f64": (dict(CONFIG1, scheme="hv", theta_scheme="theta80", forward=True, nx=50, ny=40, nt=31), "f64"),
+    "line_len4_f64": (dict(CONFIG1, scheme="mcs", nx=4, ny=5, nt=9), "f64"),
+    "wide_f64": (dict(CONFIG1, scheme="cs", nx=300, ny=6, nt=11, **NU), "f64"),
+})
+
+
+@pytest.mark.parametrize("key", sorted(CASES))
+def test_reference_arith_is_bitwise_identical_to_oracle(lss, oracle, key):
+    kw, fp = CASES[key]
+    op, pp = problem_pair(kw)
+    want = oracle.solve(op, fp)
+    s = lss.ImplicitHestonSolver(pp, precision=fp, arith="reference")
+    got, _ = s.solve()
+    assert got.dtype == want.dtype
+    assert np.array_equal(got, want), f"max rel err {rel_err(got, want):.3e}"
+
+
+@pytest.mark.parametrize("key", ["config1_dr_f64", "cs_nu_f64", "mcs_odd_f64", "hv_nu_f64", "hv_theta80_fwd_f64"])
+def test_fast_arith_within_1e10_of_oracle(lss, oracle, key):
+    kw, fp = CASES[key]
+    op, pp = problem_pair(kw)
+    want = oracle.solve(op, "f64")
+    got, _ = lss.ImplicitHestonSolver(pp, precision="f64", arith="fast").solve()
+    assert rel_err(got, want) < 1e-10
+
+
+@pytest.mark.parametrize("key", ["config1_dr_f32", "cs_f32", "mcs_nu_f32", "hv_f32"])
+def test_fast_arith_fp32_within_1e4_of_fp32_oracle(lss, oracle, key):
+    kw, fp = CASES[key]
+    op, pp = problem_pair(kw)
+    want = oracle.solve(op, "f32")
+    got, _ = lss.ImplicitHestonSolver(pp, precision="f32", arith="fast").solve()
+    assert rel_err(got, want) < 1e-4
+
+
+@pytest.mark.parametrize("arith", ["reference", "fast"])
+def test_graph_replay_equals_stream_launches(lss, arith):
+    _, pp = problem_pair(dict(CONFIG1, scheme="hv", nx=60, ny=30, nt=27, **NU))
+    s = lss.ImplicitHestonSolver(pp, precision="f64", arith=arith)
+    a, va = s.solve()
+    b, vb = s.solve(graph=True)
+    c, vc = s.solve(graph=True)
+    assert np.array_equal(a, b) and np.array_equal(b, c)
+    assert va == vb == vc
+
+
+def test_custom_payoff_and_bilinear_value(lss, oracle):
+    kw = dict(CONFIG1, scheme="mcs", nx=50, ny=30, nt=41, **NU)
+    op, pp = problem_pair(kw)
+    rng = np.random.default_rng(7)
+    payoff = rng.uniform(0.0, 50.0, size=(op.nx, op.ny))
+    want = oracle.solve(op, "f64", payoff=payoff)
+    s = lss.ImplicitHestonSolver(pp, precision="f64", arith="reference")
+    got, val = s.solve(payoff=payoff)
+    assert np.array_equal(got, want)
+    x, y = s.grid()
+    ox, oy = oracle.grid(op, "f64")
+    assert np.array_equal(x, ox) and np.array_equal(y, oy)
+    i = np.searchsorted(x, pp.eval_s) - 1
+    j = np.searchsorted(y, pp.eval_v) - 1
+    wx = (pp.eval_s - x[i]) / (x[i + 1] - x[i])
+    wy = (pp.eval_v - y[j]) / (y[j + 1] - y[j])
+    ref_val = ((1 - wx) * (1 - wy) * want[i, j] + wx * (1 - wy) * want[i + 1, j] + (1 - wx) * wy * want[i, j + 1]
+               + wx * wy * want[i + 1, j + 1])
+    assert abs(val - ref_val) <= 1e-12 * max(1.0, abs(ref_val))
+
+
+def test_fp64_tables_option_tracks_fp64_problem(lss, oracle):
+    # the reference's FP32 remaps differ from its FP64 ones; with FP64 tables the FP32
+    # device path follows the FP64 solution far more closely than the reference's FP32
+    kw = dict(CONFIG1)
+    op, pp = problem_pair(kw)
+    v64 = oracle.solve(op, "f64")
+    ref32 = oracle.solve(op, "f32")
+    pp.fp64_tables = True
+    got, _ = lss.ImplicitHestonSolver(pp, precision="f32", arith="fast").solve()
+    assert rel_err(got, v64) < rel_err(ref32, v64)
+    assert rel_err(got, v64) < 1e-3
+
+
+def thomas_numpy(lo, dg, up, rhs, blo, bhi):
+    """The reference's Thomas LU with Dirichlet ends, column-wise, numpy (IEEE, no FMA)."""
+    n, L = lo.shape
+    x = np.zeros_like(rhs)
+    e = n - 2
+    beta = dg[1].copy()
+    gam = np.zeros_like(rhs)
+    gam[1] = up[1] / beta
+    x[1] = (rhs[1] - lo[1] * blo) / beta
+    for t in range(2, e + 1):
+        beta = dg[t] - lo[t] * gam[t - 1]
+        f = rhs[t] if t < e else rhs[t] - up[t] * bhi
+        x[t] = (f - lo[t] * x[t - 1]) / beta
+        if t < e:
+            gam[t] = up[t] / beta
+    for t in range(e - 1, 0, -1):
+        x[t] = x[t] - gam[t] * x[t + 1]
+    x[0] = blo
+    x[n - 1] = bhi
+    return x
+
+
+@pytest.mark.parametrize("n,lines,fp", [(4, 1, "f64"), (37, 129, "f64"), (256, 1000, "f64"), (64, 33, "f32")])
+def test_tridiag_building_block_bitwise(lss, n, lines, fp):
+    rng = np.random.default_rng(n * 1000 + lines)
+    dt = np.float32 if fp == "f32" else np.float64
+    lo = rng.uniform(-1, 0, (n, lines)).astype(dt)
+    up = rng.uniform(-1, 0, (n, lines)).astype(dt)
+    dg = (2.5 + rng.uniform(0, 1, (n, lines))).astype(dt)
+    rhs = rng.normal(size=(n, lines)).astype(dt)
+    blo = rng.normal(size=lines).astype(dt)
+    bhi = rng.normal(size=lines).astype(dt)
+    got = lss.thomas_lu_lines(lo, dg, up, rhs, blo, bhi, precision=fp)
+    want = thomas_numpy(lo, dg, up, rhs, blo, bhi)
+    assert np.array_equal(got, want)
