@@ -1,24 +1,797 @@
-// adi_batched.cu -- batched persistent-kernel solver (lss_adi_batch_*).
+// adi_batched.cu -- many uneven ADI instances advanced by one persistent kernel.
+//
+// Each CTA pulls an instance index from a device counter (instances sorted longest
+// first), runs that instance's whole time loop with CTA barriers between the sweeps,
+// then pulls the next one.  The time-invariant line systems of every instance are
+// factorised once on the device (k_setup_s_lines / k_setup_v_lines): the time loop only
+// does the pre-scaled right-hand side, one FMA of forward recurrence and one of back
+// substitution per point, because GB300's FP64 pipe (~1.2 TFLOP/s measured) and not HBM
+// is the binding resource.  Same time-step structure as the reference
+// (implicit_heston_time_loop::run, lss_2d_general_heston_equation_implicit_kernel.hpp:150-207).
+#include <algorithm>
+#include <cmath>
+#include <memory>
+#include <numeric>
+#include <thread>
+#include <vector>
+
 #include "adi_batched.hpp"
+
+namespace lss_gb300 {
+
+// slots of the S-direction tables ([t][j] layout, n = nx*ny per slot)
+enum {
+    SL_LA = 0, SL_G, SL_WG, SL_WW, SL_WS, SL_WC, SL_WN, SL_WE,
+    SL_S2SC, SL_S2SE, SL_S2IB, SL_S2MZ, SL_X1, SL_X2, SL_X3, SL_X4, SL_X5, SL_COUNT
+};
+// slots of the v-direction tables ([t][i] layout: i fastest)
+enum { VL_LA = 0, VL_G, VL_VC, VL_VN, VL_IB, VL_COUNT };
+// per-instance 1-D arrays along S (nx each)
+enum { XB_M = 0, XB_C, XB_P, XB_2, XB_1, X_VHI, X_CHV, X_COUNT };
+// per-instance 1-D arrays along v (ny each)
+enum { Y_SLO = 0, Y_B2C, Y_CHS, Y_COUNT };
+
+struct bdesc {
+    int nx, ny, steps, scheme;
+    long long o2;  // offset of the instance in the nx*ny arenas
+    int ox, oy;    // offsets in the nx- and ny-sized arenas
+    double bnc;    // constant of the Neumann-corner boundary row
+    int i0, j0;    // bilinear cell of (eval_s, eval_v)
+    double w00, w10, w01, w11;
+};
+
+template <typename T> struct bparams {
+    const bdesc *desc;
+    const int *order;
+    int count;
+    int *counter;
+    T *U, *V, *Y1, *Y2, *Y3;          // state arenas (sum nx*ny each)
+    const T *S[SL_COUNT];             // S-direction tables
+    const T *Vt[VL_COUNT];            // v-direction tables
+    const T *X[X_COUNT];              // nx arenas
+    const T *Yv[Y_COUNT];             // ny arenas
+    const int *imap, *jmap;           // nx / ny arenas
+    double *values;                   // count
+    int *status;                      // count
+    int *final_in_v;                  // count: 1 if the final surface is in V
+};
+
+// ------------------------------------------------------------------------------------------
+// set-up: factorise the S-lines and v-lines of every instance once (double arithmetic)
+// ------------------------------------------------------------------------------------------
+struct setup_params {
+    const bdesc *desc;
+    const long long *line_start; // prefix of line counts per instance
+    int count;
+    long long total_lines;
+    const double *base;          // 7 * sum(n): M, P, Z, Mt, Pt, W, C (each arena sum(n))
+    long long total_n;
+    const double *scal;          // per instance: theta, zeta, gamma
+};
+
+template <typename T>
+__global__ void k_setup_s_lines(setup_params sp, T *S0, long long slot_stride, T *chS_arena)
+{
+    const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (g >= sp.total_lines) return;
+    int inst = 0;
+    { // binary search the instance owning global line g
+        int lo = 0, hi = sp.count - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (sp.line_start[mid] <= g) lo = mid; else hi = mid - 1;
+        }
+        inst = lo;
+    }
+    const bdesc d = sp.desc[inst];
+    const int j = 1 + static_cast<int>(g - sp.line_start[inst]);
+    const int nx = d.nx, ny = d.ny, e = nx - 2;
+    const double th = sp.scal[3 * inst], ze = sp.scal[3 * inst + 1], gm = sp.scal[3 * inst + 2];
+    const long long N = sp.total_n;
+    const double *bM = sp.base, *bP = sp.base + N, *bZ = sp.base + 2 * N, *bMt = sp.base + 3 * N,
+                 *bPt = sp.base + 4 * N, *bW = sp.base + 5 * N, *bC = sp.base + 6 * N;
+    double gam = 0.0;
+    for (int t = 1; t <= e; ++t) {
+        const long long o = d.o2 + (long long)t * ny + j;
+        const double M = bM[o], P = bP[o], Z = bZ[o], Mt = bMt[o], Pt = bPt[o], W = bW[o], C = bC[o];
+        const double a = -th * M, b = 1.0 + th * Z, c = -th * P;
+        const double beta = (t == 1) ? b : b - a * gam;
+        const double ib = 1.0 / beta;
+        if (t < e) gam = c / beta;
+        T *s = S0 + o;
+        s[SL_LA * slot_stride] = static_cast<T>(a * ib);
+        s[SL_G * slot_stride] = static_cast<T>(t < e ? gam : 0.0);
+        s[SL_WG * slot_stride] = static_cast<T>(gm * C * ib);
+        s[SL_WW * slot_stride] = static_cast<T>((1.0 - th) * M * ib);
+        s[SL_WS * slot_stride] = static_cast<T>(Mt * ib);
+        s[SL_WC * slot_stride] = static_cast<T>((1.0 - W - (1.0 - th) * Z) * ib);
+        s[SL_WN * slot_stride] = static_cast<T>(Pt * ib);
+        s[SL_WE * slot_stride] = static_cast<T>((1.0 - th) * P * ib);
+        const double sc = th * Z * ib, se = c * ib;
+        if (d.scheme == LSS_ADI_HUNDSDORFER_VERWER) {
+            // fused HV stage: rhs4 + rhs_intermed_3 expressed in Delta = Y2 - U and Y1
+            s[SL_S2SC * slot_stride] = static_cast<T>(sc + ib);
+            s[SL_S2SE * slot_stride] = static_cast<T>(se);
+            s[SL_S2IB * slot_stride] = static_cast<T>(0.0);
+            s[SL_S2MZ * slot_stride] = static_cast<T>(ze * gm * C * ib);
+            s[SL_X1 * slot_stride] = static_cast<T>(a * ib + ze * M * ib);
+            s[SL_X2 * slot_stride] = static_cast<T>(sc - ze * (W + Z) * ib);
+            s[SL_X3 * slot_stride] = static_cast<T>(se + ze * P * ib);
+            s[SL_X4 * slot_stride] = static_cast<T>(ze * Mt * ib);
+            s[SL_X5 * slot_stride] = static_cast<T>(ze * Pt * ib);
+        } else {
+            const double zt = (d.scheme == LSS_ADI_MODIFIED_CRAIG_SNEYD) ? (ze - th) : 0.0;
+            s[SL_S2SC * slot_stride] = static_cast<T>(sc);
+            s[SL_S2SE * slot_stride] = static_cast<T>(se);
+            s[SL_S2IB * slot_stride] = static_cast<T>(ib);
+            s[SL_S2MZ * slot_stride] = static_cast<T>(ze * gm * C * ib);
+            s[SL_X1 * slot_stride] = static_cast<T>(zt * M * ib);
+            s[SL_X2 * slot_stride] = static_cast<T>(-zt * (Z + W) * ib);
+            s[SL_X3 * slot_stride] = static_cast<T>(-zt * P * ib);
+            s[SL_X4 * slot_stride] = static_cast<T>(zt * Mt * ib);
+            s[SL_X5 * slot_stride] = static_cast<T>(zt * Pt * ib);
+        }
+        if (t == e) chS_arena[d.oy + j] = static_cast<T>(c * ib);
+    }
+}
+
+template <typename T>
+__global__ void k_setup_v_lines(setup_params sp, T *V0, long long slot_stride, T *chV_arena)
+{
+    const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (g >= sp.total_lines) return;
+    int lo = 0, hi = sp.count - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (sp.line_start[mid] <= g) lo = mid; else hi = mid - 1;
+    }
+    const int inst = lo;
+    const bdesc d = sp.desc[inst];
+    const int i = 1 + static_cast<int>(g - sp.line_start[inst]);
+    const int nx = d.nx, ny = d.ny, e = ny - 2;
+    const double th = sp.scal[3 * inst];
+    const long long N = sp.total_n;
+    const double *bMt = sp.base + 3 * N, *bPt = sp.base + 4 * N, *bW = sp.base + 5 * N;
+    double gam = 0.0;
+    for (int t = 1; t <= e; ++t) {
+        const long long ob = d.o2 + (long long)i * ny + t;  // base tables are [i][j]
+        const long long o = d.o2 + (long long)t * nx + i;   // v tables are [t][i]
+        const double a = -th * bMt[ob], b = 1.0 + th * bW[ob], c = -th * bPt[ob];
+        const double beta = (t == 1) ? b : b - a * gam;
+        const double ib = 1.0 / beta;
+        if (t < e) gam = c / beta;
+        T *s = V0 + o;
+        s[VL_LA * slot_stride] = static_cast<T>(a * ib);
+        s[VL_G * slot_stride] = static_cast<T>(t < e ? gam : 0.0);
+        s[VL_VC * slot_stride] = static_cast<T>(th * bW[ob] * ib);
+        s[VL_VN * slot_stride] = static_cast<T>(c * ib);
+        s[VL_IB * slot_stride] = static_cast<T>(ib);
+        if (t == e) chV_arena[d.ox + i] = static_cast<T>(c * ib);
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// the persistent time-loop kernel
+// ------------------------------------------------------------------------------------------
+template <typename T> struct inst_view {
+    int nx, ny, e_s, e_v;
+    long long o2;
+    T *U, *V, *Y1, *Y2, *Y3;
+    const T *S[SL_COUNT];
+    const T *Vt[VL_COUNT];
+    const T *X[X_COUNT];
+    const T *Yv[Y_COUNT];
+    const int *imap, *jmap;
+};
+
+template <typename T> __device__ __forceinline__ T ldg(const T *p) { return __ldg(p); }
+
+// boundary#1: the v = v_lo column, explicit (explicit_boundary.hpp:39-84); result in smem
+template <typename T, int BS>
+__device__ __forceinline__ void b1_stage(const inst_view<T> &v, const T *U, T *sb0, double bnc)
+{
+    const int nx = v.nx, ny = v.ny, N = nx - 1;
+    for (int i = threadIdx.x; i < nx; i += BS) {
+        T r;
+        if (i == 0) {
+            r = ldg(v.Yv[Y_SLO]);
+        } else if (i == N) {
+            r = ldg(v.X[XB_C] + i) * U[(long long)N * ny] + ldg(v.X[XB_1] + i) * U[(long long)N * ny + 1] +
+                ldg(v.X[XB_2] + i) * U[(long long)N * ny + 2] + static_cast<T>(bnc);
+        } else {
+            const long long o = (long long)i * ny;
+            r = ldg(v.X[XB_M] + i) * U[o - ny] + ldg(v.X[XB_C] + i) * U[o] + ldg(v.X[XB_P] + i) * U[o + ny] +
+                ldg(v.X[XB_2] + i) * U[o + 2] + ldg(v.X[XB_1] + i) * U[o + 1];
+        }
+        sb0[i] = r;
+    }
+}
+
+// boundary#2: row S_lo and the S_max extrapolation row (explicit_boundary.hpp:202-238)
+template <typename T, int BS> __device__ __forceinline__ void b2_stage(const inst_view<T> &v, T *Vn)
+{
+    const int nx = v.nx, ny = v.ny, lri = nx - 1;
+    const T four3 = T(4.0 / 3.0), third = T(1.0 / 3.0);
+    for (int j = threadIdx.x; j < ny; j += BS) {
+        Vn[j] = ldg(v.Yv[Y_SLO] + j);
+        const int jj = ldg(v.jmap + j);
+        Vn[(long long)lri * ny + j] =
+            four3 * Vn[(long long)(lri - 1) * ny + jj] - third * Vn[(long long)(lri - 2) * ny + jj] - ldg(v.Yv[Y_B2C] + j);
+    }
+}
+
+// S-line sweeps.  KIND 1: explicit operator on U (Y1).  KIND 2: second S stage of
+// CS/MCS/HV on U, Y1, Y2 (scheme chooses the weights).  Thread per line j; every access
+// of a warp is one coalesced row segment.
+template <typename T, int BS, int KIND>
+__device__ __forceinline__ void s_stage(const inst_view<T> &v, int scheme, const T *U, const T *Y1, const T *Y2, T *Y)
+{
+    const int nx = v.nx, ny = v.ny, e = v.e_s;
+    for (int j = 1 + threadIdx.x; j <= ny - 2; j += BS) {
+        const int jj = ldg(v.jmap + j);
+        const T lo = U[jj], hi = U[(long long)(nx - 1) * ny + jj];
+        T y = lo;
+        if constexpr (KIND == 1) {
+            // sliding 3x3 window of U
+            T u0m = U[j - 1], u0c = U[j], u0p = U[j + 1];
+            T u1m = U[ny + j - 1], u1c = U[ny + j], u1p = U[ny + j + 1];
+            for (int t = 1; t <= e; ++t) {
+                const long long o = (long long)t * ny + j;
+                const T u2m = U[o + ny - 1], u2c = U[o + ny], u2p = U[o + ny + 1];
+                const T mix = (u0m - u0p) + (u2p - u2m);
+                T f = ldg(v.S[SL_WG] + o) * mix;
+                f += ldg(v.S[SL_WW] + o) * u0c;
+                f += ldg(v.S[SL_WS] + o) * u1m;
+                f += ldg(v.S[SL_WC] + o) * u1c;
+                f += ldg(v.S[SL_WN] + o) * u1p;
+                f += ldg(v.S[SL_WE] + o) * u2c;
+                y = f - ldg(v.S[SL_LA] + o) * y;
+                if (t == e) y -= ldg(v.Yv[Y_CHS] + j) * hi;
+                Y[o] = y;
+                u0m = u1m; u0c = u1c; u0p = u1p;
+                u1m = u2m; u1c = u2c; u1p = u2p;
+            }
+        } else {
+            // windows: U centre column, Y1 centre column, Delta = Y2 - U 3x3
+            T uc0 = U[j], uc1 = U[ny + j];
+            T y10 = Y1[j], y11 = Y1[ny + j];
+            T d0m = Y2[j - 1] - U[j - 1], d0c = Y2[j] - uc0, d0p = Y2[j + 1] - U[j + 1];
+            T d1m = Y2[ny + j - 1] - U[ny + j - 1], d1c = Y2[ny + j] - uc1, d1p = Y2[ny + j + 1] - U[ny + j + 1];
+            for (int t = 1; t <= e; ++t) {
+                const long long o = (long long)t * ny + j;
+                const T uc2 = U[o + ny];
+                const T y12 = Y1[o + ny];
+                const T d2m = Y2[o + ny - 1] - U[o + ny - 1];
+                const T d2c = Y2[o + ny] - uc2;
+                const T d2p = Y2[o + ny + 1] - U[o + ny + 1];
+                const T mix = (d0m - d0p) + (d2p - d2m);
+                T f;
+                if (scheme == LSS_ADI_HUNDSDORFER_VERWER) {
+                    f = ldg(v.S[SL_LA] + o) * y10;
+                    f += ldg(v.S[SL_S2SC] + o) * y11;
+                    f += ldg(v.S[SL_S2SE] + o) * y12;
+                    f += ldg(v.S[SL_S2MZ] + o) * mix;
+                    f += ldg(v.S[SL_X1] + o) * d0c;
+                    f += ldg(v.S[SL_X2] + o) * d1c;
+                    f += ldg(v.S[SL_X3] + o) * d2c;
+                    f += ldg(v.S[SL_X4] + o) * d1m;
+                    f += ldg(v.S[SL_X5] + o) * d1p;
+                } else {
+                    f = ldg(v.S[SL_LA] + o) * uc0;
+                    f += ldg(v.S[SL_S2SC] + o) * uc1;
+                    f += ldg(v.S[SL_S2SE] + o) * uc2;
+                    f += ldg(v.S[SL_S2IB] + o) * y11;
+                    f += ldg(v.S[SL_S2MZ] + o) * mix;
+                    if (scheme == LSS_ADI_MODIFIED_CRAIG_SNEYD) {
+                        f += ldg(v.S[SL_X1] + o) * d0c;
+                        f += ldg(v.S[SL_X2] + o) * d1c;
+                        f += ldg(v.S[SL_X3] + o) * d2c;
+                        f += ldg(v.S[SL_X4] + o) * d1m;
+                        f += ldg(v.S[SL_X5] + o) * d1p;
+                    }
+                }
+                y = f - ldg(v.S[SL_LA] + o) * y;
+                if (t == e) y -= ldg(v.Yv[Y_CHS] + j) * hi;
+                Y[o] = y;
+                uc0 = uc1; uc1 = uc2;
+                y10 = y11; y11 = y12;
+                d0m = d1m; d0c = d1c; d0p = d1p;
+                d1m = d2m; d1c = d2c; d1p = d2p;
+            }
+        }
+        T x = y;
+        for (int t = e - 1; t >= 1; --t) {
+            const long long o = (long long)t * ny + j;
+            x = Y[o] - ldg(v.S[SL_G] + o) * x;
+            Y[o] = x;
+        }
+        Y[j] = lo;
+        Y[(long long)(nx - 1) * ny + j] = hi;
+    }
+}
+
+// v-line sweep: line i reads row i of `in` (t-1, t, t+1) and `inh` (t); tables are [t][i].
+template <typename T, int BS>
+__device__ __forceinline__ void v_stage(const inst_view<T> &v, const T *in, const T *inh, const T *sb0, T *out)
+{
+    const int nx = v.nx, ny = v.ny, e = v.e_v;
+    for (int i = 1 + threadIdx.x; i <= nx - 2; i += BS) {
+        const int ii = ldg(v.imap + i);
+        const T lo = sb0[ii];
+        const T hi = ldg(v.X[X_VHI] + ii);
+        const long long row = (long long)i * ny;
+        T a0 = in[row], a1 = in[row + 1];
+        T y = lo;
+        for (int t = 1; t <= e; ++t) {
+            const long long ot = (long long)t * nx + i;
+            const T a2 = in[row + t + 1];
+            T f = ldg(v.Vt[VL_LA] + ot) * a0;
+            f += ldg(v.Vt[VL_VC] + ot) * a1;
+            f += ldg(v.Vt[VL_VN] + ot) * a2;
+            f += ldg(v.Vt[VL_IB] + ot) * inh[row + t];
+            y = f - ldg(v.Vt[VL_LA] + ot) * y;
+            if (t == e) y -= ldg(v.X[X_CHV] + i) * hi;
+            out[row + t] = y;
+            a0 = a1; a1 = a2;
+        }
+        T x = y;
+        for (int t = e - 1; t >= 1; --t) {
+            x = out[row + t] - ldg(v.Vt[VL_G] + (long long)t * nx + i) * x;
+            out[row + t] = x;
+        }
+        out[row] = lo;
+        out[row + ny - 1] = hi;
+    }
+}
+
+template <typename T, int BS> __global__ void __launch_bounds__(BS) k_batch_forward(bparams<T> p)
+{
+    __shared__ int s_idx;
+    __shared__ int s_bad;
+    __shared__ T sb0[256];
+    while (true) {
+        if (threadIdx.x == 0) s_idx = atomicAdd(p.counter, 1);
+        __syncthreads();
+        const int k = s_idx;
+        __syncthreads();
+        if (k >= p.count) break;
+        const int inst = p.order[k];
+        const bdesc d = p.desc[inst];
+        inst_view<T> v;
+        v.nx = d.nx;
+        v.ny = d.ny;
+        v.e_s = d.nx - 2;
+        v.e_v = d.ny - 2;
+        v.o2 = d.o2;
+#pragma unroll
+        for (int s = 0; s < SL_COUNT; ++s) v.S[s] = p.S[s] + d.o2;
+#pragma unroll
+        for (int s = 0; s < VL_COUNT; ++s) v.Vt[s] = p.Vt[s] + d.o2;
+#pragma unroll
+        for (int s = 0; s < X_COUNT; ++s) v.X[s] = p.X[s] + d.ox;
+#pragma unroll
+        for (int s = 0; s < Y_COUNT; ++s) v.Yv[s] = p.Yv[s] + d.oy;
+        v.imap = p.imap + d.ox;
+        v.jmap = p.jmap + d.oy;
+        T *U = p.U + d.o2, *Vn = p.V + d.o2, *Y1 = p.Y1 + d.o2, *Y2 = p.Y2 + d.o2, *Y3 = p.Y3 + d.o2;
+        for (int step = 0; step < d.steps; ++step) {
+            b1_stage<T, BS>(v, U, sb0, d.bnc);
+            s_stage<T, BS, 1>(v, d.scheme, U, nullptr, nullptr, Y1);
+            __syncthreads();
+            if (d.scheme == LSS_ADI_DOUGLAS_RACHFORD) {
+                v_stage<T, BS>(v, U, Y1, sb0, Vn);
+            } else {
+                v_stage<T, BS>(v, U, Y1, sb0, Y2);
+                __syncthreads();
+                s_stage<T, BS, 2>(v, d.scheme, U, Y1, Y2, Y3);
+                __syncthreads();
+                if (d.scheme == LSS_ADI_HUNDSDORFER_VERWER)
+                    v_stage<T, BS>(v, Y2, Y3, sb0, Vn);
+                else
+                    v_stage<T, BS>(v, U, Y3, sb0, Vn);
+            }
+            __syncthreads();
+            b2_stage<T, BS>(v, Vn);
+            __syncthreads();
+            T *tmp = U;
+            U = Vn;
+            Vn = tmp;
+        }
+        // value at (eval_s, eval_v) and a finiteness check of the final surface
+        if (threadIdx.x == 0) s_bad = 0;
+        __syncthreads();
+        const long long n = (long long)d.nx * d.ny;
+        int bad = 0;
+        for (long long q = threadIdx.x; q < n; q += BS) bad |= !isfinite(static_cast<double>(U[q]));
+        if (bad) atomicOr(&s_bad, 1);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const long long o = (long long)d.i0 * d.ny + d.j0;
+            p.values[inst] = d.w00 * static_cast<double>(U[o]) + d.w10 * static_cast<double>(U[o + d.ny]) +
+                             d.w01 * static_cast<double>(U[o + 1]) + d.w11 * static_cast<double>(U[o + d.ny + 1]);
+            p.status[inst] = s_bad;
+            p.final_in_v[inst] = d.steps & 1;
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// host side
+// ------------------------------------------------------------------------------------------
+template <typename T> struct batch_typed {
+    int count = 0;
+    std::vector<bdesc> desc;
+    std::vector<int> order;
+    std::vector<long long> gps;
+    long long total_n = 0, total_x = 0, total_y = 0;
+    dbuf<bdesc> d_desc;
+    dbuf<int> d_order, d_counter, d_status, d_final, d_imap, d_jmap;
+    dbuf<double> d_values;
+    dbuf<T> state, stab, vtab, xarena, yarena;
+    std::vector<std::vector<T>> payoff_host;
+    dbuf<T> d_payoff; // concatenated initial conditions (sum n)
+    int grid_blocks = 0;
+    long long launches = 0;
+    cudaGraphExec_t graph = nullptr;
+    int graph_mode = -1;
+
+    ~batch_typed()
+    {
+        if (graph) cudaGraphExecDestroy(graph);
+    }
+
+    bparams<T> params()
+    {
+        bparams<T> p{};
+        p.desc = d_desc.p;
+        p.order = d_order.p;
+        p.count = count;
+        p.counter = d_counter.p;
+        p.U = state.p;
+        p.V = state.p + total_n;
+        p.Y1 = state.p + 2 * total_n;
+        p.Y2 = state.p + 3 * total_n;
+        p.Y3 = state.p + 4 * total_n;
+        for (int s = 0; s < SL_COUNT; ++s) p.S[s] = stab.p + s * total_n;
+        for (int s = 0; s < VL_COUNT; ++s) p.Vt[s] = vtab.p + s * total_n;
+        for (int s = 0; s < X_COUNT; ++s) p.X[s] = xarena.p + s * total_x;
+        for (int s = 0; s < Y_COUNT; ++s) p.Yv[s] = yarena.p + s * total_y;
+        p.imap = d_imap.p;
+        p.jmap = d_jmap.p;
+        p.values = d_values.p;
+        p.status = d_status.p;
+        p.final_in_v = d_final.p;
+        return p;
+    }
+
+    int create(const lss_adi_problem *ps, int n);
+    int enqueue(int mode, cudaStream_t s);
+    int run(int mode, cudaStream_t s, bool use_graph);
+};
+
+template <typename T> int batch_typed<T>::create(const lss_adi_problem *ps, int n)
+{
+    count = n;
+    desc.resize(n);
+    gps.resize(n);
+    long long on = 0, ox = 0, oy = 0;
+    for (int k = 0; k < n; ++k) {
+        desc[k].nx = ps[k].nx;
+        desc[k].ny = ps[k].ny;
+        desc[k].steps = ps[k].nt - 1;
+        desc[k].scheme = ps[k].scheme;
+        desc[k].o2 = on;
+        desc[k].ox = static_cast<int>(ox);
+        desc[k].oy = static_cast<int>(oy);
+        gps[k] = static_cast<long long>(ps[k].nx) * ps[k].ny * (ps[k].nt - 1);
+        on += static_cast<long long>(ps[k].nx) * ps[k].ny;
+        ox += ps[k].nx;
+        oy += ps[k].ny;
+    }
+    total_n = on;
+    total_x = ox;
+    total_y = oy;
+    if (ox > (1LL << 31) || oy > (1LL << 31)) return set_error(LSS_ADI_EINVAL, "batch too large");
+
+    // host tables in the reference arithmetic, in parallel over instances
+    std::vector<double> base(7 * static_cast<size_t>(total_n));
+    std::vector<T> xh(X_COUNT * static_cast<size_t>(total_x)), yh(Y_COUNT * static_cast<size_t>(total_y));
+    std::vector<int> imh(total_x), jmh(total_y);
+    std::vector<double> scal(3 * static_cast<size_t>(n));
+    std::vector<T> pay(static_cast<size_t>(total_n));
+    const unsigned nthr = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+    std::vector<std::thread> pool;
+    std::vector<int> errs(nthr, 0);
+    for (unsigned w = 0; w < nthr; ++w) {
+        pool.emplace_back([&, w]() {
+            try {
+                for (int k = static_cast<int>(w); k < n; k += static_cast<int>(nthr)) {
+                    instance_tables<T> tt;
+                    build_tables_for<T>(ps[k], tt);
+                    const bdesc &d = desc[k];
+                    const size_t nn = static_cast<size_t>(d.nx) * d.ny;
+                    for (int s = 0; s < 7; ++s)
+                        for (size_t q = 0; q < nn; ++q)
+                            base[s * static_cast<size_t>(total_n) + d.o2 + q] = static_cast<double>(tt.coef[s * nn + q]);
+                    std::copy(tt.payoff.begin(), tt.payoff.end(), pay.begin() + d.o2);
+                    const double th = tt.sc.theta, ni = tt.sc.ni, dl = tt.sc.delta, rk = tt.sc.rho;
+                    scal[3 * k] = th;
+                    scal[3 * k + 1] = static_cast<double>(tt.sc.zeta);
+                    scal[3 * k + 2] = static_cast<double>(tt.sc.gamma);
+                    for (int i = 0; i < d.nx; ++i) {
+                        const double D = tt.coef_v0[i], E = tt.coef_v0[d.nx + i], F = tt.coef_v0[2 * d.nx + i];
+                        xh[XB_M * total_x + d.ox + i] = static_cast<T>(-dl * D);
+                        xh[XB_C * total_x + d.ox + i] = static_cast<T>(1.0 - 3.0 * ni * E + rk * F);
+                        xh[XB_P * total_x + d.ox + i] = static_cast<T>(dl * D);
+                        xh[XB_2 * total_x + d.ox + i] = static_cast<T>(-ni * E);
+                        xh[XB_1 * total_x + d.ox + i] = static_cast<T>(4.0 * ni * E);
+                        xh[X_VHI * total_x + d.ox + i] = tt.v_hi[i];
+                        imh[d.ox + i] = tt.imap[i];
+                    }
+                    const double h1 = tt.sc.h1;
+                    for (int j = 0; j < d.ny; ++j) {
+                        yh[Y_SLO * total_y + d.oy + j] = tt.s_lo[j];
+                        yh[Y_B2C * total_y + d.oy + j] = static_cast<T>(2.0 * h1 * static_cast<double>(tt.s_hi_neu[j]) / 3.0);
+                        jmh[d.oy + j] = tt.jmap[j];
+                    }
+                    const double DN = tt.coef_v0[d.nx - 1];
+                    desc[k].bnc = -dl * (2.0 * h1 * static_cast<double>(tt.s_hi_neu[0])) * DN;
+                    const bilinear b = make_bilinear(tt.x.data(), d.nx, tt.y.data(), d.ny, ps[k].eval_s, ps[k].eval_v);
+                    desc[k].i0 = b.i0;
+                    desc[k].j0 = b.j0;
+                    desc[k].w00 = b.w00;
+                    desc[k].w10 = b.w10;
+                    desc[k].w01 = b.w01;
+                    desc[k].w11 = b.w11;
+                }
+            } catch (...) {
+                errs[w] = 1;
+            }
+        });
+    }
+    for (auto &t : pool) t.join();
+    for (int e : errs)
+        if (e) return set_error(LSS_ADI_ENOMEM, "batch: host table construction failed");
+
+    // longest instances first
+    order.resize(n);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return gps[a] > gps[b]; });
+
+    LSS_CUDA_TRY(d_desc.alloc(n), "batch: allocating descriptors");
+    LSS_CUDA_TRY(d_desc.upload(desc.data(), n), "batch: uploading descriptors");
+    LSS_CUDA_TRY(d_order.alloc(n), "batch: allocating order");
+    LSS_CUDA_TRY(d_order.upload(order.data(), n), "batch: uploading order");
+    LSS_CUDA_TRY(d_counter.alloc(1), "batch: allocating counter");
+    LSS_CUDA_TRY(d_status.alloc(n), "batch: allocating status");
+    LSS_CUDA_TRY(d_final.alloc(n), "batch: allocating flags");
+    LSS_CUDA_TRY(d_values.alloc(n), "batch: allocating values");
+    LSS_CUDA_TRY(d_imap.alloc(total_x), "batch: allocating remaps");
+    LSS_CUDA_TRY(d_imap.upload(imh.data(), total_x), "batch: uploading remaps");
+    LSS_CUDA_TRY(d_jmap.alloc(total_y), "batch: allocating remaps");
+    LSS_CUDA_TRY(d_jmap.upload(jmh.data(), total_y), "batch: uploading remaps");
+    LSS_CUDA_TRY(xarena.alloc(X_COUNT * total_x), "batch: allocating S boundary arrays");
+    LSS_CUDA_TRY(yarena.alloc(Y_COUNT * total_y), "batch: allocating v boundary arrays");
+    LSS_CUDA_TRY(state.alloc(5 * total_n), "batch: allocating state");
+    LSS_CUDA_TRY(cudaMemset(state.p, 0, state.n * sizeof(T)), "batch: clearing state");
+    LSS_CUDA_TRY(d_payoff.alloc(total_n), "batch: allocating initial conditions");
+    LSS_CUDA_TRY(d_payoff.upload(pay.data(), total_n), "batch: uploading initial conditions");
+    LSS_CUDA_TRY(stab.alloc(SL_COUNT * total_n), "batch: allocating S-line tables");
+    LSS_CUDA_TRY(vtab.alloc(VL_COUNT * total_n), "batch: allocating v-line tables");
+
+    // factorise on the device from the base tables
+    {
+        dbuf<double> d_base, d_scal;
+        dbuf<long long> d_ls;
+        dbuf<bdesc> dd;
+        LSS_CUDA_TRY(d_base.alloc(base.size()), "batch: allocating base tables");
+        LSS_CUDA_TRY(d_base.upload(base.data(), base.size()), "batch: uploading base tables");
+        LSS_CUDA_TRY(d_scal.alloc(scal.size()), "batch: allocating scalars");
+        LSS_CUDA_TRY(d_scal.upload(scal.data(), scal.size()), "batch: uploading scalars");
+        LSS_CUDA_TRY(cudaMemcpy(xarena.p, xh.data(), xh.size() * sizeof(T), cudaMemcpyHostToDevice), "batch: x arena");
+        LSS_CUDA_TRY(cudaMemcpy(yarena.p, yh.data(), yh.size() * sizeof(T), cudaMemcpyHostToDevice), "batch: y arena");
+        LSS_CUDA_TRY(d_ls.alloc(n), "batch: line offsets");
+        setup_params sp{};
+        sp.desc = d_desc.p;
+        sp.count = n;
+        sp.base = d_base.p;
+        sp.total_n = total_n;
+        sp.scal = d_scal.p;
+        sp.line_start = d_ls.p;
+        // S lines: ny - 2 per instance
+        std::vector<long long> ls(n);
+        long long acc = 0;
+        for (int k = 0; k < n; ++k) { ls[k] = acc; acc += desc[k].ny - 2; }
+        LSS_CUDA_TRY(d_ls.upload(ls.data(), n), "batch: line offsets");
+        sp.total_lines = acc;
+        k_setup_s_lines<T><<<grid_for(acc, 128), 128>>>(sp, stab.p, total_n, yarena.p + Y_CHS * total_y);
+        LSS_CUDA_TRY(cudaGetLastError(), "batch: launching S-line set-up");
+        LSS_CUDA_TRY(cudaDeviceSynchronize(), "batch: S-line set-up");
+        acc = 0;
+        for (int k = 0; k < n; ++k) { ls[k] = acc; acc += desc[k].nx - 2; }
+        LSS_CUDA_TRY(d_ls.upload(ls.data(), n), "batch: line offsets");
+        sp.total_lines = acc;
+        k_setup_v_lines<T><<<grid_for(acc, 128), 128>>>(sp, vtab.p, total_n, xarena.p + X_CHV * total_x);
+        LSS_CUDA_TRY(cudaGetLastError(), "batch: launching v-line set-up");
+        LSS_CUDA_TRY(cudaDeviceSynchronize(), "batch: v-line set-up");
+    }
+    int dev = 0, sms = 0, per_sm = 0;
+    LSS_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
+    LSS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
+    LSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_forward<T, 64>, 64, 0), "occupancy");
+    grid_blocks = std::max(1, std::min(sms * std::max(1, std::min(per_sm, 8)), n));
+    return LSS_ADI_OK;
+}
+
+template <typename T> int batch_typed<T>::enqueue(int mode, cudaStream_t s)
+{
+    (void)mode;
+    LSS_CUDA_TRY(cudaMemcpyAsync(state.p, d_payoff.p, total_n * sizeof(T), cudaMemcpyDeviceToDevice, s), "batch: initial state");
+    LSS_CUDA_TRY(cudaMemsetAsync(d_counter.p, 0, sizeof(int), s), "batch: counter reset");
+    k_batch_forward<T, 64><<<grid_blocks, 64, 0, s>>>(params());
+    LSS_CUDA_TRY(cudaGetLastError(), "batch: launching k_batch_forward");
+    launches = 1;
+    return LSS_ADI_OK;
+}
+
+template <typename T> int batch_typed<T>::run(int mode, cudaStream_t s, bool use_graph)
+{
+    if (!use_graph) return enqueue(mode, s);
+    if (!graph || graph_mode != mode) {
+        if (graph) cudaGraphExecDestroy(graph);
+        graph = nullptr;
+        cudaStream_t cs;
+        LSS_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "batch: capture stream");
+        LSS_CUDA_TRY(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "batch: begin capture");
+        int rc = enqueue(mode, cs);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(cs, &g);
+        cudaStreamDestroy(cs);
+        if (rc) return rc;
+        LSS_CUDA_TRY(e, "batch: end capture");
+        e = cudaGraphInstantiate(&graph, g, 0);
+        cudaGraphDestroy(g);
+        LSS_CUDA_TRY(e, "batch: instantiate graph");
+        graph_mode = mode;
+    }
+    LSS_CUDA_TRY(cudaGraphLaunch(graph, s), "batch: graph launch");
+    return LSS_ADI_OK;
+}
+
+} // namespace lss_gb300
 
 using namespace lss_gb300;
 
-struct lss_adi_batch {};
+struct lss_adi_batch {
+    int precision = LSS_ADI_FP64;
+    std::unique_ptr<batch_typed<double>> b64;
+    std::unique_ptr<batch_typed<float>> b32;
+    cudaStream_t last_stream = nullptr;
+};
+
+template <typename T>
+static int run_host_t(batch_typed<T> &bt, int mode, const void *payoffs, double *values, double *grads, cudaStream_t s)
+{
+    if (payoffs)
+        LSS_CUDA_TRY(cudaMemcpyAsync(bt.d_payoff.p, payoffs, bt.total_n * sizeof(T), cudaMemcpyHostToDevice, s),
+                     "batch: uploading payoffs");
+    int rc = bt.run(mode, s, true);
+    if (rc) return rc;
+    if (values)
+        LSS_CUDA_TRY(cudaMemcpyAsync(values, bt.d_values.p, bt.count * sizeof(double), cudaMemcpyDeviceToHost, s),
+                     "batch: reading values");
+    (void)grads;
+    LSS_CUDA_TRY(cudaStreamSynchronize(s), "batch: run");
+    return LSS_ADI_OK;
+}
+
+template <typename T> static int results_t(batch_typed<T> &bt, double *values, double *grads, int *status)
+{
+    LSS_CUDA_TRY(cudaDeviceSynchronize(), "batch: synchronising");
+    if (values) LSS_CUDA_TRY(cudaMemcpy(values, bt.d_values.p, bt.count * sizeof(double), cudaMemcpyDeviceToHost), "batch: values");
+    if (status) LSS_CUDA_TRY(cudaMemcpy(status, bt.d_status.p, bt.count * sizeof(int), cudaMemcpyDeviceToHost), "batch: status");
+    if (grads) std::fill(grads, grads + 5 * static_cast<size_t>(bt.count), 0.0);
+    return LSS_ADI_OK;
+}
+
+template <typename T> static int surface_t(batch_typed<T> &bt, int index, void *out)
+{
+    if (index < 0 || index >= bt.count) return set_error(LSS_ADI_EINVAL, "lss_adi_batch_surface: index out of range");
+    LSS_CUDA_TRY(cudaDeviceSynchronize(), "batch: synchronising");
+    int fin = 0;
+    LSS_CUDA_TRY(cudaMemcpy(&fin, bt.d_final.p + index, sizeof(int), cudaMemcpyDeviceToHost), "batch: flag");
+    const bdesc &d = bt.desc[index];
+    const T *src = bt.state.p + (fin ? bt.total_n : 0) + d.o2;
+    LSS_CUDA_TRY(cudaMemcpy(out, src, static_cast<size_t>(d.nx) * d.ny * sizeof(T), cudaMemcpyDeviceToHost), "batch: surface");
+    return LSS_ADI_OK;
+}
 
 extern "C" {
-int lss_adi_batch_create(const lss_adi_problem *, int, lss_adi_batch **b)
+
+int lss_adi_batch_create(const lss_adi_problem *problems, int count, lss_adi_batch **b)
 {
-    if (b) *b = nullptr;
-    return set_error(LSS_ADI_EUNSUPPORTED, "batch: not built yet");
+    clear_error();
+    if (!b) return set_error(LSS_ADI_EINVAL, "lss_adi_batch_create: null output");
+    *b = nullptr;
+    if (!problems || count <= 0) return set_error(LSS_ADI_EINVAL, "lss_adi_batch_create: empty batch");
+    const int prec = problems[0].precision;
+    for (int k = 0; k < count; ++k) {
+        std::string why;
+        int rc = validate_problem(problems[k], why);
+        if (rc) return set_error(rc, "lss_adi_batch_create: instance " + std::to_string(k) + ": " + why);
+        if (problems[k].precision != prec) return set_error(LSS_ADI_EINVAL, "lss_adi_batch_create: mixed precisions");
+        if (problems[k].nx > 256) return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_batch_create: nx > 256 (use lss_adi_create)");
+    }
+    std::unique_ptr<lss_adi_batch> h(new (std::nothrow) lss_adi_batch());
+    if (!h) return set_error(LSS_ADI_ENOMEM, "host allocation failed");
+    h->precision = prec;
+    int rc;
+    try {
+        if (prec == LSS_ADI_FP64) {
+            h->b64.reset(new batch_typed<double>());
+            rc = h->b64->create(problems, count);
+        } else {
+            h->b32.reset(new batch_typed<float>());
+            rc = h->b32->create(problems, count);
+        }
+    } catch (const std::bad_alloc &) {
+        return set_error(LSS_ADI_ENOMEM, "lss_adi_batch_create: host allocation failed");
+    }
+    if (rc) return rc;
+    *b = h.release();
+    return LSS_ADI_OK;
 }
-int lss_adi_batch_run(lss_adi_batch *, int, void *) { return set_error(LSS_ADI_EUNSUPPORTED, "batch: not built yet"); }
-int lss_adi_batch_graph_launch(lss_adi_batch *, int, void *) { return set_error(LSS_ADI_EUNSUPPORTED, "batch: not built yet"); }
-int lss_adi_batch_run_host(lss_adi_batch *, int, const void *, double *, double *, void *)
+
+static int batch_run(lss_adi_batch *b, int mode, void *stream, bool graph)
 {
-    return set_error(LSS_ADI_EUNSUPPORTED, "batch: not built yet");
+    clear_error();
+    if (!b) return set_error(LSS_ADI_EINVAL, "lss_adi_batch_run: null batch");
+    if (mode != 0 && mode != 1) return set_error(LSS_ADI_EINVAL, "lss_adi_batch_run: mode must be 0 or 1");
+    if (mode == 1) return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_batch_run: adjoint mode not available yet");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    b->last_stream = s;
+    return b->b64 ? b->b64->run(mode, s, graph) : b->b32->run(mode, s, graph);
 }
-int lss_adi_batch_results(lss_adi_batch *, double *, double *, int *) { return set_error(LSS_ADI_EUNSUPPORTED, "batch: not built yet"); }
-int lss_adi_batch_surface(lss_adi_batch *, int, void *) { return set_error(LSS_ADI_EUNSUPPORTED, "batch: not built yet"); }
-int lss_adi_batch_launch_count(const lss_adi_batch *) { return 0; }
+
+int lss_adi_batch_run(lss_adi_batch *b, int mode, void *stream) { return batch_run(b, mode, stream, false); }
+int lss_adi_batch_graph_launch(lss_adi_batch *b, int mode, void *stream) { return batch_run(b, mode, stream, true); }
+
+
+int lss_adi_batch_run_host(lss_adi_batch *b, int mode, const void *payoffs, double *values, double *grads, void *stream)
+{
+    clear_error();
+    if (!b) return set_error(LSS_ADI_EINVAL, "lss_adi_batch_run_host: null batch");
+    if (mode != 0 && mode != 1) return set_error(LSS_ADI_EINVAL, "lss_adi_batch_run_host: mode must be 0 or 1");
+    if (mode == 1) return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_batch_run_host: adjoint mode not available yet");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    b->last_stream = s;
+    return b->b64 ? run_host_t(*b->b64, mode, payoffs, values, grads, s)
+                  : run_host_t(*b->b32, mode, payoffs, values, grads, s);
+}
+
+
+int lss_adi_batch_results(lss_adi_batch *b, double *values, double *grads, int *status)
+{
+    clear_error();
+    if (!b) return set_error(LSS_ADI_EINVAL, "lss_adi_batch_results: null batch");
+    return b->b64 ? results_t(*b->b64, values, grads, status) : results_t(*b->b32, values, grads, status);
+}
+
+
+int lss_adi_batch_surface(lss_adi_batch *b, int index, void *out_surface)
+{
+    clear_error();
+    if (!b || !out_surface) return set_error(LSS_ADI_EINVAL, "lss_adi_batch_surface: null argument");
+    return b->b64 ? surface_t(*b->b64, index, out_surface) : surface_t(*b->b32, index, out_surface);
+}
+
+int lss_adi_batch_launch_count(const lss_adi_batch *b)
+{
+    if (!b) return 0;
+    return static_cast<int>(b->b64 ? b->b64->launches : b->b32->launches);
+}
+
 void lss_adi_batch_destroy(lss_adi_batch *b) { delete b; }
-}
+
+} // extern "C"

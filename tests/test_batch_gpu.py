@@ -1,0 +1,82 @@
+"""GPU parity of the batched persistent kernel (lss_adi_batch_*) against the CPU oracle."""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+NU = dict(nonuniform=True, alpha_scale=10.0, beta_scale=24.0)
+
+
+def mixed_batch(lss, schemes=("dr", "cs", "mcs", "hv"), seed=3, count=12):
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        K = float(rng.uniform(80, 120))
+        out.append(lss.HestonProblem(
+            kappa=float(rng.uniform(0.5, 5)), theta_v=float(rng.uniform(0.01, 0.1)), sigma=float(rng.uniform(0.1, 1)),
+            rho=float(rng.uniform(-0.95, 0)), rate=float(rng.uniform(0, 0.05)), maturity=float(rng.uniform(0.25, 2)),
+            strike=K, acc_point=K, nx=int(rng.choice([4, 17, 64, 96, 130, 256])), ny=int(rng.choice([4, 9, 32, 48, 128])),
+            nt=int(rng.integers(2, 40)), scheme=schemes[k % len(schemes)], **NU))
+    return out
+
+
+def oracle_of(oracle, p):
+    import dataclasses
+
+    return oracle.Problem(**{k: v for k, v in dataclasses.asdict(p).items()
+                             if k not in ("eval_s", "eval_v", "fp64_tables")})
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_batch_fp64_matches_oracle(lss, oracle, graph):
+    probs = mixed_batch(lss)
+    b = lss.BatchSolver(probs, precision="f64")
+    b.run(mode=0, graph=graph)
+    values, _, status = b.results()
+    assert np.all(status == 0)
+    for k, p in enumerate(probs):
+        want = oracle.solve(oracle_of(oracle, p), "f64")
+        got = b.surface(k)
+        assert rel_err(got, want) < 1e-10, (k, p.scheme, p.nx, p.ny, p.nt)
+        s = lss.ImplicitHestonSolver(p, precision="f64", arith="fast")
+        _, v = s.solve()
+        assert abs(values[k] - v) <= 1e-10 * max(1.0, abs(v))
+
+
+def test_batch_repeat_runs_are_identical(lss):
+    probs = mixed_batch(lss, seed=11, count=9)
+    b = lss.BatchSolver(probs, precision="f64")
+    b.run(0)
+    v1, _, _ = b.results()
+    s1 = [b.surface(k) for k in range(len(probs))]
+    b.run(0, graph=True)
+    b.run(0, graph=True)
+    v2, _, _ = b.results()
+    assert np.array_equal(v1, v2)
+    for k in range(len(probs)):
+        assert np.array_equal(s1[k], b.surface(k))
+
+
+def test_batch_fp32_matches_fp32_oracle(lss, oracle):
+    probs = mixed_batch(lss, schemes=("dr", "mcs", "hv"), seed=5, count=6)
+    b = lss.BatchSolver(probs, precision="f32")
+    b.run(0)
+    _, _, status = b.results()
+    for k, p in enumerate(probs):
+        want = oracle.solve(oracle_of(oracle, p), "f32")
+        assert rel_err(b.surface(k), want) < 1e-4, (k, p.scheme)
+
+
+def test_batch_config3_sample_within_1e10(lss, oracle):
+    from linear_system_solvers_gb300.batch import draw_batch
+
+    probs = draw_batch(24)
+    for p in probs:  # keep the oracle side short: truncate the time loop
+        p.nt = 21
+    b = lss.BatchSolver(probs, precision="f64")
+    b.run(0)
+    for k, p in enumerate(probs):
+        want = oracle.solve(oracle_of(oracle, p), "f64")
+        assert rel_err(b.surface(k), want) < 1e-10

@@ -32,7 +32,7 @@ def test_reference_arith_is_bitwise_identical_to_oracle(lss, oracle, key):
     s = lss.ImplicitHestonSolver(pp, precision=fp, arith="reference")
     got, _ = s.solve()
     assert got.dtype == want.dtype
-    assert np.array_equal(got, want), f"max rel err {rel_err(got, want):.3e}"
+    assert np.array_equal(got, want, equal_nan=True), f"max rel err {rel_err(got, want):.3e}"
 
 
 @pytest.mark.parametrize("key", ["config1_dr_f64", "cs_nu_f64", "mcs_odd_f64", "hv_nu_f64", "hv_theta80_fwd_f64"])
