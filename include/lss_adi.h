@@ -174,8 +174,10 @@ void lss_adi_destroy(lss_adi_handle *h);
  * work counter).  All problems share precision (FP64 or FP32); arith must be FAST. */
 int lss_adi_batch_create(const lss_adi_problem *problems, int count, lss_adi_batch **b);
 
-/* mode 0 = forward values only, 1 = forward + adjoint (values and the 5 parameter
- * sensitivities per instance).  Device-resident: inputs were uploaded by batch_create. */
+/* mode 0 = forward values only, 1 = forward + adjoint (values, the 5 parameter
+ * sensitivities and dV/d(initial condition) per instance; FP64 Heston with DR, CS or MCS).
+ * The adjoint keeps a checkpoint every ceil(sqrt(steps)) steps and recomputes each segment
+ * once.  Device-resident: inputs were uploaded by batch_create. */
 int lss_adi_batch_run(lss_adi_batch *b, int mode, void *stream);
 
 /* Captures lss_adi_batch_run(b, mode) once into a CUDA graph and launches the graph. */
@@ -194,6 +196,9 @@ int lss_adi_batch_results(lss_adi_batch *b, double *values, double *grads, int *
 
 /* Final surface of instance `index` (host buffer of its Nx*Ny, precision type). */
 int lss_adi_batch_surface(lss_adi_batch *b, int index, void *out_surface);
+
+/* dV/d(initial condition grid) of instance `index` after a mode-1 run (host, FP64, Nx*Ny). */
+int lss_adi_batch_payoff_gradient(lss_adi_batch *b, int index, void *out);
 
 /* Kernel launches made by the last lss_adi_batch_run / graph launch (own kernels only). */
 int lss_adi_batch_launch_count(const lss_adi_batch *b);

@@ -99,5 +99,11 @@ class BatchSolver:
         L.check(self.lib.lss_adi_batch_surface(self._b, int(index), out.ctypes.data))
         return out
 
+    def payoff_gradient(self, index: int) -> np.ndarray:
+        p = self.problems[index]
+        out = np.empty((p.nx, p.ny), dtype=np.float64)
+        L.check(self.lib.lss_adi_batch_payoff_gradient(self._b, int(index), out.ctypes.data))
+        return out
+
     def launch_count(self) -> int:
         return int(self.lib.lss_adi_batch_launch_count(self._b))

@@ -1,0 +1,279 @@
+// adi_adjoint.cuh -- reverse-mode (adjoint) of one ADI time step in the factorised form
+// used by the batched kernel, for Douglas-Rachford, Craig-Sneyd and modified Craig-Sneyd.
+//
+// Forward step (see adi_batched.cu): B1 -> S1 -> V1 -> S2 -> V2 -> B2, where each S/V stage
+// solves  a x_{t-1} + b x_t + c x_{t+1} = f_t  per line through the precomputed factors
+//   y_t = f_t/beta_t - la_t y_{t-1},   x_t = y_t - g_t x_{t+1}   (y_0 = lo, x_{e+1} = hi).
+// The adjoint of such a solve, given xbar_t, is
+//   z_t = xbar_t - g_{t-1} z_{t-1}          (t = 1..e)
+//   w_t = z_t - la_{t+1} w_{t+1}            (t = e..1)
+//   fbar_t(scaled) = w_t,  lobar = -la_1 w_1,  hibar = -ch w_e,
+// i.e. the transposed factorisation, one FMA per point each way.  Right-hand-side terms
+// that stay on the line are applied by the line's thread; cross-line terms (mixed
+// derivative, neighbouring lines) by a gather pass over columns.  Parameter
+// sensitivities dV/d(kappa, theta, sigma, rho, r) use, per stage and grid point,
+//   mu_t * (d f_t/dp - d a_t/dp x_{t-1} - d b_t/dp x_t - d c_t/dp x_{t+1}),  mu_t = w_t / beta_t,
+// with the Heston coefficient derivatives (all separable into 1-D tables).
+#pragma once
+// Included by adi_batched.cu inside namespace lss_gb300, after the forward stage functions.
+
+struct adj_acc {
+    // S-line sums, already scaled: r, kappa, theta, sigma, rho
+    double s[5];
+    // v-line raw sums: sum mu (dm-dn) ek, (dm-dn) et, (dm-dn) es, (2dc-dm-dn) bs, dc
+    double vk, vt, vs1, vs2, vb;
+};
+
+// B2^T: fold the S_max extrapolation row into rows nx-2 / nx-3; clear rows 0 and nx-1 of UB.
+template <int BS> __device__ __forceinline__ void adj_b2(const inst_view<double> &v, double *VB, double *UB)
+{
+    const int nx = v.nx, ny = v.ny, lri = nx - 1;
+    const double four3 = 4.0 / 3.0, third = 1.0 / 3.0;
+    for (int q = threadIdx.x; q < ny; q += BS) {
+        double add = 0.0;
+        if (__ldg(v.jmap + q) == q) add += VB[(long long)lri * ny + q];
+        if (q + 1 < ny && __ldg(v.jmap + q + 1) == q) add += VB[(long long)lri * ny + q + 1];
+        VB[(long long)(lri - 1) * ny + q] += four3 * add;
+        VB[(long long)(lri - 2) * ny + q] -= third * add;
+        UB[q] = 0.0;
+        UB[(long long)lri * ny + q] = 0.0;
+    }
+}
+
+// V-line stage adjoint.  XB: adjoint of the stage output (rows i, incl. the lo copy at t=0);
+// in/out: the stage's `in` array and its output; INB (+)= adjoint of `in`; INHB (+)= adjoint
+// of `inh`; LV (+)= adjoint of the line's lo value.
+template <int BS, bool FIRST>
+__device__ __forceinline__ void adj_v(const inst_view<double> &v, const double *in, const double *out, const double *XB,
+                                      double *INB, double *INHB, double *TMP, double *LV, adj_acc &acc)
+{
+    const int nx = v.nx, ny = v.ny, e = ny - 2;
+    for (int i = 1 + threadIdx.x; i <= nx - 2; i += BS) {
+        const long long row = (long long)i * ny;
+        double z = 0.0;
+        for (int t = 1; t <= e; ++t) {
+            const double gprev = (t > 1) ? __ldg(v.Vt[VL_G] + (long long)(t - 1) * nx + i) : 0.0;
+            z = XB[row + t] - gprev * z;
+            TMP[row + t] = z;
+        }
+        double w = 0.0, la_next = 0.0;
+        double acc_t1 = 0.0, acc_t = 0.0; // pending adjoint of in(t+1) / in(t)
+        // windows of (in - out) at t+1 and t
+        double dn = in[row + e + 1] - out[row + e + 1];
+        double dc = in[row + e] - out[row + e];
+        for (int t = e; t >= 1; --t) {
+            const long long ot = (long long)t * nx + i;
+            w = TMP[row + t] - la_next * w;
+            const double la = __ldg(v.Vt[VL_LA] + ot), vc = __ldg(v.Vt[VL_VC] + ot), vn = __ldg(v.Vt[VL_VN] + ot);
+            const double ib = __ldg(v.Vt[VL_IB] + ot);
+            const double fin = acc_t1 + vn * w; // adjoint of in(t+1) is complete
+            if (FIRST) INB[row + t + 1] = fin; else INB[row + t + 1] += fin;
+            acc_t1 = acc_t + vc * w;
+            acc_t = la * w;
+            const double mu = ib * w;
+            if (FIRST) INHB[row + t] = mu; else INHB[row + t] += mu;
+            const double dm = in[row + t - 1] - out[row + t - 1];
+            const double q = mu * (dm - dn);
+            acc.vk += q * __ldg(v.Yv[Y_EK] + t);
+            acc.vt += q * __ldg(v.Yv[Y_ET] + t);
+            acc.vs1 += q * __ldg(v.Yv[Y_ES] + t);
+            acc.vs2 += mu * (2.0 * dc - dm - dn) * __ldg(v.Yv[Y_BS] + t);
+            acc.vb += mu * dc;
+            dn = dc;
+            dc = dm;
+            la_next = la;
+        }
+        if (FIRST) { INB[row + 1] = acc_t1; INB[row] = acc_t; }
+        else { INB[row + 1] += acc_t1; INB[row] += acc_t; }
+        const double lob = -la_next * w + XB[row];
+        if (FIRST) LV[i] = lob; else LV[i] += lob;
+    }
+}
+
+// S-line stage adjoint.  KIND 1: S1 (explicit operator on U, output Y1).  KIND 2: second S
+// stage of CS/MCS (output Y3).  XB: adjoint of the stage output; FB receives the scaled
+// right-hand-side adjoint w; LS/HS the lo/hi adjoints of the line.
+template <int BS, int KIND>
+__device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d, const double *U, const double *Y1,
+                                      const double *Y2, const double *Yo, const double *XB, double *FB, double *TMP,
+                                      double *LS, double *HS, double *UB, double *Y1B, adj_acc &acc)
+{
+    const int nx = v.nx, ny = v.ny, e = nx - 2;
+    const double th = d.a_theta;
+    const double zt = (d.scheme == LSS_ADI_MODIFIED_CRAIG_SNEYD) ? (d.a_zeta - th) : 0.0;
+    for (int j = 1 + threadIdx.x; j <= ny - 2; j += BS) {
+        double z = 0.0;
+        for (int t = 1; t <= e; ++t) {
+            const long long o = (long long)t * ny + j;
+            const double gprev = (t > 1) ? __ldg(v.S[SL_G] + o - ny) : 0.0;
+            z = XB[o] - gprev * z;
+            TMP[o] = z;
+        }
+        double w = 0.0, la_next = 0.0, w_e = 0.0;
+        double acc_t1 = 0.0, acc_t = 0.0;
+        double pA = 0.0, pB = 0.0, pQ = 0.0, pD = 0.0, pE = 0.0;
+        for (int t = e; t >= 1; --t) {
+            const long long o = (long long)t * ny + j;
+            w = TMP[o] - la_next * w;
+            if (t == e) w_e = w;
+            FB[o] = w;
+            const double la = __ldg(v.S[SL_LA] + o);
+            const double ib = __ldg(v.S[SL_IB] + o);
+            const double mu = ib * w;
+            const double hx = __ldg(v.X[X_HX] + t);
+            const double Uw = U[o - ny], Uc = U[o], Ue = U[o + ny], Us = U[o - 1], Un = U[o + 1];
+            double sM, sZ, sP, sMt, sW, sPt, sC;
+            if constexpr (KIND == 1) {
+                const double omt = 1.0 - th;
+                sM = omt * Uw + th * Yo[o - ny];
+                sZ = -(omt * Uc + th * Yo[o]);
+                sP = omt * Ue + th * Yo[o + ny];
+                sMt = Us;
+                sW = -Uc;
+                sPt = Un;
+                sC = d.a_gamma * ((U[o - ny - 1] - U[o - ny + 1]) + (U[o + ny + 1] - U[o + ny - 1]));
+            } else {
+                // along-line terms of the second S stage: la U(t-1) + sc U(t) + se U(t+1) + ib Y1(t)
+                const double sc = __ldg(v.S[SL_S2SC] + o), se = __ldg(v.S[SL_S2SE] + o);
+                const double fin = acc_t1 + se * w;
+                UB[o + ny] += fin;
+                acc_t1 = acc_t + sc * w;
+                acc_t = la * w;
+                Y1B[o] = mu;
+                const double Dw = Y2[o - ny] - Uw, Dc = Y2[o] - Uc, De = Y2[o + ny] - Ue;
+                const double Ds = Y2[o - 1] - Us, Dn = Y2[o + 1] - Un;
+                sM = th * (Yo[o - ny] - Uw) + zt * Dw;
+                sZ = -th * (Yo[o] - Uc) - zt * Dc;
+                sP = th * (Yo[o + ny] - Ue) - zt * De;
+                sW = -zt * Dc;
+                sMt = zt * Ds;
+                sPt = zt * Dn;
+                const double mix = ((Y2[o - ny - 1] - U[o - ny - 1]) - (Y2[o - ny + 1] - U[o - ny + 1])) +
+                                   ((Y2[o + ny + 1] - U[o + ny + 1]) - (Y2[o + ny - 1] - U[o + ny - 1]));
+                sC = d.a_zeta * d.a_gamma * mix;
+            }
+            pA += mu * hx * (sP - sM);
+            pB += mu * (sZ + sW);
+            pQ += mu * (sPt - sMt);
+            pD += mu * (sMt + sPt + 2.0 * sW);
+            pE += mu * hx * sC;
+            la_next = la;
+        }
+        if constexpr (KIND == 2) {
+            UB[(long long)ny + j] += acc_t1;
+            UB[j] += acc_t;
+        }
+        LS[j] = -la_next * w + XB[j];
+        HS[j] = -__ldg(v.Yv[Y_CHS] + j) * w_e + XB[(long long)(nx - 1) * ny + j];
+        const double ek = __ldg(v.Yv[Y_EK] + j), et = __ldg(v.Yv[Y_ET] + j), es = __ldg(v.Yv[Y_ES] + j);
+        const double bs = __ldg(v.Yv[Y_BS] + j), hy = __ldg(v.Yv[Y_HY] + j);
+        acc.s[0] += d.a_delta * pA + d.a_halfk * pB;
+        acc.s[1] += d.a_ni * ek * pQ;
+        acc.s[2] += d.a_ni * et * pQ;
+        acc.s[3] += d.a_ni * es * pQ + d.a_betat * bs * pD + d.a_rho * hy * pE;
+        acc.s[4] += d.a_sigma * hy * pE;
+    }
+}
+
+// Gather pass over columns q: cross-line right-hand-side adjoints of an S stage into UB
+// (and Y2B for KIND 2), the lo/hi adjoints of the S lines, and for KIND 1 the adjoint of
+// the explicit v = v_lo boundary column (B1^T) with its parameter sensitivities.
+template <int BS, int KIND>
+__device__ __forceinline__ void adj_gather(const inst_view<double> &v, const bdesc &d, const double *U, const double *FB,
+                                           const double *LS, const double *HS, const double *LV, double *UB,
+                                           double *Y2B, adj_acc &acc)
+{
+    const int nx = v.nx, ny = v.ny;
+    auto F = [&](int p, int q) -> double {
+        return (p >= 1 && p <= nx - 2 && q >= 1 && q <= ny - 2) ? FB[(long long)p * ny + q] : 0.0;
+    };
+    auto W = [&](int slot, int p, int q) -> double {
+        return (p >= 1 && p <= nx - 2 && q >= 1 && q <= ny - 2) ? __ldg(v.S[slot] + (long long)p * ny + q) : 0.0;
+    };
+    // lo-value adjoint of the explicit boundary column: bbar0(i) = sum over v lines i' with imap[i'] = i
+    auto B0 = [&](int i) -> double {
+        if (i < 1 || i > nx - 2) return 0.0;
+        double s = 0.0;
+        if (__ldg(v.imap + i) == i) s += LV[i];
+        if (i + 1 <= nx - 2 && __ldg(v.imap + i + 1) == i) s += LV[i + 1];
+        return s;
+    };
+    for (int q = threadIdx.x; q < ny; q += BS) {
+        double lsum = 0.0, hsum = 0.0;
+        if (q >= 1 && q <= ny - 2 && __ldg(v.jmap + q) == q) { lsum += LS[q]; hsum += HS[q]; }
+        if (q + 1 <= ny - 2 && __ldg(v.jmap + q + 1) == q) { lsum += LS[q + 1]; hsum += HS[q + 1]; }
+        for (int p = 0; p < nx; ++p) {
+            const long long o = (long long)p * ny + q;
+            double val = 0.0;
+            if constexpr (KIND == 2) {
+                const double db = W(SL_X1, p + 1, q) * F(p + 1, q) + W(SL_X2, p, q) * F(p, q) +
+                                  W(SL_X3, p - 1, q) * F(p - 1, q) + W(SL_X4, p, q + 1) * F(p, q + 1) +
+                                  W(SL_X5, p, q - 1) * F(p, q - 1) + W(SL_S2MZ, p + 1, q + 1) * F(p + 1, q + 1) -
+                                  W(SL_S2MZ, p + 1, q - 1) * F(p + 1, q - 1) - W(SL_S2MZ, p - 1, q + 1) * F(p - 1, q + 1) +
+                                  W(SL_S2MZ, p - 1, q - 1) * F(p - 1, q - 1);
+                Y2B[o] = db;
+                val -= db;
+            } else {
+                val += W(SL_WW, p + 1, q) * F(p + 1, q) + W(SL_WE, p - 1, q) * F(p - 1, q) +
+                       W(SL_WS, p, q + 1) * F(p, q + 1) + W(SL_WN, p, q - 1) * F(p, q - 1) + W(SL_WC, p, q) * F(p, q) +
+                       W(SL_WG, p + 1, q + 1) * F(p + 1, q + 1) - W(SL_WG, p + 1, q - 1) * F(p + 1, q - 1) -
+                       W(SL_WG, p - 1, q + 1) * F(p - 1, q + 1) + W(SL_WG, p - 1, q - 1) * F(p - 1, q - 1);
+                if (q <= 2) {
+                    if (q == 0) {
+                        val += (p + 1 <= nx - 2 ? __ldg(v.X[XB_M] + p + 1) * B0(p + 1) : 0.0) +
+                               __ldg(v.X[XB_C] + p) * B0(p) + (p >= 1 ? __ldg(v.X[XB_P] + p - 1) * B0(p - 1) : 0.0);
+                        if (p >= 1 && p <= nx - 2) {
+                            const double bb = B0(p);
+                            if (bb != 0.0) {
+                                const double u0 = U[o], u1 = U[o + 1], u2 = U[o + 2];
+                                const double um = U[o - ny], up = U[o + ny];
+                                const double ee = d.a_ni * bb * (4.0 * u1 - 3.0 * u0 - u2);
+                                acc.s[0] += bb * (d.a_delta * __ldg(v.X[X_HX] + p) * (up - um) - d.a_k * u0);
+                                acc.s[1] += ee * __ldg(v.Yv[Y_EK]);
+                                acc.s[2] += ee * __ldg(v.Yv[Y_ET]);
+                                acc.s[3] += ee * __ldg(v.Yv[Y_ES]);
+                            }
+                        }
+                    } else if (q == 1) {
+                        val += __ldg(v.X[XB_1] + p) * B0(p);
+                    } else {
+                        val += __ldg(v.X[XB_2] + p) * B0(p);
+                    }
+                }
+            }
+            if (p == 0) val += lsum;
+            if (p == nx - 1) val += hsum;
+            UB[o] += val;
+        }
+    }
+}
+
+// Adjoint of one time step: VB = adjoint of the step output (modified in place), UB receives
+// the adjoint of the step input.  U/Y1/Y2/Y3/Vo: the step's input, stage outputs and output.
+template <int BS>
+__device__ __forceinline__ void adj_step(const inst_view<double> &v, const bdesc &d, const double *U, const double *Y1,
+                                         const double *Y2, const double *Y3, const double *Vo, double *VB, double *UB,
+                                         double *Y1B, double *Y2B, double *Y3B, double *FB, double *TMP, double *LV,
+                                         double *LS, double *HS, adj_acc &acc)
+{
+    adj_b2<BS>(v, VB, UB);
+    __syncthreads();
+    if (d.scheme == LSS_ADI_DOUGLAS_RACHFORD) {
+        adj_v<BS, true>(v, U, Vo, VB, UB, Y1B, TMP, LV, acc);
+        __syncthreads();
+    } else {
+        adj_v<BS, true>(v, U, Vo, VB, UB, Y3B, TMP, LV, acc);
+        __syncthreads();
+        adj_s<BS, 2>(v, d, U, Y1, Y2, Y3, Y3B, FB, TMP, LS, HS, UB, Y1B, acc);
+        __syncthreads();
+        adj_gather<BS, 2>(v, d, U, FB, LS, HS, LV, UB, Y2B, acc);
+        __syncthreads();
+        adj_v<BS, false>(v, U, Y2, Y2B, UB, Y1B, TMP, LV, acc);
+        __syncthreads();
+    }
+    adj_s<BS, 1>(v, d, U, Y1, Y2, Y1, Y1B, FB, TMP, LS, HS, UB, Y1B, acc);
+    __syncthreads();
+    adj_gather<BS, 1>(v, d, U, FB, LS, HS, LV, UB, Y2B, acc);
+    __syncthreads();
+}
+

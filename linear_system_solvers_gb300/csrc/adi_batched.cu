@@ -12,7 +12,9 @@
 #include <cmath>
 #include <memory>
 #include <numeric>
+#include <string>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 #include "adi_batched.hpp"
@@ -22,14 +24,16 @@ namespace lss_gb300 {
 // slots of the S-direction tables ([t][j] layout, n = nx*ny per slot)
 enum {
     SL_LA = 0, SL_G, SL_WG, SL_WW, SL_WS, SL_WC, SL_WN, SL_WE,
-    SL_S2SC, SL_S2SE, SL_S2IB, SL_S2MZ, SL_X1, SL_X2, SL_X3, SL_X4, SL_X5, SL_COUNT
+    SL_S2SC, SL_S2SE, SL_S2IB, SL_S2MZ, SL_X1, SL_X2, SL_X3, SL_X4, SL_X5, SL_IB, SL_COUNT
 };
 // slots of the v-direction tables ([t][i] layout: i fastest)
 enum { VL_LA = 0, VL_G, VL_VC, VL_VN, VL_IB, VL_COUNT };
 // per-instance 1-D arrays along S (nx each)
-enum { XB_M = 0, XB_C, XB_P, XB_2, XB_1, X_VHI, X_CHV, X_COUNT };
+// X_HX: X/A = dd^/dr (adjoint only)
+enum { XB_M = 0, XB_C, XB_P, XB_2, XB_1, X_VHI, X_CHV, X_HX, X_COUNT };
 // per-instance 1-D arrays along v (ny each)
-enum { Y_SLO = 0, Y_B2C, Y_CHS, Y_COUNT };
+// Y_HY = v/B, Y_BS = db^/dsigma, Y_EK = de^/dkappa, Y_ET = de^/dtheta, Y_ES = de^/dsigma (adjoint only)
+enum { Y_SLO = 0, Y_B2C, Y_CHS, Y_HY, Y_BS, Y_EK, Y_ET, Y_ES, Y_COUNT };
 
 struct bdesc {
     int nx, ny, steps, scheme;
@@ -38,6 +42,10 @@ struct bdesc {
     double bnc;    // constant of the Neumann-corner boundary row
     int i0, j0;    // bilinear cell of (eval_s, eval_v)
     double w00, w10, w01, w11;
+    int ck;        // checkpoint interval of the adjoint (steps)
+    int pad_;
+    // scalars of the parameter derivatives: delta, k/2, ni, beta~, sigma, rho, theta, zeta, gamma, k
+    double a_delta, a_halfk, a_ni, a_betat, a_sigma, a_rho, a_theta, a_zeta, a_gamma, a_k;
 };
 
 template <typename T> struct bparams {
@@ -54,6 +62,11 @@ template <typename T> struct bparams {
     double *values;                   // count
     int *status;                      // count
     int *final_in_v;                  // count: 1 if the final surface is in V
+    // forward + adjoint (mode 1, FP64 only)
+    double *grads;                    // 5 * count: d value / d(kappa, theta, sigma, rho, r)
+    double *ws;                       // per-CTA adjoint workspace
+    long long ws_stride;              // doubles per CTA
+    const T *payoff;                  // sum nx*ny initial conditions
 };
 
 // ------------------------------------------------------------------------------------------
@@ -131,6 +144,7 @@ __global__ void k_setup_s_lines(setup_params sp, T *S0, long long slot_stride, T
             s[SL_X4 * slot_stride] = static_cast<T>(zt * Mt * ib);
             s[SL_X5 * slot_stride] = static_cast<T>(zt * Pt * ib);
         }
+        s[SL_IB * slot_stride] = static_cast<T>(ib);
         if (t == e) chS_arena[d.oy + j] = static_cast<T>(c * ib);
     }
 }
@@ -344,6 +358,52 @@ __device__ __forceinline__ void v_stage(const inst_view<T> &v, const T *in, cons
     }
 }
 
+template <typename T> __device__ __forceinline__ inst_view<T> make_view(const bparams<T> &p, const bdesc &d)
+{
+    inst_view<T> v;
+    v.nx = d.nx;
+    v.ny = d.ny;
+    v.e_s = d.nx - 2;
+    v.e_v = d.ny - 2;
+    v.o2 = d.o2;
+#pragma unroll
+    for (int s = 0; s < SL_COUNT; ++s) v.S[s] = p.S[s] + d.o2;
+#pragma unroll
+    for (int s = 0; s < VL_COUNT; ++s) v.Vt[s] = p.Vt[s] + d.o2;
+#pragma unroll
+    for (int s = 0; s < X_COUNT; ++s) v.X[s] = p.X[s] + d.ox;
+#pragma unroll
+    for (int s = 0; s < Y_COUNT; ++s) v.Yv[s] = p.Yv[s] + d.oy;
+    v.imap = p.imap + d.ox;
+    v.jmap = p.jmap + d.oy;
+    return v;
+}
+
+// One time step U -> Vn with stage outputs in Y1, Y2, Y3; ends with a CTA barrier.
+template <typename T, int BS>
+__device__ __forceinline__ void fwd_step(const inst_view<T> &v, int scheme, const T *U, T *Y1, T *Y2, T *Y3, T *Vn,
+                                         T *sb0, double bnc)
+{
+    b1_stage<T, BS>(v, U, sb0, bnc);
+    s_stage<T, BS, 1>(v, scheme, U, nullptr, nullptr, Y1);
+    __syncthreads();
+    if (scheme == LSS_ADI_DOUGLAS_RACHFORD) {
+        v_stage<T, BS>(v, U, Y1, sb0, Vn);
+    } else {
+        v_stage<T, BS>(v, U, Y1, sb0, Y2);
+        __syncthreads();
+        s_stage<T, BS, 2>(v, scheme, U, Y1, Y2, Y3);
+        __syncthreads();
+        if (scheme == LSS_ADI_HUNDSDORFER_VERWER)
+            v_stage<T, BS>(v, Y2, Y3, sb0, Vn);
+        else
+            v_stage<T, BS>(v, U, Y3, sb0, Vn);
+    }
+    __syncthreads();
+    b2_stage<T, BS>(v, Vn);
+    __syncthreads();
+}
+
 template <typename T, int BS> __global__ void __launch_bounds__(BS) k_batch_forward(bparams<T> p)
 {
     __shared__ int s_idx;
@@ -357,42 +417,10 @@ template <typename T, int BS> __global__ void __launch_bounds__(BS) k_batch_forw
         if (k >= p.count) break;
         const int inst = p.order[k];
         const bdesc d = p.desc[inst];
-        inst_view<T> v;
-        v.nx = d.nx;
-        v.ny = d.ny;
-        v.e_s = d.nx - 2;
-        v.e_v = d.ny - 2;
-        v.o2 = d.o2;
-#pragma unroll
-        for (int s = 0; s < SL_COUNT; ++s) v.S[s] = p.S[s] + d.o2;
-#pragma unroll
-        for (int s = 0; s < VL_COUNT; ++s) v.Vt[s] = p.Vt[s] + d.o2;
-#pragma unroll
-        for (int s = 0; s < X_COUNT; ++s) v.X[s] = p.X[s] + d.ox;
-#pragma unroll
-        for (int s = 0; s < Y_COUNT; ++s) v.Yv[s] = p.Yv[s] + d.oy;
-        v.imap = p.imap + d.ox;
-        v.jmap = p.jmap + d.oy;
+        const inst_view<T> v = make_view(p, d);
         T *U = p.U + d.o2, *Vn = p.V + d.o2, *Y1 = p.Y1 + d.o2, *Y2 = p.Y2 + d.o2, *Y3 = p.Y3 + d.o2;
         for (int step = 0; step < d.steps; ++step) {
-            b1_stage<T, BS>(v, U, sb0, d.bnc);
-            s_stage<T, BS, 1>(v, d.scheme, U, nullptr, nullptr, Y1);
-            __syncthreads();
-            if (d.scheme == LSS_ADI_DOUGLAS_RACHFORD) {
-                v_stage<T, BS>(v, U, Y1, sb0, Vn);
-            } else {
-                v_stage<T, BS>(v, U, Y1, sb0, Y2);
-                __syncthreads();
-                s_stage<T, BS, 2>(v, d.scheme, U, Y1, Y2, Y3);
-                __syncthreads();
-                if (d.scheme == LSS_ADI_HUNDSDORFER_VERWER)
-                    v_stage<T, BS>(v, Y2, Y3, sb0, Vn);
-                else
-                    v_stage<T, BS>(v, U, Y3, sb0, Vn);
-            }
-            __syncthreads();
-            b2_stage<T, BS>(v, Vn);
-            __syncthreads();
+            fwd_step<T, BS>(v, d.scheme, U, Y1, Y2, Y3, Vn, sb0, d.bnc);
             T *tmp = U;
             U = Vn;
             Vn = tmp;
@@ -416,6 +444,139 @@ template <typename T, int BS> __global__ void __launch_bounds__(BS) k_batch_forw
     }
 }
 
+#include "adi_adjoint.cuh"
+
+// Forward + adjoint of each instance by one CTA: forward pass keeping a checkpoint every
+// d.ck steps, then per segment (last first) a forward recomputation that keeps the stage
+// values of every step, followed by the adjoint steps of the segment in reverse order.
+// Results: value, the 5 parameter sensitivities, the final surface (state U arena) and
+// dV/d(initial condition) (state V arena).
+template <int BS> __global__ void __launch_bounds__(BS) k_batch_fwdadj(bparams<double> p)
+{
+    __shared__ int s_idx;
+    __shared__ int s_bad;
+    __shared__ double sb0[256];
+    __shared__ double red[5][BS];
+    double *ws = p.ws + (long long)blockIdx.x * p.ws_stride;
+    while (true) {
+        if (threadIdx.x == 0) s_idx = atomicAdd(p.counter, 1);
+        __syncthreads();
+        const int k = s_idx;
+        __syncthreads();
+        if (k >= p.count) break;
+        const int inst = p.order[k];
+        const bdesc d = p.desc[inst];
+        const inst_view<double> v = make_view(p, d);
+        const int nx = d.nx, ny = d.ny;
+        const long long n = (long long)nx * ny;
+        const int c = d.ck;
+        const int nseg = (d.steps + c - 1) / c;
+        // workspace carve-up
+        double *CK = ws;                                  // nseg * n
+        double *SEG = CK + (long long)nseg * n;           // (c + 1) * 4 * n
+        double *W0 = SEG + (long long)(c + 1) * 4 * n;    // n
+        double *W1 = W0 + n;                              // n
+        double *UB = W1 + n, *VB = UB + n, *Y1B = VB + n, *Y2B = Y1B + n, *Y3B = Y2B + n, *FB = Y3B + n;
+        double *TMP = FB + n;
+        double *LV = TMP + n, *LS = LV + nx, *HS = LS + ny;
+        auto slot = [&](int m, int a) -> double * { return SEG + ((long long)m * 4 + a) * n; };
+
+        // clear what must start at zero for this instance's shape
+        for (long long q = threadIdx.x; q < n; q += BS) {
+            FB[q] = 0.0;
+            Y1B[q] = 0.0;
+            Y3B[q] = 0.0;
+            CK[q] = static_cast<double>(p.payoff[d.o2 + q]);
+        }
+        for (int m = 0; m < c; ++m) {
+            double *y2 = slot(m, 2);
+            for (int q = threadIdx.x; q < ny; q += BS) {
+                y2[q] = 0.0;
+                y2[(long long)(nx - 1) * ny + q] = 0.0;
+            }
+        }
+        __syncthreads();
+        // forward pass with checkpoints
+        const double *cur = CK;
+        for (int step = 0; step < d.steps; ++step) {
+            double *next = ((step + 1) % c == 0 && step + 1 < d.steps) ? CK + (long long)((step + 1) / c) * n
+                                                                        : ((step & 1) ? W1 : W0);
+            fwd_step<double, BS>(v, d.scheme, cur, slot(0, 1), slot(0, 2), slot(0, 3), next, sb0, d.bnc);
+            cur = next;
+        }
+        // value, finiteness, final surface
+        if (threadIdx.x == 0) s_bad = 0;
+        __syncthreads();
+        int bad = 0;
+        double *outU = p.U + d.o2;
+        for (long long q = threadIdx.x; q < n; q += BS) {
+            const double val = cur[q];
+            bad |= !isfinite(val);
+            outU[q] = val;
+            VB[q] = 0.0;
+        }
+        if (bad) atomicOr(&s_bad, 1);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const long long o = (long long)d.i0 * ny + d.j0;
+            p.values[inst] = d.w00 * cur[o] + d.w10 * cur[o + ny] + d.w01 * cur[o + 1] + d.w11 * cur[o + ny + 1];
+            p.status[inst] = s_bad;
+            p.final_in_v[inst] = 0;
+            VB[o] = d.w00;
+            VB[o + ny] = d.w10;
+            VB[o + 1] = d.w01;
+            VB[o + ny + 1] = d.w11;
+        }
+        __syncthreads();
+        // reverse sweep over the segments
+        adj_acc acc;
+        for (int q = 0; q < 5; ++q) acc.s[q] = 0.0;
+        acc.vk = acc.vt = acc.vs1 = acc.vs2 = acc.vb = 0.0;
+        double *ub = UB, *vb = VB;
+        for (int sgi = nseg - 1; sgi >= 0; --sgi) {
+            const int n0 = sgi * c;
+            const int L = min(c, d.steps - n0);
+            const double *u0 = CK + (long long)sgi * n;
+            for (int m = 0; m < L; ++m) {
+                const double *um = (m == 0) ? u0 : slot(m, 0);
+                fwd_step<double, BS>(v, d.scheme, um, slot(m, 1), slot(m, 2), slot(m, 3), slot(m + 1, 0), sb0, d.bnc);
+            }
+            for (int m = L - 1; m >= 0; --m) {
+                const double *um = (m == 0) ? u0 : slot(m, 0);
+                adj_step<BS>(v, d, um, slot(m, 1), slot(m, 2), slot(m, 3), slot(m + 1, 0), vb, ub, Y1B, Y2B, Y3B, FB,
+                             TMP, LV, LS, HS, acc);
+                double *t = ub;
+                ub = vb;
+                vb = t;
+            }
+        }
+        // vb = adjoint of the initial condition
+        double *outL = p.V + d.o2;
+        for (long long q = threadIdx.x; q < n; q += BS) outL[q] = vb[q];
+        const double th = d.a_theta, ni = d.a_ni;
+        double g[5];
+        g[0] = acc.s[0] + d.a_halfk * th * acc.vb;
+        g[1] = acc.s[1] + ni * th * acc.vk;
+        g[2] = acc.s[2] + ni * th * acc.vt;
+        g[3] = acc.s[3] + ni * th * acc.vs1 + d.a_betat * th * acc.vs2;
+        g[4] = acc.s[4];
+        // order in the output: kappa, theta, sigma, rho, r
+        red[0][threadIdx.x] = g[1];
+        red[1][threadIdx.x] = g[2];
+        red[2][threadIdx.x] = g[3];
+        red[3][threadIdx.x] = g[4];
+        red[4][threadIdx.x] = g[0];
+        __syncthreads();
+        for (int h = BS / 2; h > 0; h >>= 1) {
+            if (threadIdx.x < h)
+                for (int q = 0; q < 5; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + h];
+            __syncthreads();
+        }
+        if (threadIdx.x < 5) p.grads[5LL * inst + threadIdx.x] = red[threadIdx.x][0];
+        __syncthreads();
+    }
+}
+
 // ------------------------------------------------------------------------------------------
 // host side
 // ------------------------------------------------------------------------------------------
@@ -433,6 +594,14 @@ template <typename T> struct batch_typed {
     dbuf<T> d_payoff; // concatenated initial conditions (sum n)
     int grid_blocks = 0;
     long long launches = 0;
+    // forward + adjoint
+    bool adjoint_ok = false;      // FP64 Heston DR/CS/MCS only
+    std::string adjoint_why;
+    int ck_override = 0;          // checkpoint interval (0 = ceil(sqrt(steps)))
+    int grid_adj = 0;
+    long long ws_stride = 0;
+    dbuf<double> d_grads, d_ws;
+    int sms = 0;
     cudaGraphExec_t graph = nullptr;
     int graph_mode = -1;
 
@@ -462,10 +631,15 @@ template <typename T> struct batch_typed {
         p.values = d_values.p;
         p.status = d_status.p;
         p.final_in_v = d_final.p;
+        p.grads = d_grads.p;
+        p.ws = d_ws.p;
+        p.ws_stride = ws_stride;
+        p.payoff = d_payoff.p;
         return p;
     }
 
     int create(const lss_adi_problem *ps, int n);
+    int prepare_adjoint(cudaStream_t s);
     int enqueue(int mode, cudaStream_t s);
     int run(int mode, cudaStream_t s, bool use_graph);
 };
@@ -530,6 +704,37 @@ template <typename T> int batch_typed<T>::create(const lss_adi_problem *ps, int 
                         imh[d.ox + i] = tt.imap[i];
                     }
                     const double h1 = tt.sc.h1;
+                    {
+                        // Heston coefficient derivatives (adjoint): X/A, v/B, db^/dsigma, de^/dkappa,
+                        // de^/dtheta, de^/dsigma on the grid (double)
+                        sinh_map<double> g;
+                        g.init(ps[k]);
+                        const double sg = ps[k].sigma;
+                        for (int i = 0; i < d.nx; ++i) {
+                            const double z = static_cast<double>(tt.sc.h1) * i;
+                            xh[X_HX * total_x + d.ox + i] = static_cast<T>(g.x(z) / g.a_der(z));
+                        }
+                        for (int j = 0; j < d.ny; ++j) {
+                            const double e = static_cast<double>(tt.sc.h2) * j;
+                            const double B = g.b_der(e), Bdd = g.d_der(e), vv = g.y(e);
+                            yh[Y_HY * total_y + d.oy + j] = static_cast<T>(vv / B);
+                            yh[Y_BS * total_y + d.oy + j] = static_cast<T>(sg * vv / (B * B));
+                            yh[Y_EK * total_y + d.oy + j] = static_cast<T>((ps[k].theta_v - vv) / B);
+                            yh[Y_ET * total_y + d.oy + j] = static_cast<T>(ps[k].kappa / B);
+                            yh[Y_ES * total_y + d.oy + j] = static_cast<T>(-sg * vv * Bdd / (B * B * B));
+                        }
+                        desc[k].a_delta = static_cast<double>(tt.sc.delta);
+                        desc[k].a_halfk = 0.5 * static_cast<double>(tt.sc.k);
+                        desc[k].a_ni = static_cast<double>(tt.sc.ni);
+                        desc[k].a_betat = static_cast<double>(tt.sc.beta);
+                        desc[k].a_sigma = sg;
+                        desc[k].a_rho = ps[k].rho;
+                        desc[k].a_theta = static_cast<double>(tt.sc.theta);
+                        desc[k].a_zeta = static_cast<double>(tt.sc.zeta);
+                        desc[k].a_gamma = static_cast<double>(tt.sc.gamma);
+                        desc[k].a_k = static_cast<double>(tt.sc.k);
+                        desc[k].ck = std::max(1, static_cast<int>(std::ceil(std::sqrt(static_cast<double>(d.steps)))));
+                    }
                     for (int j = 0; j < d.ny; ++j) {
                         yh[Y_SLO * total_y + d.oy + j] = tt.s_lo[j];
                         yh[Y_B2C * total_y + d.oy + j] = static_cast<T>(2.0 * h1 * static_cast<double>(tt.s_hi_neu[j]) / 3.0);
@@ -579,6 +784,17 @@ template <typename T> int batch_typed<T>::create(const lss_adi_problem *ps, int 
     LSS_CUDA_TRY(d_payoff.upload(pay.data(), total_n), "batch: uploading initial conditions");
     LSS_CUDA_TRY(stab.alloc(SL_COUNT * total_n), "batch: allocating S-line tables");
     LSS_CUDA_TRY(vtab.alloc(VL_COUNT * total_n), "batch: allocating v-line tables");
+    // boundary rows/columns of the line tables are read (as zeros) by the adjoint's gather
+    LSS_CUDA_TRY(cudaMemset(stab.p, 0, stab.n * sizeof(T)), "batch: clearing S-line tables");
+    LSS_CUDA_TRY(cudaMemset(vtab.p, 0, vtab.n * sizeof(T)), "batch: clearing v-line tables");
+    LSS_CUDA_TRY(d_grads.alloc(5 * static_cast<size_t>(n)), "batch: allocating gradients");
+    LSS_CUDA_TRY(cudaMemset(d_grads.p, 0, d_grads.n * sizeof(double)), "batch: clearing gradients");
+    adjoint_ok = std::is_same<T, double>::value;
+    adjoint_why = adjoint_ok ? "" : "the adjoint is FP64 only";
+    for (int k = 0; k < n && adjoint_ok; ++k) {
+        if (ps[k].model != LSS_ADI_HESTON) { adjoint_ok = false; adjoint_why = "the adjoint covers the Heston model only"; }
+        if (ps[k].scheme == LSS_ADI_HUNDSDORFER_VERWER) { adjoint_ok = false; adjoint_why = "no adjoint for Hundsdorfer-Verwer yet"; }
+    }
 
     // factorise on the device from the base tables
     {
@@ -616,17 +832,52 @@ template <typename T> int batch_typed<T>::create(const lss_adi_problem *ps, int 
         LSS_CUDA_TRY(cudaGetLastError(), "batch: launching v-line set-up");
         LSS_CUDA_TRY(cudaDeviceSynchronize(), "batch: v-line set-up");
     }
-    int dev = 0, sms = 0, per_sm = 0;
+    int dev = 0, sms = 0, per_sm = 0; // local
     LSS_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
     LSS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
     LSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_forward<T, 64>, 64, 0), "occupancy");
     grid_blocks = std::max(1, std::min(sms * std::max(1, std::min(per_sm, 8)), n));
+    this->sms = sms;
+    return LSS_ADI_OK;
+}
+
+template <typename T> int batch_typed<T>::prepare_adjoint(cudaStream_t s)
+{
+    (void)s;
+    if (!adjoint_ok) return set_error(LSS_ADI_EUNSUPPORTED, "batch: " + adjoint_why);
+    long long need = 0;
+    for (int k = 0; k < count; ++k) {
+        bdesc &d = desc[k];
+        const int c = ck_override > 0 ? std::min(ck_override, d.steps) : d.ck;
+        if (c != d.ck) {
+            d.ck = c;
+            LSS_CUDA_TRY(cudaMemcpy(d_desc.p + k, &d, sizeof(bdesc), cudaMemcpyHostToDevice), "batch: descriptor");
+        }
+        const long long nn = static_cast<long long>(d.nx) * d.ny;
+        const long long nseg = (d.steps + c - 1) / c;
+        need = std::max(need, (nseg + 4LL * (c + 1) + 2 + 7) * nn + d.nx + 2LL * d.ny);
+    }
+    const int want = std::max(1, std::min(sms * 4, count));
+    if (d_ws.p && ws_stride >= need && grid_adj == want) return LSS_ADI_OK;
+    ws_stride = (need + 31) / 32 * 32;
+    grid_adj = want;
+    LSS_CUDA_TRY(d_ws.alloc(static_cast<size_t>(ws_stride) * grid_adj), "batch: allocating adjoint workspace");
     return LSS_ADI_OK;
 }
 
 template <typename T> int batch_typed<T>::enqueue(int mode, cudaStream_t s)
 {
-    (void)mode;
+    if (mode == 1) {
+        if constexpr (std::is_same<T, double>::value) {
+            LSS_CUDA_TRY(cudaMemsetAsync(d_counter.p, 0, sizeof(int), s), "batch: counter reset");
+            k_batch_fwdadj<64><<<grid_adj, 64, 0, s>>>(params());
+            LSS_CUDA_TRY(cudaGetLastError(), "batch: launching k_batch_fwdadj");
+            launches = 1;
+            return LSS_ADI_OK;
+        } else {
+            return set_error(LSS_ADI_EUNSUPPORTED, "batch: the adjoint is FP64 only");
+        }
+    }
     LSS_CUDA_TRY(cudaMemcpyAsync(state.p, d_payoff.p, total_n * sizeof(T), cudaMemcpyDeviceToDevice, s), "batch: initial state");
     LSS_CUDA_TRY(cudaMemsetAsync(d_counter.p, 0, sizeof(int), s), "batch: counter reset");
     k_batch_forward<T, 64><<<grid_blocks, 64, 0, s>>>(params());
@@ -637,6 +888,10 @@ template <typename T> int batch_typed<T>::enqueue(int mode, cudaStream_t s)
 
 template <typename T> int batch_typed<T>::run(int mode, cudaStream_t s, bool use_graph)
 {
+    if (mode == 1) {
+        int rc = prepare_adjoint(s);
+        if (rc) return rc;
+    }
     if (!use_graph) return enqueue(mode, s);
     if (!graph || graph_mode != mode) {
         if (graph) cudaGraphExecDestroy(graph);
@@ -656,6 +911,65 @@ template <typename T> int batch_typed<T>::run(int mode, cudaStream_t s, bool use
         graph_mode = mode;
     }
     LSS_CUDA_TRY(cudaGraphLaunch(graph, s), "batch: graph launch");
+    return LSS_ADI_OK;
+}
+
+// lss_adi_adjoint: one parametric FP64 Heston instance through the batched forward+adjoint kernel.
+struct adjoint_impl {
+    batch_typed<double> b;
+};
+
+adjoint_solver::adjoint_solver() = default;
+adjoint_solver::~adjoint_solver() = default;
+
+int adjoint_solver::init(const lss_adi_problem &p)
+{
+    if (p.nx > 256) return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_adjoint: nx > 256 not supported");
+    if (p.scheme == LSS_ADI_HUNDSDORFER_VERWER)
+        return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_adjoint: no adjoint for Hundsdorfer-Verwer yet");
+    impl.reset(new (std::nothrow) adjoint_impl());
+    if (!impl) return set_error(LSS_ADI_ENOMEM, "host allocation failed");
+    lss_adi_problem q = p;
+    q.arith = LSS_ADI_ARITH_FAST;
+    return impl->b.create(&q, 1);
+}
+
+int adjoint_solver::run(const void *payoff, double *out_value, double *dv_dparams, void *dv_dpayoff, int checkpoint_every,
+                        int flags, void *stream)
+{
+    batch_typed<double> &b = impl->b;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const bool dev = (flags & LSS_ADI_DEVICE_POINTERS) != 0;
+    const size_t n = static_cast<size_t>(b.total_n);
+    if (payoff)
+        LSS_CUDA_TRY(cudaMemcpyAsync(b.d_payoff.p, payoff, n * sizeof(double),
+                                     dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s),
+                     "lss_adi_adjoint: copying the terminal condition");
+    b.ck_override = checkpoint_every;
+    int rc = b.run(1, s, false);
+    if (rc) return rc;
+    if (out_value)
+        LSS_CUDA_TRY(cudaMemcpyAsync(out_value, b.d_values.p, sizeof(double), cudaMemcpyDeviceToHost, s), "lss_adi_adjoint: value");
+    if (dv_dparams)
+        LSS_CUDA_TRY(cudaMemcpyAsync(dv_dparams, b.d_grads.p, 5 * sizeof(double), cudaMemcpyDeviceToHost, s),
+                     "lss_adi_adjoint: gradients");
+    if (dv_dpayoff)
+        LSS_CUDA_TRY(cudaMemcpyAsync(dv_dpayoff, b.state.p + b.total_n, n * sizeof(double),
+                                     dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s),
+                     "lss_adi_adjoint: payoff gradient");
+    LSS_CUDA_TRY(cudaStreamSynchronize(s), "lss_adi_adjoint: run");
+    return LSS_ADI_OK;
+}
+
+template <typename T> static int payoff_grad_t(batch_typed<T> &bt, int index, void *out)
+{
+    if (index < 0 || index >= bt.count) return set_error(LSS_ADI_EINVAL, "lss_adi_batch_payoff_gradient: index out of range");
+    if (!std::is_same<T, double>::value) return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_batch_payoff_gradient: FP64 only");
+    LSS_CUDA_TRY(cudaDeviceSynchronize(), "batch: synchronising");
+    const bdesc &d = bt.desc[index];
+    LSS_CUDA_TRY(cudaMemcpy(out, bt.state.p + bt.total_n + d.o2, static_cast<size_t>(d.nx) * d.ny * sizeof(T),
+                            cudaMemcpyDeviceToHost),
+                 "batch: payoff gradient");
     return LSS_ADI_OK;
 }
 
@@ -681,7 +995,9 @@ static int run_host_t(batch_typed<T> &bt, int mode, const void *payoffs, double 
     if (values)
         LSS_CUDA_TRY(cudaMemcpyAsync(values, bt.d_values.p, bt.count * sizeof(double), cudaMemcpyDeviceToHost, s),
                      "batch: reading values");
-    (void)grads;
+    if (grads && mode == 1)
+        LSS_CUDA_TRY(cudaMemcpyAsync(grads, bt.d_grads.p, 5 * bt.count * sizeof(double), cudaMemcpyDeviceToHost, s),
+                     "batch: reading gradients");
     LSS_CUDA_TRY(cudaStreamSynchronize(s), "batch: run");
     return LSS_ADI_OK;
 }
@@ -691,7 +1007,7 @@ template <typename T> static int results_t(batch_typed<T> &bt, double *values, d
     LSS_CUDA_TRY(cudaDeviceSynchronize(), "batch: synchronising");
     if (values) LSS_CUDA_TRY(cudaMemcpy(values, bt.d_values.p, bt.count * sizeof(double), cudaMemcpyDeviceToHost), "batch: values");
     if (status) LSS_CUDA_TRY(cudaMemcpy(status, bt.d_status.p, bt.count * sizeof(int), cudaMemcpyDeviceToHost), "batch: status");
-    if (grads) std::fill(grads, grads + 5 * static_cast<size_t>(bt.count), 0.0);
+    if (grads) LSS_CUDA_TRY(cudaMemcpy(grads, bt.d_grads.p, 5 * bt.count * sizeof(double), cudaMemcpyDeviceToHost), "batch: grads");
     return LSS_ADI_OK;
 }
 
@@ -748,7 +1064,6 @@ static int batch_run(lss_adi_batch *b, int mode, void *stream, bool graph)
     clear_error();
     if (!b) return set_error(LSS_ADI_EINVAL, "lss_adi_batch_run: null batch");
     if (mode != 0 && mode != 1) return set_error(LSS_ADI_EINVAL, "lss_adi_batch_run: mode must be 0 or 1");
-    if (mode == 1) return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_batch_run: adjoint mode not available yet");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     b->last_stream = s;
     return b->b64 ? b->b64->run(mode, s, graph) : b->b32->run(mode, s, graph);
@@ -763,7 +1078,6 @@ int lss_adi_batch_run_host(lss_adi_batch *b, int mode, const void *payoffs, doub
     clear_error();
     if (!b) return set_error(LSS_ADI_EINVAL, "lss_adi_batch_run_host: null batch");
     if (mode != 0 && mode != 1) return set_error(LSS_ADI_EINVAL, "lss_adi_batch_run_host: mode must be 0 or 1");
-    if (mode == 1) return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_batch_run_host: adjoint mode not available yet");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     b->last_stream = s;
     return b->b64 ? run_host_t(*b->b64, mode, payoffs, values, grads, s)
@@ -784,6 +1098,13 @@ int lss_adi_batch_surface(lss_adi_batch *b, int index, void *out_surface)
     clear_error();
     if (!b || !out_surface) return set_error(LSS_ADI_EINVAL, "lss_adi_batch_surface: null argument");
     return b->b64 ? surface_t(*b->b64, index, out_surface) : surface_t(*b->b32, index, out_surface);
+}
+
+int lss_adi_batch_payoff_gradient(lss_adi_batch *b, int index, void *out)
+{
+    clear_error();
+    if (!b || !out) return set_error(LSS_ADI_EINVAL, "lss_adi_batch_payoff_gradient: null argument");
+    return b->b64 ? payoff_grad_t(*b->b64, index, out) : payoff_grad_t(*b->b32, index, out);
 }
 
 int lss_adi_batch_launch_count(const lss_adi_batch *b)

@@ -1,0 +1,150 @@
+"""Adjoint (lss_adi_adjoint / batch mode 1) against finite differences and linearity.
+
+The reference has no sensitivities; its forward path is the check: dV/d(kappa, theta, sigma,
+rho, r) against central finite differences (relative bump 1e-5) of (a) the device forward
+and (b) the CPU oracle (bit-exact with the reference's Thomas-LU path), and
+dV/d(payoff grid) against the exact linearity of the scheme in the terminal condition.
+"""
+import dataclasses
+
+import numpy as np
+import pytest
+
+from conftest import oracle_unstable
+
+pytestmark = pytest.mark.gpu
+
+PARAMS = ("kappa", "theta_v", "sigma", "rho", "rate")
+BASE = dict(model="heston", kappa=1.5, theta_v=0.04, sigma=0.3, rho=-0.6, rate=0.02, strike=100.0, maturity=1.0,
+            s_lo=0.0, s_hi=200.0, v_lo=0.0, v_hi=1.2, nonuniform=True, acc_point=100.0, alpha_scale=10.0,
+            beta_scale=24.0, eval_s=100.0, eval_v=0.04)
+
+
+def bilinear_value(surface, x, y, s0, v0):
+    i = max(0, min(len(x) - 2, int(np.searchsorted(x, s0, side="right")) - 1))
+    j = max(0, min(len(y) - 2, int(np.searchsorted(y, v0, side="right")) - 1))
+    wx = min(1.0, max(0.0, (s0 - x[i]) / (x[i + 1] - x[i])))
+    wy = min(1.0, max(0.0, (v0 - y[j]) / (y[j + 1] - y[j])))
+    return ((1 - wx) * (1 - wy) * surface[i, j] + wx * (1 - wy) * surface[i + 1, j] + (1 - wx) * wy * surface[i, j + 1]
+            + wx * wy * surface[i + 1, j + 1])
+
+
+def device_value(lss, p):
+    return lss.ImplicitHestonSolver(p, precision="f64", arith="fast").solve()[1]
+
+
+def oracle_value(oracle, lss, p):
+    kw = {k: v for k, v in dataclasses.asdict(p).items() if k not in ("eval_s", "eval_v", "fp64_tables")}
+    op = oracle.Problem(**kw)
+    surf = oracle.solve(op, "f64")
+    x, y = oracle.grid(op, "f64")
+    return bilinear_value(surf, x, y, p.eval_s, p.eval_v)
+
+
+def fd_grad(fn, p, name, rel=1e-5):
+    base = getattr(p, name)
+    h = rel * abs(base)
+    up = dataclasses.replace(p, **{name: base + h})
+    dn = dataclasses.replace(p, **{name: base - h})
+    return (fn(up) - fn(dn)) / (2 * h)
+
+
+CASES = {
+    "mcs_64x32": dict(BASE, scheme="mcs", nx=64, ny=32, nt=51),
+    "mcs_97x41": dict(BASE, scheme="mcs", nx=97, ny=41, nt=40, rho=-0.3, sigma=0.5, kappa=2.5),
+    "cs_60x30": dict(BASE, scheme="cs", nx=60, ny=30, nt=31, rho=-0.2),
+    "dr_70x35": dict(BASE, scheme="dr", nx=70, ny=35, nt=41),
+    "mcs_z08_theta80": dict(BASE, scheme="mcs", zeta=0.8, theta_scheme="theta80", nx=48, ny=24, nt=31, rho=-0.4),
+}
+
+
+@pytest.mark.parametrize("key", sorted(CASES))
+def test_parameter_gradients_match_device_finite_differences(lss, key):
+    p = lss.HestonProblem(**CASES[key])
+    s = lss.ImplicitHestonSolver(p, precision="f64", arith="fast")
+    val, grads, _ = s.adjoint(want_payoff_grad=False)
+    assert abs(val - device_value(lss, p)) <= 1e-12 * max(1.0, abs(val))
+    for k, name in enumerate(PARAMS):
+        fd = fd_grad(lambda q: device_value(lss, q), p, name)
+        assert abs(grads[k] - fd) <= 1e-6 * max(abs(fd), 1e-3 * abs(val)), (name, grads[k], fd)
+
+
+@pytest.mark.parametrize("key", ["mcs_64x32", "dr_70x35"])
+def test_parameter_gradients_match_reference_bump_and_revalue(lss, oracle, key):
+    p = lss.HestonProblem(**CASES[key])
+    val, grads, _ = lss.ImplicitHestonSolver(p, precision="f64", arith="fast").adjoint(want_payoff_grad=False)
+    for k, name in enumerate(PARAMS):
+        fd = fd_grad(lambda q: oracle_value(oracle, lss, q), p, name)
+        assert abs(grads[k] - fd) <= 1e-6 * max(abs(fd), 1e-3 * abs(val)), (name, grads[k], fd)
+
+
+@pytest.mark.parametrize("key", ["mcs_64x32", "cs_60x30", "dr_70x35"])
+def test_payoff_gradient_is_the_linear_response(lss, key):
+    p = lss.HestonProblem(**CASES[key])
+    s = lss.ImplicitHestonSolver(p, precision="f64", arith="fast")
+    rng = np.random.default_rng(1)
+    payoff = rng.uniform(0.0, 100.0, size=(p.nx, p.ny))
+    val, _, lam = s.adjoint(payoff=payoff)
+    delta = rng.normal(size=(p.nx, p.ny))
+    v1 = s.solve(payoff=payoff + delta)[1]
+    v0 = s.solve(payoff=payoff)[1]
+    assert abs(v0 - val) <= 1e-12 * max(1.0, abs(val))
+    pred = float(np.sum(lam * delta))
+    assert abs((v1 - v0) - pred) <= 1e-9 * max(1.0, np.sum(np.abs(lam * delta)))
+
+
+def test_checkpoint_interval_does_not_change_results(lss):
+    p = lss.HestonProblem(**CASES["mcs_64x32"])
+    s = lss.ImplicitHestonSolver(p, precision="f64", arith="fast")
+    ref = None
+    for ck in (0, 1, 3, 7, 50, 1000):
+        val, g, lam = s.adjoint(checkpoint_every=ck)
+        if ref is None:
+            ref = (val, g, lam)
+        else:
+            assert val == ref[0]
+            assert np.array_equal(g, ref[1])
+            assert np.array_equal(lam, ref[2])
+
+
+def test_batch_mode1_matches_single_instance_and_mode0(lss):
+    from linear_system_solvers_gb300.batch import draw_batch
+
+    probs = draw_batch(12)
+    for p in probs:
+        p.nt = 31
+    b = lss.BatchSolver(probs, precision="f64")
+    b.run(0)
+    v0, _, _ = b.results()
+    b.run(1)
+    v1, g1, st = b.results()
+    assert np.array_equal(v0, v1)
+    for k in (0, 5, 11):
+        val, g, lam = lss.ImplicitHestonSolver(probs[k], precision="f64", arith="fast").adjoint()
+        assert val == v1[k]
+        np.testing.assert_allclose(g1[k], g, rtol=1e-13, atol=1e-15)
+        np.testing.assert_allclose(b.payoff_gradient(k), lam, rtol=1e-13, atol=1e-15)
+
+
+def test_batch_gradients_finite_difference_sample(lss):
+    """Config-4 style instances (uneven batch, MCS): stable members checked against FD."""
+    from linear_system_solvers_gb300.batch import draw_batch
+
+    probs = draw_batch(16, seed=20261204)
+    for p in probs:
+        p.nt = 21
+        p.nx = min(p.nx, 96)
+        p.ny = min(p.ny, 48)
+    b = lss.BatchSolver(probs, precision="f64")
+    b.run(1)
+    vals, grads, _ = b.results()
+    checked = 0
+    for k, p in enumerate(probs):
+        surf = b.surface(k)
+        if oracle_unstable(surf, p.s_hi):
+            continue
+        for q, name in enumerate(PARAMS):
+            fd = fd_grad(lambda pp: device_value(lss, pp), p, name)
+            assert abs(grads[k, q] - fd) <= 1e-6 * max(abs(fd), 1e-3 * abs(vals[k])), (k, name, grads[k, q], fd)
+        checked += 1
+    assert checked >= 4
