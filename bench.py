@@ -41,6 +41,7 @@ def parse():
     ap.add_argument("--mode", default="auto", choices=["auto", "fwd", "fwdadj"])
     ap.add_argument("--cpu-sample", type=int, default=32, help="instances timed on the host cores")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip timing the plain per-instance device path")
     return ap.parse_args()
 
 
@@ -313,7 +314,7 @@ def main():
     }
     if cpu is not None:
         out["cpu_baseline"] = cpu
-    if world == 1:
+    if world == 1 and not args.no_plain:
         out["plain_path"] = time_plain_path(lss, problems, stream, value)
     print(json.dumps(out))
     if world > 1:
