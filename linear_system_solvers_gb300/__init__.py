@@ -6,8 +6,8 @@ Hundsdorfer-Verwer splitting with Thomas-LU line solves), exposed through the C-
 ``include/lss_adi.h`` (``_build/liblss_adi.so``) and this thin Python layer.
 """
 from ._lib import LssError, load  # noqa: F401
-from .solver import HestonProblem, ImplicitHestonSolver, thomas_lu_lines  # noqa: F401
+from .solver import HestonProblem, ImplicitHestonSolver, TabulatedHestonSolver, thomas_lu_lines  # noqa: F401
 from .batch import BatchSolver, draw_batch  # noqa: F401
 
-__all__ = ["HestonProblem", "ImplicitHestonSolver", "BatchSolver", "draw_batch", "thomas_lu_lines", "LssError",
+__all__ = ["HestonProblem", "ImplicitHestonSolver", "TabulatedHestonSolver", "BatchSolver", "draw_batch", "thomas_lu_lines", "LssError",
            "load"]

@@ -126,6 +126,40 @@ class ImplicitHestonSolver:
         return val.value, np.array(list(g)), dpay
 
 
+class TabulatedHestonSolver(ImplicitHestonSolver):
+    """Time-invariant coefficients sampled on the grid by the caller (``lss_adi_create_tabulated``):
+    the device drop-in for arbitrary coefficient functions of the reference's
+    heat_coefficient_data_config_2d.
+
+    coef: (7, nx, ny) M, P, Z, M~, P~, W, C; coef_v0: (3, nx) D, E, F on the v = v_lo line;
+    s_lo: (ny,) Dirichlet values at S_lo; s_hi_neumann: (ny,) transformed Neumann data at S_hi;
+    v_hi: (nx,) Dirichlet values at v_hi; payoff: (nx, ny).
+    """
+
+    def __init__(self, nt, t_lo, t_hi, scheme, theta_scheme, coef, coef_v0, s_lo, s_hi_neumann, v_hi, payoff,
+                 zeta=0.5, forward=False, precision="f64", arith="fast"):
+        self.lib = L.load()
+        self.precision = precision
+        self.dtype = _dtype(precision)
+        arrs = [np.ascontiguousarray(a, dtype=self.dtype) for a in (coef, coef_v0, s_lo, s_hi_neumann, v_hi, payoff)]
+        self._keep = arrs
+        nx, ny = arrs[5].shape
+        self.problem = HestonProblem(nx=nx, ny=ny, nt=nt)
+        t = L.LssAdiTables()
+        t.nx, t.ny, t.nt = nx, ny, int(nt)
+        t.t_lo, t.t_hi = float(t_lo), float(t_hi)
+        t.scheme = L.SCHEMES[scheme]
+        t.theta_scheme = L.THETAS[theta_scheme]
+        t.forward = int(bool(forward))
+        t.precision = L.FP32 if precision == "f32" else L.FP64
+        t.arith = L.ARITH_REFERENCE if arith == "reference" else L.ARITH_FAST
+        t.zeta = float(zeta)
+        t.coef, t.coef_v0, t.s_lo_dirichlet, t.s_hi_neumann, t.v_hi_dirichlet, t.payoff = [a.ctypes.data for a in arrs]
+        h = ctypes.c_void_p()
+        L.check(self.lib.lss_adi_create_tabulated(ctypes.byref(t), ctypes.byref(h)))
+        self._h = h
+
+
 def thomas_lu_lines(lo, diag, up, rhs, bnd_lo, bnd_hi, precision: str = "f64"):
     """Batched Thomas LU through lss_tridiag_thomas_lu (arrays (n, lines), host numpy).
 

@@ -133,3 +133,33 @@ def test_tridiag_building_block_bitwise(lss, n, lines, fp):
     got = lss.thomas_lu_lines(lo, dg, up, rhs, blo, bhi, precision=fp)
     want = thomas_numpy(lo, dg, up, rhs, blo, bhi)
     assert np.array_equal(got, want)
+
+
+def _a_der_at_one(p):
+    """A(1) of the reference's sinh map, evaluated like the library (double, same order)."""
+    import math
+
+    lo, hi, pt = p.s_lo, p.s_hi, p.acc_point
+    alpha = (pt - lo) / p.alpha_scale if p.nonuniform else hi - lo
+    c0 = math.asinh((hi - pt) / alpha)
+    c1 = math.asinh((lo - pt) / alpha)
+    return alpha * (c0 - c1) * math.cosh(c0 * 1.0 + c1 * (1.0 - 1.0))
+
+
+@pytest.mark.parametrize("scheme", ["dr", "mcs", "hv"])
+def test_tabulated_drop_in_bitwise_equals_parametric(lss, oracle, scheme):
+    """Coefficients sampled by the caller (the reference's std::function coefficient path)
+    through lss_adi_create_tabulated give the same bits as the parametric set-up."""
+    kw = dict(CONFIG1, scheme=scheme, nx=45, ny=27, nt=31, **NU)
+    op, pp = problem_pair(kw)
+    k = oracle.coefficients(op, 0.0)
+    coef = np.stack([k[n] for n in ("M", "P", "Z", "Mt", "Pt", "W", "C")])
+    v0 = np.stack([k[n][:, 0] for n in ("D", "E", "F")])
+    x, _ = oracle.grid(op, "f64")
+    neu = pp.neumann_value * _a_der_at_one(pp)
+    payoff = np.repeat(np.maximum(x - pp.strike, 0.0)[:, None], op.ny, axis=1)
+    tab = lss.TabulatedHestonSolver(op.nt, 0.0, op.maturity, scheme, "cn", coef, v0, np.zeros(op.ny),
+                                    np.full(op.ny, neu), x, payoff, arith="reference")
+    got, _ = tab.solve()
+    want = oracle.solve(op, "f64")
+    assert np.array_equal(got, want)
