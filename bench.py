@@ -223,7 +223,9 @@ def main():
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    problems = problems_all if rank == 0 else draw_batch(args.count, seed=SEED + rank)
+    from linear_system_solvers_gb300.sharding import max_over_ranks, rank_seed
+
+    problems = problems_all if rank == 0 else draw_batch(args.count, seed=rank_seed(SEED, rank))
     gps = grid_point_steps(problems)
 
     lib = L.load()
@@ -278,11 +280,7 @@ def main():
         e2e_s = (time.perf_counter() - t0) / args.steps
     e2e_ok = bool(np.allclose(vals_h, values, rtol=1e-12, atol=1e-12))
 
-    t_max = ms
-    if world > 1:
-        tt = torch.tensor([ms, e2e_s], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_max, e2e_s = float(tt[0]), float(tt[1])
+    t_max, e2e_s = max_over_ranks([ms, e2e_s], device="cuda")
     if rank != 0:
         torch.distributed.destroy_process_group()
         return
