@@ -25,11 +25,11 @@ struct adj_acc {
 };
 
 // B2^T: fold the S_max extrapolation row into rows nx-2 / nx-3; clear rows 0 and nx-1 of UB.
-template <int BS> __device__ __forceinline__ void adj_b2(const inst_view<double> &v, double *VB, double *UB)
+__device__ __forceinline__ void adj_b2(const inst_view<double> &v, double *VB, double *UB, int l0, int ls)
 {
     const int nx = v.nx, ny = v.ny, lri = nx - 1;
     const double four3 = 4.0 / 3.0, third = 1.0 / 3.0;
-    for (int q = threadIdx.x; q < ny; q += BS) {
+    for (int q = l0; q < ny; q += ls) {
         double add = 0.0;
         if (__ldg(v.jmap + q) == q) add += VB[(long long)lri * ny + q];
         if (q + 1 < ny && __ldg(v.jmap + q + 1) == q) add += VB[(long long)lri * ny + q + 1];
@@ -43,12 +43,12 @@ template <int BS> __device__ __forceinline__ void adj_b2(const inst_view<double>
 // V-line stage adjoint.  XB: adjoint of the stage output (rows i, incl. the lo copy at t=0);
 // in/out: the stage's `in` array and its output; INB (+)= adjoint of `in`; INHB (+)= adjoint
 // of `inh`; LV (+)= adjoint of the line's lo value.
-template <int BS, bool FIRST>
+template <bool FIRST>
 __device__ __forceinline__ void adj_v(const inst_view<double> &v, const double *in, const double *out, const double *XB,
-                                      double *INB, double *INHB, double *TMP, double *LV, adj_acc &acc)
+                                      double *INB, double *INHB, double *TMP, double *LV, adj_acc &acc, int l0, int ls)
 {
     const int nx = v.nx, ny = v.ny, e = ny - 2;
-    for (int i = 1 + threadIdx.x; i <= nx - 2; i += BS) {
+    for (int i = 1 + l0; i <= nx - 2; i += ls) {
         const long long row = (long long)i * ny;
         double z = 0.0;
         for (int t = 1; t <= e; ++t) {
@@ -93,15 +93,15 @@ __device__ __forceinline__ void adj_v(const inst_view<double> &v, const double *
 // S-line stage adjoint.  KIND 1: S1 (explicit operator on U, output Y1).  KIND 2: second S
 // stage of CS/MCS (output Y3).  XB: adjoint of the stage output; FB receives the scaled
 // right-hand-side adjoint w; LS/HS the lo/hi adjoints of the line.
-template <int BS, int KIND>
+template <int KIND>
 __device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d, const double *U, const double *Y1,
                                       const double *Y2, const double *Yo, const double *XB, double *FB, double *TMP,
-                                      double *LS, double *HS, double *UB, double *Y1B, adj_acc &acc)
+                                      double *LS, double *HS, double *UB, double *Y1B, adj_acc &acc, int l0, int ls)
 {
     const int nx = v.nx, ny = v.ny, e = nx - 2;
     const double th = d.a_theta;
     const double zt = (d.scheme == LSS_ADI_MODIFIED_CRAIG_SNEYD) ? (d.a_zeta - th) : 0.0;
-    for (int j = 1 + threadIdx.x; j <= ny - 2; j += BS) {
+    for (int j = 1 + l0; j <= ny - 2; j += ls) {
         double z = 0.0;
         for (int t = 1; t <= e; ++t) {
             const long long o = (long long)t * ny + j;
@@ -178,10 +178,10 @@ __device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d
 // Gather pass over columns q: cross-line right-hand-side adjoints of an S stage into UB
 // (and Y2B for KIND 2), the lo/hi adjoints of the S lines, and for KIND 1 the adjoint of
 // the explicit v = v_lo boundary column (B1^T) with its parameter sensitivities.
-template <int BS, int KIND>
+template <int KIND>
 __device__ __forceinline__ void adj_gather(const inst_view<double> &v, const bdesc &d, const double *U, const double *FB,
                                            const double *LS, const double *HS, const double *LV, double *UB,
-                                           double *Y2B, adj_acc &acc)
+                                           double *Y2B, adj_acc &acc, int l0, int ls)
 {
     const int nx = v.nx, ny = v.ny;
     auto F = [&](int p, int q) -> double {
@@ -198,7 +198,7 @@ __device__ __forceinline__ void adj_gather(const inst_view<double> &v, const bde
         if (i + 1 <= nx - 2 && __ldg(v.imap + i + 1) == i) s += LV[i + 1];
         return s;
     };
-    for (int q = threadIdx.x; q < ny; q += BS) {
+    for (int q = l0; q < ny; q += ls) {
         double lsum = 0.0, hsum = 0.0;
         if (q >= 1 && q <= ny - 2 && __ldg(v.jmap + q) == q) { lsum += LS[q]; hsum += HS[q]; }
         if (q + 1 <= ny - 2 && __ldg(v.jmap + q + 1) == q) { lsum += LS[q + 1]; hsum += HS[q + 1]; }
@@ -256,24 +256,25 @@ __device__ __forceinline__ void adj_step(const inst_view<double> &v, const bdesc
                                          double *Y1B, double *Y2B, double *Y3B, double *FB, double *TMP, double *LV,
                                          double *LS, double *HS, adj_acc &acc)
 {
-    adj_b2<BS>(v, VB, UB);
+    const int l0 = threadIdx.x;
+    adj_b2(v, VB, UB, l0, BS);
     __syncthreads();
     if (d.scheme == LSS_ADI_DOUGLAS_RACHFORD) {
-        adj_v<BS, true>(v, U, Vo, VB, UB, Y1B, TMP, LV, acc);
+        adj_v<true>(v, U, Vo, VB, UB, Y1B, TMP, LV, acc, l0, BS);
         __syncthreads();
     } else {
-        adj_v<BS, true>(v, U, Vo, VB, UB, Y3B, TMP, LV, acc);
+        adj_v<true>(v, U, Vo, VB, UB, Y3B, TMP, LV, acc, l0, BS);
         __syncthreads();
-        adj_s<BS, 2>(v, d, U, Y1, Y2, Y3, Y3B, FB, TMP, LS, HS, UB, Y1B, acc);
+        adj_s<2>(v, d, U, Y1, Y2, Y3, Y3B, FB, TMP, LS, HS, UB, Y1B, acc, l0, BS);
         __syncthreads();
-        adj_gather<BS, 2>(v, d, U, FB, LS, HS, LV, UB, Y2B, acc);
+        adj_gather<2>(v, d, U, FB, LS, HS, LV, UB, Y2B, acc, l0, BS);
         __syncthreads();
-        adj_v<BS, false>(v, U, Y2, Y2B, UB, Y1B, TMP, LV, acc);
+        adj_v<false>(v, U, Y2, Y2B, UB, Y1B, TMP, LV, acc, l0, BS);
         __syncthreads();
     }
-    adj_s<BS, 1>(v, d, U, Y1, Y2, Y1, Y1B, FB, TMP, LS, HS, UB, Y1B, acc);
+    adj_s<1>(v, d, U, Y1, Y2, Y1, Y1B, FB, TMP, LS, HS, UB, Y1B, acc, l0, BS);
     __syncthreads();
-    adj_gather<BS, 1>(v, d, U, FB, LS, HS, LV, UB, Y2B, acc);
+    adj_gather<1>(v, d, U, FB, LS, HS, LV, UB, Y2B, acc, l0, BS);
     __syncthreads();
 }
 

@@ -54,6 +54,7 @@ struct lss_adi_handle {
     lss_adi_problem prob{};
     std::unique_ptr<plain_solver<double>> s64;
     std::unique_ptr<plain_solver<float>> s32;
+    std::unique_ptr<wide_solver_base> wide;
     std::unique_ptr<adjoint_solver> adj;
 };
 
@@ -93,8 +94,11 @@ int lss_adi_create(const lss_adi_problem *p, lss_adi_handle **h)
     hh->parametric = true;
     hh->prob = *p;
     try {
-        rc = p->precision == LSS_ADI_FP64 ? make_plain<double>(*p, p->arith, p->eval_s, p->eval_v, hh->s64)
-                                          : make_plain<float>(*p, p->arith, p->eval_s, p->eval_v, hh->s32);
+        if (p->arith == LSS_ADI_ARITH_FAST)
+            rc = make_wide_solver(*p, hh->wide);
+        else
+            rc = p->precision == LSS_ADI_FP64 ? make_plain<double>(*p, p->arith, p->eval_s, p->eval_v, hh->s64)
+                                              : make_plain<float>(*p, p->arith, p->eval_s, p->eval_v, hh->s32);
     } catch (const std::bad_alloc &) {
         return set_error(LSS_ADI_ENOMEM, "lss_adi_create: host allocation failed");
     }
@@ -138,6 +142,7 @@ static int forward_impl(lss_adi_handle *h, const void *payoff, void *out_surface
 {
     clear_error();
     if (!h) return set_error(LSS_ADI_EINVAL, "lss_adi_forward: null handle");
+    if (h->wide) return h->wide->forward(payoff, out_surface, out_value, flags, stream, graph);
     if (h->s64) return h->s64->forward(payoff, out_surface, out_value, flags, stream, graph);
     if (h->s32) return h->s32->forward(payoff, out_surface, out_value, flags, stream, graph);
     return set_error(LSS_ADI_EINVAL, "lss_adi_forward: empty handle");
@@ -176,6 +181,7 @@ int lss_adi_grid(const lss_adi_handle *h, void *x, void *y)
 {
     clear_error();
     if (!h || !x || !y) return set_error(LSS_ADI_EINVAL, "lss_adi_grid: null argument");
+    if (h->wide) return h->wide->grid(x, y);
     if (h->s64) {
         std::copy(h->s64->tab_.x.begin(), h->s64->tab_.x.end(), static_cast<double *>(x));
         std::copy(h->s64->tab_.y.begin(), h->s64->tab_.y.end(), static_cast<double *>(y));

@@ -201,11 +201,13 @@ template <typename T> struct inst_view {
 template <typename T> __device__ __forceinline__ T ldg(const T *p) { return __ldg(p); }
 
 // boundary#1: the v = v_lo column, explicit (explicit_boundary.hpp:39-84); result in smem
-template <typename T, int BS>
-__device__ __forceinline__ void b1_stage(const inst_view<T> &v, const T *U, T *sb0, double bnc)
+// Work distribution of every stage: items l0, l0 + ls, ... (threads of one CTA in the
+// batched kernel; all threads of a grid in the per-stage kernels of the wide path).
+template <typename T>
+__device__ __forceinline__ void b1_stage(const inst_view<T> &v, const T *U, T *sb0, double bnc, int l0, int ls)
 {
     const int nx = v.nx, ny = v.ny, N = nx - 1;
-    for (int i = threadIdx.x; i < nx; i += BS) {
+    for (int i = l0; i < nx; i += ls) {
         T r;
         if (i == 0) {
             r = ldg(v.Yv[Y_SLO]);
@@ -222,11 +224,11 @@ __device__ __forceinline__ void b1_stage(const inst_view<T> &v, const T *U, T *s
 }
 
 // boundary#2: row S_lo and the S_max extrapolation row (explicit_boundary.hpp:202-238)
-template <typename T, int BS> __device__ __forceinline__ void b2_stage(const inst_view<T> &v, T *Vn)
+template <typename T> __device__ __forceinline__ void b2_stage(const inst_view<T> &v, T *Vn, int l0, int ls)
 {
     const int nx = v.nx, ny = v.ny, lri = nx - 1;
     const T four3 = T(4.0 / 3.0), third = T(1.0 / 3.0);
-    for (int j = threadIdx.x; j < ny; j += BS) {
+    for (int j = l0; j < ny; j += ls) {
         Vn[j] = ldg(v.Yv[Y_SLO] + j);
         const int jj = ldg(v.jmap + j);
         Vn[(long long)lri * ny + j] =
@@ -237,11 +239,12 @@ template <typename T, int BS> __device__ __forceinline__ void b2_stage(const ins
 // S-line sweeps.  KIND 1: explicit operator on U (Y1).  KIND 2: second S stage of
 // CS/MCS/HV on U, Y1, Y2 (scheme chooses the weights).  Thread per line j; every access
 // of a warp is one coalesced row segment.
-template <typename T, int BS, int KIND>
-__device__ __forceinline__ void s_stage(const inst_view<T> &v, int scheme, const T *U, const T *Y1, const T *Y2, T *Y)
+template <typename T, int KIND>
+__device__ __forceinline__ void s_stage(const inst_view<T> &v, int scheme, const T *U, const T *Y1, const T *Y2, T *Y,
+                                        int l0, int ls)
 {
     const int nx = v.nx, ny = v.ny, e = v.e_s;
-    for (int j = 1 + threadIdx.x; j <= ny - 2; j += BS) {
+    for (int j = 1 + l0; j <= ny - 2; j += ls) {
         const int jj = ldg(v.jmap + j);
         const T lo = U[jj], hi = U[(long long)(nx - 1) * ny + jj];
         T y = lo;
@@ -325,11 +328,12 @@ __device__ __forceinline__ void s_stage(const inst_view<T> &v, int scheme, const
 }
 
 // v-line sweep: line i reads row i of `in` (t-1, t, t+1) and `inh` (t); tables are [t][i].
-template <typename T, int BS>
-__device__ __forceinline__ void v_stage(const inst_view<T> &v, const T *in, const T *inh, const T *sb0, T *out)
+template <typename T>
+__device__ __forceinline__ void v_stage(const inst_view<T> &v, const T *in, const T *inh, const T *sb0, T *out, int l0,
+                                        int ls)
 {
     const int nx = v.nx, ny = v.ny, e = v.e_v;
-    for (int i = 1 + threadIdx.x; i <= nx - 2; i += BS) {
+    for (int i = 1 + l0; i <= nx - 2; i += ls) {
         const int ii = ldg(v.imap + i);
         const T lo = sb0[ii];
         const T hi = ldg(v.X[X_VHI] + ii);
@@ -384,23 +388,24 @@ template <typename T, int BS>
 __device__ __forceinline__ void fwd_step(const inst_view<T> &v, int scheme, const T *U, T *Y1, T *Y2, T *Y3, T *Vn,
                                          T *sb0, double bnc)
 {
-    b1_stage<T, BS>(v, U, sb0, bnc);
-    s_stage<T, BS, 1>(v, scheme, U, nullptr, nullptr, Y1);
+    const int l0 = threadIdx.x;
+    b1_stage<T>(v, U, sb0, bnc, l0, BS);
+    s_stage<T, 1>(v, scheme, U, nullptr, nullptr, Y1, l0, BS);
     __syncthreads();
     if (scheme == LSS_ADI_DOUGLAS_RACHFORD) {
-        v_stage<T, BS>(v, U, Y1, sb0, Vn);
+        v_stage<T>(v, U, Y1, sb0, Vn, l0, BS);
     } else {
-        v_stage<T, BS>(v, U, Y1, sb0, Y2);
+        v_stage<T>(v, U, Y1, sb0, Y2, l0, BS);
         __syncthreads();
-        s_stage<T, BS, 2>(v, scheme, U, Y1, Y2, Y3);
+        s_stage<T, 2>(v, scheme, U, Y1, Y2, Y3, l0, BS);
         __syncthreads();
         if (scheme == LSS_ADI_HUNDSDORFER_VERWER)
-            v_stage<T, BS>(v, Y2, Y3, sb0, Vn);
+            v_stage<T>(v, Y2, Y3, sb0, Vn, l0, BS);
         else
-            v_stage<T, BS>(v, U, Y3, sb0, Vn);
+            v_stage<T>(v, U, Y3, sb0, Vn, l0, BS);
     }
     __syncthreads();
-    b2_stage<T, BS>(v, Vn);
+    b2_stage<T>(v, Vn, l0, BS);
     __syncthreads();
 }
 
@@ -578,6 +583,59 @@ template <int BS> __global__ void __launch_bounds__(BS) k_batch_fwdadj(bparams<d
 }
 
 // ------------------------------------------------------------------------------------------
+// wide path: one (large) instance, one kernel per stage over all threads of the grid, same
+// stage arithmetic as the batched kernel (bit-identical results for the same instance)
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ int gtid() { return blockIdx.x * blockDim.x + threadIdx.x; }
+__device__ __forceinline__ int gstride() { return gridDim.x * blockDim.x; }
+
+template <typename T> __global__ void k_wide_b1(bparams<T> p, const T *U, T *b0)
+{
+    const bdesc d = p.desc[0];
+    const inst_view<T> v = make_view(p, d);
+    b1_stage<T>(v, U, b0, d.bnc, gtid(), gstride());
+}
+template <typename T, int KIND>
+__global__ void k_wide_s(bparams<T> p, const T *U, const T *Y1, const T *Y2, T *Y)
+{
+    const bdesc d = p.desc[0];
+    const inst_view<T> v = make_view(p, d);
+    s_stage<T, KIND>(v, d.scheme, U, Y1, Y2, Y, gtid(), gstride());
+}
+template <typename T> __global__ void k_wide_v(bparams<T> p, const T *in, const T *inh, const T *b0, T *out)
+{
+    const bdesc d = p.desc[0];
+    const inst_view<T> v = make_view(p, d);
+    v_stage<T>(v, in, inh, b0, out, gtid(), gstride());
+}
+template <typename T> __global__ void k_wide_b2(bparams<T> p, T *Vn)
+{
+    const bdesc d = p.desc[0];
+    const inst_view<T> v = make_view(p, d);
+    b2_stage<T>(v, Vn, gtid(), gstride());
+}
+// value, finiteness flag and final-array flag of the single instance
+template <typename T> __global__ void k_wide_finish(bparams<T> p, const T *U)
+{
+    __shared__ int bad;
+    const bdesc d = p.desc[0];
+    if (threadIdx.x == 0) bad = 0;
+    __syncthreads();
+    const long long n = (long long)d.nx * d.ny;
+    int b = 0;
+    for (long long q = threadIdx.x; q < n; q += blockDim.x) b |= !isfinite(static_cast<double>(U[q]));
+    if (b) atomicOr(&bad, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const long long o = (long long)d.i0 * d.ny + d.j0;
+        p.values[0] = d.w00 * static_cast<double>(U[o]) + d.w10 * static_cast<double>(U[o + d.ny]) +
+                      d.w01 * static_cast<double>(U[o + 1]) + d.w11 * static_cast<double>(U[o + d.ny + 1]);
+        p.status[0] = bad;
+        p.final_in_v[0] = d.steps & 1;
+    }
+}
+
+// ------------------------------------------------------------------------------------------
 // host side
 // ------------------------------------------------------------------------------------------
 template <typename T> struct batch_typed {
@@ -608,6 +666,7 @@ template <typename T> struct batch_typed {
     ~batch_typed()
     {
         if (graph) cudaGraphExecDestroy(graph);
+        if (wide_graph) cudaGraphExecDestroy(wide_graph);
     }
 
     bparams<T> params()
@@ -640,6 +699,11 @@ template <typename T> struct batch_typed {
 
     int create(const lss_adi_problem *ps, int n);
     int prepare_adjoint(cudaStream_t s);
+    // wide path (count == 1)
+    dbuf<T> d_b0;
+    cudaGraphExec_t wide_graph = nullptr;
+    int enqueue_wide(cudaStream_t s);
+    int run_wide(cudaStream_t s, bool use_graph);
     int enqueue(int mode, cudaStream_t s);
     int run(int mode, cudaStream_t s, bool use_graph);
 };
@@ -886,6 +950,65 @@ template <typename T> int batch_typed<T>::enqueue(int mode, cudaStream_t s)
     return LSS_ADI_OK;
 }
 
+template <typename T> int batch_typed<T>::enqueue_wide(cudaStream_t s)
+{
+    const bdesc &d = desc[0];
+    if (!d_b0.p) LSS_CUDA_TRY(d_b0.alloc(d.nx), "wide: allocating boundary column");
+    bparams<T> p = params();
+    T *U = p.U, *V = p.V, *Y1 = p.Y1, *Y2 = p.Y2, *Y3 = p.Y3, *b0 = d_b0.p;
+    LSS_CUDA_TRY(cudaMemcpyAsync(U, d_payoff.p, total_n * sizeof(T), cudaMemcpyDeviceToDevice, s), "wide: initial state");
+    // small blocks spread the few hundred to few thousand lines over as many SMs as possible
+    const int bs = 32;
+    const int gS = grid_for(d.ny - 2, bs), gV = grid_for(d.nx - 2, bs);
+    const int gX = grid_for(d.nx, 128), gY = grid_for(d.ny, 128);
+    long long nl = 0;
+    for (int step = 0; step < d.steps; ++step) {
+        k_wide_b1<T><<<gX, 128, 0, s>>>(p, U, b0);
+        k_wide_s<T, 1><<<gS, bs, 0, s>>>(p, U, nullptr, nullptr, Y1);
+        if (d.scheme == LSS_ADI_DOUGLAS_RACHFORD) {
+            k_wide_v<T><<<gV, bs, 0, s>>>(p, U, Y1, b0, V);
+            nl += 3;
+        } else {
+            k_wide_v<T><<<gV, bs, 0, s>>>(p, U, Y1, b0, Y2);
+            k_wide_s<T, 2><<<gS, bs, 0, s>>>(p, U, Y1, Y2, Y3);
+            if (d.scheme == LSS_ADI_HUNDSDORFER_VERWER)
+                k_wide_v<T><<<gV, bs, 0, s>>>(p, Y2, Y3, b0, V);
+            else
+                k_wide_v<T><<<gV, bs, 0, s>>>(p, U, Y3, b0, V);
+            nl += 5;
+        }
+        k_wide_b2<T><<<gY, 128, 0, s>>>(p, V);
+        nl += 1;
+        std::swap(U, V);
+    }
+    k_wide_finish<T><<<1, 256, 0, s>>>(p, U);
+    LSS_CUDA_TRY(cudaGetLastError(), "wide: launching the time loop");
+    launches = nl + 1;
+    return LSS_ADI_OK;
+}
+
+template <typename T> int batch_typed<T>::run_wide(cudaStream_t s, bool use_graph)
+{
+    if (count != 1) return set_error(LSS_ADI_EINVAL, "wide path: one instance only");
+    if (!use_graph) return enqueue_wide(s);
+    if (!wide_graph) {
+        cudaStream_t cs;
+        LSS_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "wide: capture stream");
+        LSS_CUDA_TRY(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "wide: begin capture");
+        const int rc = enqueue_wide(cs);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(cs, &g);
+        cudaStreamDestroy(cs);
+        if (rc) return rc;
+        LSS_CUDA_TRY(e, "wide: end capture");
+        e = cudaGraphInstantiate(&wide_graph, g, 0);
+        cudaGraphDestroy(g);
+        LSS_CUDA_TRY(e, "wide: instantiate graph");
+    }
+    LSS_CUDA_TRY(cudaGraphLaunch(wide_graph, s), "wide: graph launch");
+    return LSS_ADI_OK;
+}
+
 template <typename T> int batch_typed<T>::run(int mode, cudaStream_t s, bool use_graph)
 {
     if (mode == 1) {
@@ -911,6 +1034,68 @@ template <typename T> int batch_typed<T>::run(int mode, cudaStream_t s, bool use
         graph_mode = mode;
     }
     LSS_CUDA_TRY(cudaGraphLaunch(graph, s), "batch: graph launch");
+    return LSS_ADI_OK;
+}
+
+template <typename T> struct wide_solver : wide_solver_base {
+    batch_typed<T> b;
+    std::vector<T> x, y, pay0;
+
+    int init(const lss_adi_problem &p)
+    {
+        instance_tables<T> tt;
+        build_tables_for<T>(p, tt);
+        x = tt.x;
+        y = tt.y;
+        pay0 = tt.payoff;
+        return b.create(&p, 1);
+    }
+    int forward(const void *payoff, void *out_surface, double *out_value, int flags, void *stream, bool use_graph) override
+    {
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        const bool dev = (flags & LSS_ADI_DEVICE_POINTERS) != 0;
+        const size_t n = static_cast<size_t>(b.total_n);
+        const void *src = payoff ? payoff : static_cast<const void *>(pay0.data());
+        LSS_CUDA_TRY(cudaMemcpyAsync(b.d_payoff.p, src, n * sizeof(T),
+                                     (payoff && dev) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s),
+                     "wide: copying the terminal condition");
+        int rc = b.run_wide(s, use_graph);
+        if (rc) return rc;
+        if (out_value)
+            LSS_CUDA_TRY(cudaMemcpyAsync(out_value, b.d_values.p, sizeof(double), cudaMemcpyDeviceToHost, s), "wide: value");
+        if (out_surface) {
+            const T *fin = b.state.p + ((b.desc[0].steps & 1) ? b.total_n : 0);
+            LSS_CUDA_TRY(cudaMemcpyAsync(out_surface, fin, n * sizeof(T), dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s),
+                         "wide: surface");
+        }
+        if (!dev || out_value) LSS_CUDA_TRY(cudaStreamSynchronize(s), "wide: time loop");
+        return LSS_ADI_OK;
+    }
+    int grid(void *gx, void *gy) const override
+    {
+        std::copy(x.begin(), x.end(), static_cast<T *>(gx));
+        std::copy(y.begin(), y.end(), static_cast<T *>(gy));
+        return LSS_ADI_OK;
+    }
+};
+
+int make_wide_solver(const lss_adi_problem &p, std::unique_ptr<wide_solver_base> &out)
+{
+    try {
+        if (p.precision == LSS_ADI_FP64) {
+            std::unique_ptr<wide_solver<double>> w(new wide_solver<double>());
+            int rc = w->init(p);
+            if (rc) return rc;
+            out = std::move(w);
+        } else {
+            std::unique_ptr<wide_solver<float>> w(new wide_solver<float>());
+            int rc = w->init(p);
+            if (rc) return rc;
+            out = std::move(w);
+        }
+    } catch (const std::bad_alloc &) {
+        return set_error(LSS_ADI_ENOMEM, "wide: host allocation failed");
+    }
     return LSS_ADI_OK;
 }
 

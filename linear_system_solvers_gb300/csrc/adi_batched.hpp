@@ -23,4 +23,14 @@ struct adjoint_solver {
             void *stream);
 };
 
+// Single instance on the factorised ("fast") arithmetic: one kernel per stage over the whole
+// GPU, graph-replayed time loop (behind lss_adi_create with LSS_ADI_ARITH_FAST).
+struct wide_solver_base {
+    virtual ~wide_solver_base() = default;
+    virtual int forward(const void *payoff, void *out_surface, double *out_value, int flags, void *stream,
+                        bool use_graph) = 0;
+    virtual int grid(void *x, void *y) const = 0;
+};
+int make_wide_solver(const lss_adi_problem &p, std::unique_ptr<wide_solver_base> &out);
+
 } // namespace lss_gb300

@@ -81,3 +81,31 @@ def test_batch_config3_sample_within_1e10(lss, oracle):
     for k, p in enumerate(probs):
         want = oracle.solve(oracle_of(oracle, p), "f64")
         assert rel_err(b.surface(k), want) < fp64_tol(want, p.s_hi)
+
+
+def test_wide_single_instance_path_is_bitwise_the_batched_kernel(lss):
+    """lss_adi_create(FAST) runs the same stage arithmetic as one kernel per stage over the
+    whole GPU; for an instance that also fits the batched kernel the bits must agree."""
+    probs = mixed_batch(lss, seed=21, count=8)
+    b = lss.BatchSolver(probs, precision="f64")
+    b.run(0)
+    values, _, _ = b.results()
+    for k, p in enumerate(probs):
+        got, v = lss.ImplicitHestonSolver(p, precision="f64", arith="fast").solve()
+        assert np.array_equal(got, b.surface(k), equal_nan=True)
+        assert v == values[k] or (np.isnan(v) and np.isnan(values[k]))
+
+
+@pytest.mark.parametrize("fp", ["f64", "f32"])
+def test_wide_path_large_grid(lss, oracle, fp):
+    kw = dict(model="heston", kappa=1.5, theta_v=0.04, sigma=0.3, rho=-0.5, rate=0.02, strike=100.0, maturity=1.0,
+              s_lo=0.0, s_hi=200.0, v_lo=0.0, v_hi=1.2, nx=401, ny=201, nt=11, scheme="hv", acc_point=100.0, **NU)
+    p = lss.HestonProblem(**kw)
+    got, _ = lss.ImplicitHestonSolver(p, precision=fp, arith="fast").solve(graph=True)
+    op = oracle_of(oracle, p)
+    if fp == "f64":
+        want = oracle.solve(op, "f64")
+        assert rel_err(got, want) < fp64_tol(want, p.s_hi)
+    else:
+        ok, e_dev, e_ref = fp32_ok(got, oracle.solve(op, "f32"), oracle.solve(op, "f64"))
+        assert ok, (e_dev, e_ref)
