@@ -42,6 +42,8 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=32, help="instances timed on the host cores")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip timing the plain per-instance device path")
+    ap.add_argument("--configs", default="", help="comma list of single-instance configurations to measure instead "
+                    "of the batched headline: c1, c2, c5, c5sabr (one JSON line each)")
     return ap.parse_args()
 
 
@@ -182,6 +184,11 @@ def main():
 
     from linear_system_solvers_gb300.batch import draw_batch, grid_point_steps
 
+    if args.configs:
+        if rank == 0:
+            run_configs(args)
+        return
+
     if args.impl == "reference":
         # the reference's own CPU path on the host cores; rank 0 only
         if rank != 0:
@@ -317,6 +324,110 @@ def main():
     print(json.dumps(out))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+# ------------------------------------------------------------------------------------------
+# single-instance configurations (measured with --configs; parity against the oracle)
+# ------------------------------------------------------------------------------------------
+CONFIG1 = dict(model="heston", kappa=1.5, theta_v=0.04, sigma=0.3, rho=-0.9, rate=0.02, strike=100.0, maturity=1.0,
+               s_lo=0.0, s_hi=200.0, v_lo=0.0, v_hi=1.2, nx=100, ny=50, nt=201, scheme="dr", eval_s=100.0,
+               eval_v=0.04)
+NU_K100 = dict(nonuniform=True, acc_point=100.0, alpha_scale=10.0, beta_scale=24.0)
+
+
+def _rel_err(a, ref):
+    import numpy as np
+
+    a = np.asarray(a, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    if not np.all(np.isfinite(ref)):
+        return float("nan")
+    den = np.maximum(np.abs(ref), 1e-3 * np.abs(ref).max())
+    return float(np.max(np.abs(a - ref) / den))
+
+
+def _time_solver(solver, reps):
+    import torch
+
+    solver.solve(graph=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        surf, val = solver.solve(graph=True)
+    torch.cuda.synchronize()
+    return (time.perf_counter() - t0) / reps, surf, val
+
+
+def run_configs(args):
+    import dataclasses
+
+    import numpy as np
+    import torch
+
+    import linear_system_solvers_gb300 as lss
+    from oracle import oracle as O
+
+    O.build()
+    torch.cuda.set_device(0)
+    wanted = [c.strip() for c in args.configs.split(",") if c.strip()]
+
+    def oracle_problem(p, nt=None):
+        kw = {k: v for k, v in dataclasses.asdict(p).items() if k not in ("eval_s", "eval_v", "fp64_tables")}
+        if nt is not None:
+            kw["nt"] = nt
+        return O.Problem(**kw)
+
+    def case(name, p, fp, reps, oracle_nt=None):
+        gps = p.nx * p.ny * (p.nt - 1)
+        s = lss.ImplicitHestonSolver(p, precision=fp, arith="fast")
+        secs, surf, val = _time_solver(s, reps)
+        rec = {"config": name, "precision": fp, "scheme": p.scheme, "grid": [p.nx, p.ny, p.nt - 1],
+               "device_gps": gps / secs, "device_seconds": secs, "value": val, "path": "wide (kernel per stage, graph)"}
+        # parity against the oracle (full run, or the first oracle_nt - 1 steps for the largest grids)
+        if oracle_nt is not None:
+            p_short = dataclasses.replace(p, nt=oracle_nt)
+            surf = lss.ImplicitHestonSolver(p_short, precision=fp, arith="fast").solve()[0]
+            op = oracle_problem(p, oracle_nt)
+            rec["parity_steps"] = oracle_nt - 1
+        else:
+            op = oracle_problem(p)
+        t0 = time.perf_counter()
+        ref64 = O.solve(op, "f64")
+        cpu_s = time.perf_counter() - t0
+        rec["cpu_oracle_gps_1core"] = op.nx * op.ny * (op.nt - 1) / cpu_s
+        rec["rel_err_vs_fp64_oracle"] = _rel_err(surf, ref64)
+        rec["oracle_unstable"] = bool((not np.all(np.isfinite(ref64))) or np.abs(ref64).max() > 10 * p.s_hi)
+        if fp == "f32":
+            rec["rel_err_reference_fp32_vs_fp64"] = _rel_err(O.solve(op, "f32"), ref64)
+        print(json.dumps(rec), flush=True)
+
+    if "c1" in wanted:
+        p = lss.HestonProblem(**CONFIG1)
+        case("config1 DR 100x50x200", p, "f64", 20)
+        ref = lss.ImplicitHestonSolver(p, precision="f64", arith="reference")
+        secs, surf, _ = _time_solver(ref, 5)
+        print(json.dumps({"config": "config1 DR 100x50x200", "path": "reference-order plain kernels (bitwise)",
+                          "device_gps": p.nx * p.ny * (p.nt - 1) / secs,
+                          "bitwise_equal_oracle": bool(np.array_equal(surf, O.solve(oracle_problem(p), "f64")))}),
+              flush=True)
+    if "c2" in wanted:
+        for scheme in ("cs", "mcs", "hv"):
+            for fp in ("f64", "f32"):
+                p = lss.HestonProblem(**dict(CONFIG1, scheme=scheme, nx=400, ny=200, nt=501, **NU_K100))
+                case(f"config2 {scheme.upper()} 400x200x500", p, fp, 2)
+            # stable companion (rho = 0) on the same grid
+            p = lss.HestonProblem(**dict(CONFIG1, scheme=scheme, rho=0.0, nx=400, ny=200, nt=501, **NU_K100))
+            case(f"config2 {scheme.upper()} 400x200x500 rho=0 companion", p, "f64", 2)
+    if "c5" in wanted:
+        for fp in ("f64", "f32"):
+            p = lss.HestonProblem(**dict(CONFIG1, scheme="hv", nx=4096, ny=2048, nt=1001, **NU_K100))
+            case("config5 HV 4096x2048x1000", p, fp, 1, oracle_nt=11)
+    if "c5sabr" in wanted:
+        p = lss.HestonProblem(model="sabr", sigma=0.4, rho=-0.3, sabr_beta=0.5, rate=0.0, strike=0.05, maturity=2.0,
+                              s_lo=0.0, s_hi=0.2, v_lo=0.0, v_hi=1.0, nx=2048, ny=1024, nt=801, scheme="dr",
+                              nonuniform=True, acc_point=0.05, alpha_scale=10.0, beta_scale=24.0, eval_s=0.05,
+                              eval_v=0.2)
+        case("config5 SABR DR 2048x1024x800", p, "f64", 1, oracle_nt=11)
 
 
 def time_plain_path(lss, problems, stream, batched_value, m=64):

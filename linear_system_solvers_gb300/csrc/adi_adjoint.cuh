@@ -25,14 +25,15 @@ struct adj_acc {
 };
 
 // B2^T: fold the S_max extrapolation row into rows nx-2 / nx-3; clear rows 0 and nx-1 of UB.
-__device__ __forceinline__ void adj_b2(const inst_view<double> &v, double *VB, double *UB, int l0, int ls)
+__device__ __forceinline__ void adj_b2(const inst_view<double> &v, double *__restrict__ VB, double *__restrict__ UB, int l0,
+                                       int ls)
 {
     const int nx = v.nx, ny = v.ny, lri = nx - 1;
     const double four3 = 4.0 / 3.0, third = 1.0 / 3.0;
     for (int q = l0; q < ny; q += ls) {
         double add = 0.0;
-        if (__ldg(v.jmap + q) == q) add += VB[(long long)lri * ny + q];
-        if (q + 1 < ny && __ldg(v.jmap + q + 1) == q) add += VB[(long long)lri * ny + q + 1];
+        if (__ldg(v.jmap() + q) == q) add += VB[(long long)lri * ny + q];
+        if (q + 1 < ny && __ldg(v.jmap() + q + 1) == q) add += VB[(long long)lri * ny + q + 1];
         VB[(long long)(lri - 1) * ny + q] += four3 * add;
         VB[(long long)(lri - 2) * ny + q] -= third * add;
         UB[q] = 0.0;
@@ -44,15 +45,18 @@ __device__ __forceinline__ void adj_b2(const inst_view<double> &v, double *VB, d
 // in/out: the stage's `in` array and its output; INB (+)= adjoint of `in`; INHB (+)= adjoint
 // of `inh`; LV (+)= adjoint of the line's lo value.
 template <bool FIRST>
-__device__ __forceinline__ void adj_v(const inst_view<double> &v, const double *in, const double *out, const double *XB,
-                                      double *INB, double *INHB, double *TMP, double *LV, adj_acc &acc, int l0, int ls)
+__device__ __forceinline__ void adj_v(const inst_view<double> &v, const double *__restrict__ in,
+                                      const double *__restrict__ out, const double *__restrict__ XB,
+                                      double *__restrict__ INB, double *__restrict__ INHB, double *__restrict__ TMP,
+                                      double *__restrict__ LV, adj_acc &acc, int l0, int ls)
 {
     const int nx = v.nx, ny = v.ny, e = ny - 2;
     for (int i = 1 + l0; i <= nx - 2; i += ls) {
         const long long row = (long long)i * ny;
         double z = 0.0;
+#pragma unroll 4
         for (int t = 1; t <= e; ++t) {
-            const double gprev = (t > 1) ? __ldg(v.Vt[VL_G] + (long long)(t - 1) * nx + i) : 0.0;
+            const double gprev = (t > 1) ? __ldg(v.Vt(VL_G) + (long long)(t - 1) * nx + i) : 0.0;
             z = XB[row + t] - gprev * z;
             TMP[row + t] = z;
         }
@@ -61,11 +65,12 @@ __device__ __forceinline__ void adj_v(const inst_view<double> &v, const double *
         // windows of (in - out) at t+1 and t
         double dn = in[row + e + 1] - out[row + e + 1];
         double dc = in[row + e] - out[row + e];
+#pragma unroll 4
         for (int t = e; t >= 1; --t) {
             const long long ot = (long long)t * nx + i;
             w = TMP[row + t] - la_next * w;
-            const double la = __ldg(v.Vt[VL_LA] + ot), vc = __ldg(v.Vt[VL_VC] + ot), vn = __ldg(v.Vt[VL_VN] + ot);
-            const double ib = __ldg(v.Vt[VL_IB] + ot);
+            const double la = __ldg(v.Vt(VL_LA) + ot), vc = __ldg(v.Vt(VL_VC) + ot), vn = __ldg(v.Vt(VL_VN) + ot);
+            const double ib = __ldg(v.Vt(VL_IB) + ot);
             const double fin = acc_t1 + vn * w; // adjoint of in(t+1) is complete
             if (FIRST) INB[row + t + 1] = fin; else INB[row + t + 1] += fin;
             acc_t1 = acc_t + vc * w;
@@ -74,10 +79,10 @@ __device__ __forceinline__ void adj_v(const inst_view<double> &v, const double *
             if (FIRST) INHB[row + t] = mu; else INHB[row + t] += mu;
             const double dm = in[row + t - 1] - out[row + t - 1];
             const double q = mu * (dm - dn);
-            acc.vk += q * __ldg(v.Yv[Y_EK] + t);
-            acc.vt += q * __ldg(v.Yv[Y_ET] + t);
-            acc.vs1 += q * __ldg(v.Yv[Y_ES] + t);
-            acc.vs2 += mu * (2.0 * dc - dm - dn) * __ldg(v.Yv[Y_BS] + t);
+            acc.vk += q * __ldg(v.Yv(Y_EK) + t);
+            acc.vt += q * __ldg(v.Yv(Y_ET) + t);
+            acc.vs1 += q * __ldg(v.Yv(Y_ES) + t);
+            acc.vs2 += mu * (2.0 * dc - dm - dn) * __ldg(v.Yv(Y_BS) + t);
             acc.vb += mu * dc;
             dn = dc;
             dc = dm;
@@ -94,33 +99,38 @@ __device__ __forceinline__ void adj_v(const inst_view<double> &v, const double *
 // stage of CS/MCS (output Y3).  XB: adjoint of the stage output; FB receives the scaled
 // right-hand-side adjoint w; LS/HS the lo/hi adjoints of the line.
 template <int KIND>
-__device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d, const double *U, const double *Y1,
-                                      const double *Y2, const double *Yo, const double *XB, double *FB, double *TMP,
-                                      double *LS, double *HS, double *UB, double *Y1B, adj_acc &acc, int l0, int ls)
+__device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d, const double *__restrict__ U,
+                                      const double *__restrict__ Y1, const double *__restrict__ Y2,
+                                      const double *__restrict__ Yo, const double *__restrict__ XB,
+                                      double *__restrict__ FB, double *__restrict__ TMP, double *__restrict__ LS,
+                                      double *__restrict__ HS, double *__restrict__ UB, double *__restrict__ Y1B,
+                                      adj_acc &acc, int l0, int ls)
 {
     const int nx = v.nx, ny = v.ny, e = nx - 2;
     const double th = d.a_theta;
     const double zt = (d.scheme == LSS_ADI_MODIFIED_CRAIG_SNEYD) ? (d.a_zeta - th) : 0.0;
     for (int j = 1 + l0; j <= ny - 2; j += ls) {
         double z = 0.0;
+#pragma unroll 4
         for (int t = 1; t <= e; ++t) {
             const long long o = (long long)t * ny + j;
-            const double gprev = (t > 1) ? __ldg(v.S[SL_G] + o - ny) : 0.0;
+            const double gprev = (t > 1) ? __ldg(v.S(SL_G) + o - ny) : 0.0;
             z = XB[o] - gprev * z;
             TMP[o] = z;
         }
         double w = 0.0, la_next = 0.0, w_e = 0.0;
         double acc_t1 = 0.0, acc_t = 0.0;
         double pA = 0.0, pB = 0.0, pQ = 0.0, pD = 0.0, pE = 0.0;
+#pragma unroll 2
         for (int t = e; t >= 1; --t) {
             const long long o = (long long)t * ny + j;
             w = TMP[o] - la_next * w;
             if (t == e) w_e = w;
             FB[o] = w;
-            const double la = __ldg(v.S[SL_LA] + o);
-            const double ib = __ldg(v.S[SL_IB] + o);
+            const double la = __ldg(v.S(SL_LA) + o);
+            const double ib = __ldg(v.S(SL_IB) + o);
             const double mu = ib * w;
-            const double hx = __ldg(v.X[X_HX] + t);
+            const double hx = __ldg(v.X(X_HX) + t);
             const double Uw = U[o - ny], Uc = U[o], Ue = U[o + ny], Us = U[o - 1], Un = U[o + 1];
             double sM, sZ, sP, sMt, sW, sPt, sC;
             if constexpr (KIND == 1) {
@@ -134,7 +144,7 @@ __device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d
                 sC = d.a_gamma * ((U[o - ny - 1] - U[o - ny + 1]) + (U[o + ny + 1] - U[o + ny - 1]));
             } else {
                 // along-line terms of the second S stage: la U(t-1) + sc U(t) + se U(t+1) + ib Y1(t)
-                const double sc = __ldg(v.S[SL_S2SC] + o), se = __ldg(v.S[SL_S2SE] + o);
+                const double sc = __ldg(v.S(SL_S2SC) + o), se = __ldg(v.S(SL_S2SE) + o);
                 const double fin = acc_t1 + se * w;
                 UB[o + ny] += fin;
                 acc_t1 = acc_t + sc * w;
@@ -164,9 +174,9 @@ __device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d
             UB[j] += acc_t;
         }
         LS[j] = -la_next * w + XB[j];
-        HS[j] = -__ldg(v.Yv[Y_CHS] + j) * w_e + XB[(long long)(nx - 1) * ny + j];
-        const double ek = __ldg(v.Yv[Y_EK] + j), et = __ldg(v.Yv[Y_ET] + j), es = __ldg(v.Yv[Y_ES] + j);
-        const double bs = __ldg(v.Yv[Y_BS] + j), hy = __ldg(v.Yv[Y_HY] + j);
+        HS[j] = -__ldg(v.Yv(Y_CHS) + j) * w_e + XB[(long long)(nx - 1) * ny + j];
+        const double ek = __ldg(v.Yv(Y_EK) + j), et = __ldg(v.Yv(Y_ET) + j), es = __ldg(v.Yv(Y_ES) + j);
+        const double bs = __ldg(v.Yv(Y_BS) + j), hy = __ldg(v.Yv(Y_HY) + j);
         acc.s[0] += d.a_delta * pA + d.a_halfk * pB;
         acc.s[1] += d.a_ni * ek * pQ;
         acc.s[2] += d.a_ni * et * pQ;
@@ -179,29 +189,32 @@ __device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d
 // (and Y2B for KIND 2), the lo/hi adjoints of the S lines, and for KIND 1 the adjoint of
 // the explicit v = v_lo boundary column (B1^T) with its parameter sensitivities.
 template <int KIND>
-__device__ __forceinline__ void adj_gather(const inst_view<double> &v, const bdesc &d, const double *U, const double *FB,
-                                           const double *LS, const double *HS, const double *LV, double *UB,
-                                           double *Y2B, adj_acc &acc, int l0, int ls)
+__device__ __forceinline__ void adj_gather(const inst_view<double> &v, const bdesc &d, const double *__restrict__ U,
+                                           const double *__restrict__ FB, const double *__restrict__ LS,
+                                           const double *__restrict__ HS, const double *__restrict__ LV,
+                                           double *__restrict__ UB, double *__restrict__ Y2B, adj_acc &acc, int l0,
+                                           int ls)
 {
     const int nx = v.nx, ny = v.ny;
     auto F = [&](int p, int q) -> double {
         return (p >= 1 && p <= nx - 2 && q >= 1 && q <= ny - 2) ? FB[(long long)p * ny + q] : 0.0;
     };
     auto W = [&](int slot, int p, int q) -> double {
-        return (p >= 1 && p <= nx - 2 && q >= 1 && q <= ny - 2) ? __ldg(v.S[slot] + (long long)p * ny + q) : 0.0;
+        return (p >= 1 && p <= nx - 2 && q >= 1 && q <= ny - 2) ? __ldg(v.S(slot) + (long long)p * ny + q) : 0.0;
     };
     // lo-value adjoint of the explicit boundary column: bbar0(i) = sum over v lines i' with imap[i'] = i
     auto B0 = [&](int i) -> double {
         if (i < 1 || i > nx - 2) return 0.0;
         double s = 0.0;
-        if (__ldg(v.imap + i) == i) s += LV[i];
-        if (i + 1 <= nx - 2 && __ldg(v.imap + i + 1) == i) s += LV[i + 1];
+        if (__ldg(v.imap() + i) == i) s += LV[i];
+        if (i + 1 <= nx - 2 && __ldg(v.imap() + i + 1) == i) s += LV[i + 1];
         return s;
     };
     for (int q = l0; q < ny; q += ls) {
         double lsum = 0.0, hsum = 0.0;
-        if (q >= 1 && q <= ny - 2 && __ldg(v.jmap + q) == q) { lsum += LS[q]; hsum += HS[q]; }
-        if (q + 1 <= ny - 2 && __ldg(v.jmap + q + 1) == q) { lsum += LS[q + 1]; hsum += HS[q + 1]; }
+        if (q >= 1 && q <= ny - 2 && __ldg(v.jmap() + q) == q) { lsum += LS[q]; hsum += HS[q]; }
+        if (q + 1 <= ny - 2 && __ldg(v.jmap() + q + 1) == q) { lsum += LS[q + 1]; hsum += HS[q + 1]; }
+#pragma unroll 2
         for (int p = 0; p < nx; ++p) {
             const long long o = (long long)p * ny + q;
             double val = 0.0;
@@ -220,24 +233,24 @@ __device__ __forceinline__ void adj_gather(const inst_view<double> &v, const bde
                        W(SL_WG, p - 1, q + 1) * F(p - 1, q + 1) + W(SL_WG, p - 1, q - 1) * F(p - 1, q - 1);
                 if (q <= 2) {
                     if (q == 0) {
-                        val += (p + 1 <= nx - 2 ? __ldg(v.X[XB_M] + p + 1) * B0(p + 1) : 0.0) +
-                               __ldg(v.X[XB_C] + p) * B0(p) + (p >= 1 ? __ldg(v.X[XB_P] + p - 1) * B0(p - 1) : 0.0);
+                        val += (p + 1 <= nx - 2 ? __ldg(v.X(XB_M) + p + 1) * B0(p + 1) : 0.0) +
+                               __ldg(v.X(XB_C) + p) * B0(p) + (p >= 1 ? __ldg(v.X(XB_P) + p - 1) * B0(p - 1) : 0.0);
                         if (p >= 1 && p <= nx - 2) {
                             const double bb = B0(p);
                             if (bb != 0.0) {
                                 const double u0 = U[o], u1 = U[o + 1], u2 = U[o + 2];
                                 const double um = U[o - ny], up = U[o + ny];
                                 const double ee = d.a_ni * bb * (4.0 * u1 - 3.0 * u0 - u2);
-                                acc.s[0] += bb * (d.a_delta * __ldg(v.X[X_HX] + p) * (up - um) - d.a_k * u0);
-                                acc.s[1] += ee * __ldg(v.Yv[Y_EK]);
-                                acc.s[2] += ee * __ldg(v.Yv[Y_ET]);
-                                acc.s[3] += ee * __ldg(v.Yv[Y_ES]);
+                                acc.s[0] += bb * (d.a_delta * __ldg(v.X(X_HX) + p) * (up - um) - d.a_k * u0);
+                                acc.s[1] += ee * __ldg(v.Yv(Y_EK));
+                                acc.s[2] += ee * __ldg(v.Yv(Y_ET));
+                                acc.s[3] += ee * __ldg(v.Yv(Y_ES));
                             }
                         }
                     } else if (q == 1) {
-                        val += __ldg(v.X[XB_1] + p) * B0(p);
+                        val += __ldg(v.X(XB_1) + p) * B0(p);
                     } else {
-                        val += __ldg(v.X[XB_2] + p) * B0(p);
+                        val += __ldg(v.X(XB_2) + p) * B0(p);
                     }
                 }
             }

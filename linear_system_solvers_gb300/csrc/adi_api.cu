@@ -18,7 +18,11 @@ int set_error(int code, const std::string &msg)
     g_last_error = msg;
     return code;
 }
-void clear_error() { g_last_error.clear(); }
+void clear_error()
+{
+    g_last_error.clear();
+    (void)cudaGetLastError(); // drop a stale non-sticky error of an earlier, unrelated call
+}
 
 // Mirrors the checks of general_heston_equation::initialize (lss_2d_general_heston_equation.hpp:104-131)
 // plus the size limits of the Dirichlet/Dirichlet Thomas LU path (n >= 4).

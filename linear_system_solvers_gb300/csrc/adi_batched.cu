@@ -187,15 +187,19 @@ __global__ void k_setup_v_lines(setup_params sp, T *V0, long long slot_stride, T
 // ------------------------------------------------------------------------------------------
 // the persistent time-loop kernel
 // ------------------------------------------------------------------------------------------
+// One instance's view of the arenas.  The arena base pointers stay in the kernel's parameter
+// space (__grid_constant__), so they cost no registers; only the offsets are carried.
 template <typename T> struct inst_view {
+    const bparams<T> *p;
     int nx, ny, e_s, e_v;
     long long o2;
-    T *U, *V, *Y1, *Y2, *Y3;
-    const T *S[SL_COUNT];
-    const T *Vt[VL_COUNT];
-    const T *X[X_COUNT];
-    const T *Yv[Y_COUNT];
-    const int *imap, *jmap;
+    int ox, oy;
+    __device__ __forceinline__ const T *S(int k) const { return p->S[k] + o2; }
+    __device__ __forceinline__ const T *Vt(int k) const { return p->Vt[k] + o2; }
+    __device__ __forceinline__ const T *X(int k) const { return p->X[k] + ox; }
+    __device__ __forceinline__ const T *Yv(int k) const { return p->Yv[k] + oy; }
+    __device__ __forceinline__ const int *imap() const { return p->imap + ox; }
+    __device__ __forceinline__ const int *jmap() const { return p->jmap + oy; }
 };
 
 template <typename T> __device__ __forceinline__ T ldg(const T *p) { return __ldg(p); }
@@ -204,20 +208,21 @@ template <typename T> __device__ __forceinline__ T ldg(const T *p) { return __ld
 // Work distribution of every stage: items l0, l0 + ls, ... (threads of one CTA in the
 // batched kernel; all threads of a grid in the per-stage kernels of the wide path).
 template <typename T>
-__device__ __forceinline__ void b1_stage(const inst_view<T> &v, const T *U, T *sb0, double bnc, int l0, int ls)
+__device__ __forceinline__ void b1_stage(const inst_view<T> &v, const T *__restrict__ U, T *__restrict__ sb0, double bnc,
+                                         int l0, int ls)
 {
     const int nx = v.nx, ny = v.ny, N = nx - 1;
     for (int i = l0; i < nx; i += ls) {
         T r;
         if (i == 0) {
-            r = ldg(v.Yv[Y_SLO]);
+            r = ldg(v.Yv(Y_SLO));
         } else if (i == N) {
-            r = ldg(v.X[XB_C] + i) * U[(long long)N * ny] + ldg(v.X[XB_1] + i) * U[(long long)N * ny + 1] +
-                ldg(v.X[XB_2] + i) * U[(long long)N * ny + 2] + static_cast<T>(bnc);
+            r = ldg(v.X(XB_C) + i) * U[(long long)N * ny] + ldg(v.X(XB_1) + i) * U[(long long)N * ny + 1] +
+                ldg(v.X(XB_2) + i) * U[(long long)N * ny + 2] + static_cast<T>(bnc);
         } else {
             const long long o = (long long)i * ny;
-            r = ldg(v.X[XB_M] + i) * U[o - ny] + ldg(v.X[XB_C] + i) * U[o] + ldg(v.X[XB_P] + i) * U[o + ny] +
-                ldg(v.X[XB_2] + i) * U[o + 2] + ldg(v.X[XB_1] + i) * U[o + 1];
+            r = ldg(v.X(XB_M) + i) * U[o - ny] + ldg(v.X(XB_C) + i) * U[o] + ldg(v.X(XB_P) + i) * U[o + ny] +
+                ldg(v.X(XB_2) + i) * U[o + 2] + ldg(v.X(XB_1) + i) * U[o + 1];
         }
         sb0[i] = r;
     }
@@ -229,10 +234,10 @@ template <typename T> __device__ __forceinline__ void b2_stage(const inst_view<T
     const int nx = v.nx, ny = v.ny, lri = nx - 1;
     const T four3 = T(4.0 / 3.0), third = T(1.0 / 3.0);
     for (int j = l0; j < ny; j += ls) {
-        Vn[j] = ldg(v.Yv[Y_SLO] + j);
-        const int jj = ldg(v.jmap + j);
+        Vn[j] = ldg(v.Yv(Y_SLO) + j);
+        const int jj = ldg(v.jmap() + j);
         Vn[(long long)lri * ny + j] =
-            four3 * Vn[(long long)(lri - 1) * ny + jj] - third * Vn[(long long)(lri - 2) * ny + jj] - ldg(v.Yv[Y_B2C] + j);
+            four3 * Vn[(long long)(lri - 1) * ny + jj] - third * Vn[(long long)(lri - 2) * ny + jj] - ldg(v.Yv(Y_B2C) + j);
     }
 }
 
@@ -240,30 +245,32 @@ template <typename T> __device__ __forceinline__ void b2_stage(const inst_view<T
 // CS/MCS/HV on U, Y1, Y2 (scheme chooses the weights).  Thread per line j; every access
 // of a warp is one coalesced row segment.
 template <typename T, int KIND>
-__device__ __forceinline__ void s_stage(const inst_view<T> &v, int scheme, const T *U, const T *Y1, const T *Y2, T *Y,
-                                        int l0, int ls)
+__device__ __forceinline__ void s_stage(const inst_view<T> &v, int scheme, const T *__restrict__ U,
+                                        const T *__restrict__ Y1, const T *__restrict__ Y2, T *__restrict__ Y, int l0,
+                                        int ls)
 {
     const int nx = v.nx, ny = v.ny, e = v.e_s;
     for (int j = 1 + l0; j <= ny - 2; j += ls) {
-        const int jj = ldg(v.jmap + j);
+        const int jj = ldg(v.jmap() + j);
         const T lo = U[jj], hi = U[(long long)(nx - 1) * ny + jj];
         T y = lo;
         if constexpr (KIND == 1) {
             // sliding 3x3 window of U
             T u0m = U[j - 1], u0c = U[j], u0p = U[j + 1];
             T u1m = U[ny + j - 1], u1c = U[ny + j], u1p = U[ny + j + 1];
+#pragma unroll 4
             for (int t = 1; t <= e; ++t) {
                 const long long o = (long long)t * ny + j;
                 const T u2m = U[o + ny - 1], u2c = U[o + ny], u2p = U[o + ny + 1];
                 const T mix = (u0m - u0p) + (u2p - u2m);
-                T f = ldg(v.S[SL_WG] + o) * mix;
-                f += ldg(v.S[SL_WW] + o) * u0c;
-                f += ldg(v.S[SL_WS] + o) * u1m;
-                f += ldg(v.S[SL_WC] + o) * u1c;
-                f += ldg(v.S[SL_WN] + o) * u1p;
-                f += ldg(v.S[SL_WE] + o) * u2c;
-                y = f - ldg(v.S[SL_LA] + o) * y;
-                if (t == e) y -= ldg(v.Yv[Y_CHS] + j) * hi;
+                T f = ldg(v.S(SL_WG) + o) * mix;
+                f += ldg(v.S(SL_WW) + o) * u0c;
+                f += ldg(v.S(SL_WS) + o) * u1m;
+                f += ldg(v.S(SL_WC) + o) * u1c;
+                f += ldg(v.S(SL_WN) + o) * u1p;
+                f += ldg(v.S(SL_WE) + o) * u2c;
+                y = f - ldg(v.S(SL_LA) + o) * y;
+                if (t == e) y -= ldg(v.Yv(Y_CHS) + j) * hi;
                 Y[o] = y;
                 u0m = u1m; u0c = u1c; u0p = u1p;
                 u1m = u2m; u1c = u2c; u1p = u2p;
@@ -274,6 +281,7 @@ __device__ __forceinline__ void s_stage(const inst_view<T> &v, int scheme, const
             T y10 = Y1[j], y11 = Y1[ny + j];
             T d0m = Y2[j - 1] - U[j - 1], d0c = Y2[j] - uc0, d0p = Y2[j + 1] - U[j + 1];
             T d1m = Y2[ny + j - 1] - U[ny + j - 1], d1c = Y2[ny + j] - uc1, d1p = Y2[ny + j + 1] - U[ny + j + 1];
+#pragma unroll 4
             for (int t = 1; t <= e; ++t) {
                 const long long o = (long long)t * ny + j;
                 const T uc2 = U[o + ny];
@@ -284,31 +292,31 @@ __device__ __forceinline__ void s_stage(const inst_view<T> &v, int scheme, const
                 const T mix = (d0m - d0p) + (d2p - d2m);
                 T f;
                 if (scheme == LSS_ADI_HUNDSDORFER_VERWER) {
-                    f = ldg(v.S[SL_LA] + o) * y10;
-                    f += ldg(v.S[SL_S2SC] + o) * y11;
-                    f += ldg(v.S[SL_S2SE] + o) * y12;
-                    f += ldg(v.S[SL_S2MZ] + o) * mix;
-                    f += ldg(v.S[SL_X1] + o) * d0c;
-                    f += ldg(v.S[SL_X2] + o) * d1c;
-                    f += ldg(v.S[SL_X3] + o) * d2c;
-                    f += ldg(v.S[SL_X4] + o) * d1m;
-                    f += ldg(v.S[SL_X5] + o) * d1p;
+                    f = ldg(v.S(SL_LA) + o) * y10;
+                    f += ldg(v.S(SL_S2SC) + o) * y11;
+                    f += ldg(v.S(SL_S2SE) + o) * y12;
+                    f += ldg(v.S(SL_S2MZ) + o) * mix;
+                    f += ldg(v.S(SL_X1) + o) * d0c;
+                    f += ldg(v.S(SL_X2) + o) * d1c;
+                    f += ldg(v.S(SL_X3) + o) * d2c;
+                    f += ldg(v.S(SL_X4) + o) * d1m;
+                    f += ldg(v.S(SL_X5) + o) * d1p;
                 } else {
-                    f = ldg(v.S[SL_LA] + o) * uc0;
-                    f += ldg(v.S[SL_S2SC] + o) * uc1;
-                    f += ldg(v.S[SL_S2SE] + o) * uc2;
-                    f += ldg(v.S[SL_S2IB] + o) * y11;
-                    f += ldg(v.S[SL_S2MZ] + o) * mix;
+                    f = ldg(v.S(SL_LA) + o) * uc0;
+                    f += ldg(v.S(SL_S2SC) + o) * uc1;
+                    f += ldg(v.S(SL_S2SE) + o) * uc2;
+                    f += ldg(v.S(SL_S2IB) + o) * y11;
+                    f += ldg(v.S(SL_S2MZ) + o) * mix;
                     if (scheme == LSS_ADI_MODIFIED_CRAIG_SNEYD) {
-                        f += ldg(v.S[SL_X1] + o) * d0c;
-                        f += ldg(v.S[SL_X2] + o) * d1c;
-                        f += ldg(v.S[SL_X3] + o) * d2c;
-                        f += ldg(v.S[SL_X4] + o) * d1m;
-                        f += ldg(v.S[SL_X5] + o) * d1p;
+                        f += ldg(v.S(SL_X1) + o) * d0c;
+                        f += ldg(v.S(SL_X2) + o) * d1c;
+                        f += ldg(v.S(SL_X3) + o) * d2c;
+                        f += ldg(v.S(SL_X4) + o) * d1m;
+                        f += ldg(v.S(SL_X5) + o) * d1p;
                     }
                 }
-                y = f - ldg(v.S[SL_LA] + o) * y;
-                if (t == e) y -= ldg(v.Yv[Y_CHS] + j) * hi;
+                y = f - ldg(v.S(SL_LA) + o) * y;
+                if (t == e) y -= ldg(v.Yv(Y_CHS) + j) * hi;
                 Y[o] = y;
                 uc0 = uc1; uc1 = uc2;
                 y10 = y11; y11 = y12;
@@ -317,9 +325,10 @@ __device__ __forceinline__ void s_stage(const inst_view<T> &v, int scheme, const
             }
         }
         T x = y;
+#pragma unroll 4
         for (int t = e - 1; t >= 1; --t) {
             const long long o = (long long)t * ny + j;
-            x = Y[o] - ldg(v.S[SL_G] + o) * x;
+            x = Y[o] - ldg(v.S(SL_G) + o) * x;
             Y[o] = x;
         }
         Y[j] = lo;
@@ -329,32 +338,34 @@ __device__ __forceinline__ void s_stage(const inst_view<T> &v, int scheme, const
 
 // v-line sweep: line i reads row i of `in` (t-1, t, t+1) and `inh` (t); tables are [t][i].
 template <typename T>
-__device__ __forceinline__ void v_stage(const inst_view<T> &v, const T *in, const T *inh, const T *sb0, T *out, int l0,
-                                        int ls)
+__device__ __forceinline__ void v_stage(const inst_view<T> &v, const T *__restrict__ in, const T *__restrict__ inh,
+                                        const T *__restrict__ sb0, T *__restrict__ out, int l0, int ls)
 {
     const int nx = v.nx, ny = v.ny, e = v.e_v;
     for (int i = 1 + l0; i <= nx - 2; i += ls) {
-        const int ii = ldg(v.imap + i);
+        const int ii = ldg(v.imap() + i);
         const T lo = sb0[ii];
-        const T hi = ldg(v.X[X_VHI] + ii);
+        const T hi = ldg(v.X(X_VHI) + ii);
         const long long row = (long long)i * ny;
         T a0 = in[row], a1 = in[row + 1];
         T y = lo;
+#pragma unroll 4
         for (int t = 1; t <= e; ++t) {
             const long long ot = (long long)t * nx + i;
             const T a2 = in[row + t + 1];
-            T f = ldg(v.Vt[VL_LA] + ot) * a0;
-            f += ldg(v.Vt[VL_VC] + ot) * a1;
-            f += ldg(v.Vt[VL_VN] + ot) * a2;
-            f += ldg(v.Vt[VL_IB] + ot) * inh[row + t];
-            y = f - ldg(v.Vt[VL_LA] + ot) * y;
-            if (t == e) y -= ldg(v.X[X_CHV] + i) * hi;
+            T f = ldg(v.Vt(VL_LA) + ot) * a0;
+            f += ldg(v.Vt(VL_VC) + ot) * a1;
+            f += ldg(v.Vt(VL_VN) + ot) * a2;
+            f += ldg(v.Vt(VL_IB) + ot) * inh[row + t];
+            y = f - ldg(v.Vt(VL_LA) + ot) * y;
+            if (t == e) y -= ldg(v.X(X_CHV) + i) * hi;
             out[row + t] = y;
             a0 = a1; a1 = a2;
         }
         T x = y;
+#pragma unroll 4
         for (int t = e - 1; t >= 1; --t) {
-            x = out[row + t] - ldg(v.Vt[VL_G] + (long long)t * nx + i) * x;
+            x = out[row + t] - ldg(v.Vt(VL_G) + (long long)t * nx + i) * x;
             out[row + t] = x;
         }
         out[row] = lo;
@@ -365,21 +376,14 @@ __device__ __forceinline__ void v_stage(const inst_view<T> &v, const T *in, cons
 template <typename T> __device__ __forceinline__ inst_view<T> make_view(const bparams<T> &p, const bdesc &d)
 {
     inst_view<T> v;
+    v.p = &p;
     v.nx = d.nx;
     v.ny = d.ny;
     v.e_s = d.nx - 2;
     v.e_v = d.ny - 2;
     v.o2 = d.o2;
-#pragma unroll
-    for (int s = 0; s < SL_COUNT; ++s) v.S[s] = p.S[s] + d.o2;
-#pragma unroll
-    for (int s = 0; s < VL_COUNT; ++s) v.Vt[s] = p.Vt[s] + d.o2;
-#pragma unroll
-    for (int s = 0; s < X_COUNT; ++s) v.X[s] = p.X[s] + d.ox;
-#pragma unroll
-    for (int s = 0; s < Y_COUNT; ++s) v.Yv[s] = p.Yv[s] + d.oy;
-    v.imap = p.imap + d.ox;
-    v.jmap = p.jmap + d.oy;
+    v.ox = d.ox;
+    v.oy = d.oy;
     return v;
 }
 
@@ -409,7 +413,7 @@ __device__ __forceinline__ void fwd_step(const inst_view<T> &v, int scheme, cons
     __syncthreads();
 }
 
-template <typename T, int BS> __global__ void __launch_bounds__(BS) k_batch_forward(bparams<T> p)
+template <typename T, int BS> __global__ void __launch_bounds__(BS) k_batch_forward(const __grid_constant__ bparams<T> p)
 {
     __shared__ int s_idx;
     __shared__ int s_bad;
@@ -456,7 +460,7 @@ template <typename T, int BS> __global__ void __launch_bounds__(BS) k_batch_forw
 // values of every step, followed by the adjoint steps of the segment in reverse order.
 // Results: value, the 5 parameter sensitivities, the final surface (state U arena) and
 // dV/d(initial condition) (state V arena).
-template <int BS> __global__ void __launch_bounds__(BS) k_batch_fwdadj(bparams<double> p)
+template <int BS> __global__ void __launch_bounds__(BS, 8) k_batch_fwdadj(const __grid_constant__ bparams<double> p)
 {
     __shared__ int s_idx;
     __shared__ int s_bad;
@@ -589,33 +593,33 @@ template <int BS> __global__ void __launch_bounds__(BS) k_batch_fwdadj(bparams<d
 __device__ __forceinline__ int gtid() { return blockIdx.x * blockDim.x + threadIdx.x; }
 __device__ __forceinline__ int gstride() { return gridDim.x * blockDim.x; }
 
-template <typename T> __global__ void k_wide_b1(bparams<T> p, const T *U, T *b0)
+template <typename T> __global__ void k_wide_b1(const __grid_constant__ bparams<T> p, const T *U, T *b0)
 {
     const bdesc d = p.desc[0];
     const inst_view<T> v = make_view(p, d);
     b1_stage<T>(v, U, b0, d.bnc, gtid(), gstride());
 }
 template <typename T, int KIND>
-__global__ void k_wide_s(bparams<T> p, const T *U, const T *Y1, const T *Y2, T *Y)
+__global__ void k_wide_s(const __grid_constant__ bparams<T> p, const T *U, const T *Y1, const T *Y2, T *Y)
 {
     const bdesc d = p.desc[0];
     const inst_view<T> v = make_view(p, d);
     s_stage<T, KIND>(v, d.scheme, U, Y1, Y2, Y, gtid(), gstride());
 }
-template <typename T> __global__ void k_wide_v(bparams<T> p, const T *in, const T *inh, const T *b0, T *out)
+template <typename T> __global__ void k_wide_v(const __grid_constant__ bparams<T> p, const T *in, const T *inh, const T *b0, T *out)
 {
     const bdesc d = p.desc[0];
     const inst_view<T> v = make_view(p, d);
     v_stage<T>(v, in, inh, b0, out, gtid(), gstride());
 }
-template <typename T> __global__ void k_wide_b2(bparams<T> p, T *Vn)
+template <typename T> __global__ void k_wide_b2(const __grid_constant__ bparams<T> p, T *Vn)
 {
     const bdesc d = p.desc[0];
     const inst_view<T> v = make_view(p, d);
     b2_stage<T>(v, Vn, gtid(), gstride());
 }
 // value, finiteness flag and final-array flag of the single instance
-template <typename T> __global__ void k_wide_finish(bparams<T> p, const T *U)
+template <typename T> __global__ void k_wide_finish(const __grid_constant__ bparams<T> p, const T *U)
 {
     __shared__ int bad;
     const bdesc d = p.desc[0];
@@ -900,8 +904,9 @@ template <typename T> int batch_typed<T>::create(const lss_adi_problem *ps, int 
     LSS_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
     LSS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
     LSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_forward<T, 64>, 64, 0), "occupancy");
-    grid_blocks = std::max(1, std::min(sms * std::max(1, std::min(per_sm, 8)), n));
+    grid_blocks = std::max(1, std::min(sms * std::max(1, std::min(per_sm, 16)), n));
     this->sms = sms;
+    if (n == 1) LSS_CUDA_TRY(d_b0.alloc(desc[0].nx), "batch: allocating the boundary column");
     return LSS_ADI_OK;
 }
 
@@ -921,7 +926,9 @@ template <typename T> int batch_typed<T>::prepare_adjoint(cudaStream_t s)
         const long long nseg = (d.steps + c - 1) / c;
         need = std::max(need, (nseg + 4LL * (c + 1) + 2 + 7) * nn + d.nx + 2LL * d.ny);
     }
-    const int want = std::max(1, std::min(sms * 4, count));
+    int per_sm = 0;
+    LSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_fwdadj<64>, 64, 0), "occupancy");
+    const int want = std::max(1, std::min(sms * std::max(1, per_sm), count));
     if (d_ws.p && ws_stride >= need && grid_adj == want) return LSS_ADI_OK;
     ws_stride = (need + 31) / 32 * 32;
     grid_adj = want;
@@ -953,7 +960,6 @@ template <typename T> int batch_typed<T>::enqueue(int mode, cudaStream_t s)
 template <typename T> int batch_typed<T>::enqueue_wide(cudaStream_t s)
 {
     const bdesc &d = desc[0];
-    if (!d_b0.p) LSS_CUDA_TRY(d_b0.alloc(d.nx), "wide: allocating boundary column");
     bparams<T> p = params();
     T *U = p.U, *V = p.V, *Y1 = p.Y1, *Y2 = p.Y2, *Y3 = p.Y3, *b0 = d_b0.p;
     LSS_CUDA_TRY(cudaMemcpyAsync(U, d_payoff.p, total_n * sizeof(T), cudaMemcpyDeviceToDevice, s), "wide: initial state");

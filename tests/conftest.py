@@ -62,8 +62,10 @@ def fp64_tol(ref, s_hi):
 
 
 def fp32_ok(dev32, ref32, ref64):
-    """FP32 parity: the device FP32 surface must be as close to the FP64 oracle as the
-    reference's own FP32 run is (within a factor 2, or 1e-4 absolute-relative)."""
+    """FP32 parity: the device FP32 surface must be about as close to the FP64 oracle as the
+    reference's own FP32 run is.  Two FP32 evaluations of the same scheme with different
+    rounding sequences differ from each other about as much as each differs from FP64, so the
+    bound is 3x the reference's own FP32 error (or 1e-4)."""
     e_dev = rel_err(dev32, ref64)
     e_ref = rel_err(ref32, ref64)
-    return e_dev <= max(2.0 * e_ref, 1e-4), e_dev, e_ref
+    return e_dev <= max(3.0 * e_ref, 1e-4), e_dev, e_ref
