@@ -218,6 +218,18 @@ int lss_tridiag_thomas_lu(int precision, int n, int lines, const void *lo, const
                           const void *up, const void *rhs, const void *bnd_lo, const void *bnd_hi,
                           void *x, void *stream);
 
+/* Same solve as lss_tridiag_thomas_lu for callers that must not allocate device memory
+ * during the call (code inside a memory pool or allocator it does not control, real-time
+ * paths, hosts that reserve all device memory up front).  No counterpart in the reference.
+ * It allocates nothing: its scratch is a fixed 8 MiB array inside the library, held by every
+ * GPU that loads the library until the process exits, so n*lines*element size must not exceed
+ * 8 MiB (larger requests return LSS_ADI_EINVAL).  The first call on a device looks up the
+ * array's device address; make that first call before any stream capture.  All calls on a
+ * device share the array: calls whose kernels overlap on the GPU race. */
+int lss_tridiag_thomas_lu_noalloc(int precision, int n, int lines, const void *lo, const void *diag,
+                                  const void *up, const void *rhs, const void *bnd_lo, const void *bnd_hi,
+                                  void *x, void *stream);
+
 /* --- diagnostics ---------------------------------------------------------------------- */
 
 const char *lss_adi_last_error(void);

@@ -74,6 +74,8 @@ SIGNATURES = {
     "lss_adi_batch_destroy": (None, [c_void_p]),
     "lss_tridiag_thomas_lu": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                       c_void_p, c_void_p, c_void_p]),
+    "lss_tridiag_thomas_lu_noalloc": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
+                                              c_void_p, c_void_p, c_void_p, c_void_p]),
 }
 
 _lib = None
