@@ -200,6 +200,12 @@ int lss_adi_batch_surface(lss_adi_batch *b, int index, void *out_surface);
 /* dV/d(initial condition grid) of instance `index` after a mode-1 run (host, FP64, Nx*Ny). */
 int lss_adi_batch_payoff_gradient(lss_adi_batch *b, int index, void *out);
 
+/* Lines-per-CTA autotuner: runs `mode` once per CTA size (64, 128, 256 threads per instance;
+ * each thread owns one S-line or v-line at a time) and keeps the fastest for later runs of
+ * that mode.  With *threads_per_instance > 0 on entry it sets that size without timing; on
+ * return it holds the size in use.  The runs overwrite the batch's results. */
+int lss_adi_batch_autotune(lss_adi_batch *b, int mode, int *threads_per_instance, void *stream);
+
 /* Kernel launches made by the last lss_adi_batch_run / graph launch (own kernels only). */
 int lss_adi_batch_launch_count(const lss_adi_batch *b);
 

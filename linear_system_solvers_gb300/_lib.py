@@ -70,6 +70,7 @@ SIGNATURES = {
     "lss_adi_batch_results": (c_int, [c_void_p, P(c_double), P(c_double), P(c_int)]),
     "lss_adi_batch_surface": (c_int, [c_void_p, c_int, c_void_p]),
     "lss_adi_batch_payoff_gradient": (c_int, [c_void_p, c_int, c_void_p]),
+    "lss_adi_batch_autotune": (c_int, [c_void_p, c_int, P(c_int), c_void_p]),
     "lss_adi_batch_launch_count": (c_int, [c_void_p]),
     "lss_adi_batch_destroy": (None, [c_void_p]),
     "lss_tridiag_thomas_lu": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,

@@ -105,5 +105,11 @@ class BatchSolver:
         L.check(self.lib.lss_adi_batch_payoff_gradient(self._b, int(index), out.ctypes.data))
         return out
 
+    def autotune(self, mode: int = 0, threads: int = 0, stream: int = 0) -> int:
+        """Pick the CTA size (threads per instance) for `mode` by timing, or set `threads`."""
+        t = ctypes.c_int(int(threads))
+        L.check(self.lib.lss_adi_batch_autotune(self._b, int(mode), ctypes.byref(t), ctypes.c_void_p(stream)))
+        return t.value
+
     def launch_count(self) -> int:
         return int(self.lib.lss_adi_batch_launch_count(self._b))

@@ -460,7 +460,7 @@ template <typename T, int BS> __global__ void __launch_bounds__(BS) k_batch_forw
 // values of every step, followed by the adjoint steps of the segment in reverse order.
 // Results: value, the 5 parameter sensitivities, the final surface (state U arena) and
 // dV/d(initial condition) (state V arena).
-template <int BS> __global__ void __launch_bounds__(BS, 8) k_batch_fwdadj(const __grid_constant__ bparams<double> p)
+template <int BS> __global__ void __launch_bounds__(BS, 512 / BS) k_batch_fwdadj(const __grid_constant__ bparams<double> p)
 {
     __shared__ int s_idx;
     __shared__ int s_bad;
@@ -703,6 +703,11 @@ template <typename T> struct batch_typed {
 
     int create(const lss_adi_problem *ps, int n);
     int prepare_adjoint(cudaStream_t s);
+    // threads per instance (CTA size) of the persistent kernels, per mode; chosen by autotune()
+    int bs_mode[2] = {64, 64};
+    template <int BS> int launch_forward(cudaStream_t s);
+    template <int BS> int launch_fwdadj(cudaStream_t s);
+    int autotune(int mode, int *chosen, cudaStream_t s);
     // wide path (count == 1)
     dbuf<T> d_b0;
     cudaGraphExec_t wide_graph = nullptr;
@@ -926,6 +931,7 @@ template <typename T> int batch_typed<T>::prepare_adjoint(cudaStream_t s)
         const long long nseg = (d.steps + c - 1) / c;
         need = std::max(need, (nseg + 4LL * (c + 1) + 2 + 7) * nn + d.nx + 2LL * d.ny);
     }
+    // workspace for the largest resident grid over the CTA sizes (64 threads: most CTAs)
     int per_sm = 0;
     LSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_fwdadj<64>, 64, 0), "occupancy");
     const int want = std::max(1, std::min(sms * std::max(1, per_sm), count));
@@ -936,24 +942,96 @@ template <typename T> int batch_typed<T>::prepare_adjoint(cudaStream_t s)
     return LSS_ADI_OK;
 }
 
+template <typename T> template <int BS> int batch_typed<T>::launch_forward(cudaStream_t s)
+{
+    int per_sm = 0;
+    LSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_forward<T, BS>, BS, 0), "occupancy");
+    const int grid = std::max(1, std::min(sms * std::max(1, per_sm), count));
+    k_batch_forward<T, BS><<<grid, BS, 0, s>>>(params());
+    LSS_CUDA_TRY(cudaGetLastError(), "batch: launching k_batch_forward");
+    return LSS_ADI_OK;
+}
+
+template <typename T> template <int BS> int batch_typed<T>::launch_fwdadj(cudaStream_t s)
+{
+    if constexpr (std::is_same<T, double>::value) {
+        int per_sm = 0;
+        LSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_fwdadj<BS>, BS, 0), "occupancy");
+        const int grid = std::max(1, std::min({sms * std::max(1, per_sm), count, grid_adj}));
+        k_batch_fwdadj<BS><<<grid, BS, 0, s>>>(params());
+        LSS_CUDA_TRY(cudaGetLastError(), "batch: launching k_batch_fwdadj");
+        return LSS_ADI_OK;
+    } else {
+        (void)s;
+        return set_error(LSS_ADI_EUNSUPPORTED, "batch: the adjoint is FP64 only");
+    }
+}
+
 template <typename T> int batch_typed<T>::enqueue(int mode, cudaStream_t s)
 {
+    int rc;
+    const int bs = bs_mode[mode == 1 ? 1 : 0];
     if (mode == 1) {
-        if constexpr (std::is_same<T, double>::value) {
-            LSS_CUDA_TRY(cudaMemsetAsync(d_counter.p, 0, sizeof(int), s), "batch: counter reset");
-            k_batch_fwdadj<64><<<grid_adj, 64, 0, s>>>(params());
-            LSS_CUDA_TRY(cudaGetLastError(), "batch: launching k_batch_fwdadj");
-            launches = 1;
-            return LSS_ADI_OK;
-        } else {
-            return set_error(LSS_ADI_EUNSUPPORTED, "batch: the adjoint is FP64 only");
-        }
+        LSS_CUDA_TRY(cudaMemsetAsync(d_counter.p, 0, sizeof(int), s), "batch: counter reset");
+        rc = bs == 256 ? launch_fwdadj<256>(s) : bs == 128 ? launch_fwdadj<128>(s) : launch_fwdadj<64>(s);
+    } else {
+        LSS_CUDA_TRY(cudaMemcpyAsync(state.p, d_payoff.p, total_n * sizeof(T), cudaMemcpyDeviceToDevice, s),
+                     "batch: initial state");
+        LSS_CUDA_TRY(cudaMemsetAsync(d_counter.p, 0, sizeof(int), s), "batch: counter reset");
+        rc = bs == 256 ? launch_forward<256>(s) : bs == 128 ? launch_forward<128>(s) : launch_forward<64>(s);
     }
-    LSS_CUDA_TRY(cudaMemcpyAsync(state.p, d_payoff.p, total_n * sizeof(T), cudaMemcpyDeviceToDevice, s), "batch: initial state");
-    LSS_CUDA_TRY(cudaMemsetAsync(d_counter.p, 0, sizeof(int), s), "batch: counter reset");
-    k_batch_forward<T, 64><<<grid_blocks, 64, 0, s>>>(params());
-    LSS_CUDA_TRY(cudaGetLastError(), "batch: launching k_batch_forward");
     launches = 1;
+    return rc;
+}
+
+// Times one run per CTA size (64, 128, 256 threads per instance) and keeps the fastest for
+// `mode`; with *chosen > 0 on entry, sets that size without timing.
+template <typename T> int batch_typed<T>::autotune(int mode, int *chosen, cudaStream_t s)
+{
+    const int m = mode == 1 ? 1 : 0;
+    if (mode == 1) {
+        int rc = prepare_adjoint(s);
+        if (rc) return rc;
+    }
+    if (chosen && *chosen > 0) {
+        if (*chosen != 64 && *chosen != 128 && *chosen != 256)
+            return set_error(LSS_ADI_EINVAL, "autotune: threads per instance must be 64, 128 or 256");
+        bs_mode[m] = *chosen;
+    } else {
+        const int cand[3] = {64, 128, 256};
+        float best = 1e30f;
+        int best_bs = bs_mode[m];
+        cudaEvent_t e0, e1;
+        LSS_CUDA_TRY(cudaEventCreate(&e0), "autotune: event");
+        LSS_CUDA_TRY(cudaEventCreate(&e1), "autotune: event");
+        for (int c : cand) {
+            bs_mode[m] = c;
+            cudaEventRecord(e0, s);
+            int rc = enqueue(mode, s);
+            cudaEventRecord(e1, s);
+            if (rc) {
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                return rc;
+            }
+            LSS_CUDA_TRY(cudaEventSynchronize(e1), "autotune: run");
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms < best) {
+                best = ms;
+                best_bs = c;
+            }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        bs_mode[m] = best_bs;
+    }
+    if (graph && graph_mode == mode) {
+        cudaGraphExecDestroy(graph);
+        graph = nullptr;
+        graph_mode = -1;
+    }
+    if (chosen) *chosen = bs_mode[m];
     return LSS_ADI_OK;
 }
 
@@ -1296,6 +1374,15 @@ int lss_adi_batch_payoff_gradient(lss_adi_batch *b, int index, void *out)
     clear_error();
     if (!b || !out) return set_error(LSS_ADI_EINVAL, "lss_adi_batch_payoff_gradient: null argument");
     return b->b64 ? payoff_grad_t(*b->b64, index, out) : payoff_grad_t(*b->b32, index, out);
+}
+
+int lss_adi_batch_autotune(lss_adi_batch *b, int mode, int *threads_per_instance, void *stream)
+{
+    clear_error();
+    if (!b) return set_error(LSS_ADI_EINVAL, "lss_adi_batch_autotune: null batch");
+    if (mode != 0 && mode != 1) return set_error(LSS_ADI_EINVAL, "lss_adi_batch_autotune: mode must be 0 or 1");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    return b->b64 ? b->b64->autotune(mode, threads_per_instance, s) : b->b32->autotune(mode, threads_per_instance, s);
 }
 
 int lss_adi_batch_launch_count(const lss_adi_batch *b)

@@ -109,3 +109,27 @@ def test_wide_path_large_grid(lss, oracle, fp):
     else:
         ok, e_dev, e_ref = fp32_ok(got, oracle.solve(op, "f32"), oracle.solve(op, "f64"))
         assert ok, (e_dev, e_ref)
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_cta_size_does_not_change_bits(lss, mode):
+    """Each line is solved by one thread whatever the CTA size, so every size the autotuner
+    may pick gives the same bits."""
+    from linear_system_solvers_gb300.batch import draw_batch
+
+    probs = draw_batch(10, seed=77)
+    for p in probs:
+        p.nt = 15
+    b = lss.BatchSolver(probs, precision="f64")
+    ref = None
+    for threads in (64, 128, 256):
+        assert b.autotune(mode=mode, threads=threads) == threads
+        b.run(mode)
+        v, g, _ = b.results()
+        surf = [b.surface(k) for k in range(len(probs))]
+        if ref is None:
+            ref = (v, g, surf)
+        else:
+            assert np.array_equal(v, ref[0]) and np.array_equal(g, ref[1])
+            assert all(np.array_equal(a, c) for a, c in zip(surf, ref[2]))
+    assert b.autotune(mode=mode) in (64, 128, 256)
