@@ -150,22 +150,34 @@ __device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d
                 acc_t1 = acc_t + sc * w;
                 acc_t = la * w;
                 Y1B[o] = mu;
-                const double Dw = Y2[o - ny] - Uw, Dc = Y2[o] - Uc, De = Y2[o + ny] - Ue;
-                const double Ds = Y2[o - 1] - Us, Dn = Y2[o + 1] - Un;
-                sM = th * (Yo[o - ny] - Uw) + zt * Dw;
-                sZ = -th * (Yo[o] - Uc) - zt * Dc;
-                sP = th * (Yo[o + ny] - Ue) - zt * De;
-                sW = -zt * Dc;
-                sMt = zt * Ds;
-                sPt = zt * Dn;
+                if (zt != 0.0) {
+                    const double Dw = Y2[o - ny] - Uw, Dc = Y2[o] - Uc, De = Y2[o + ny] - Ue;
+                    const double Ds = Y2[o - 1] - Us, Dn = Y2[o + 1] - Un;
+                    sM = th * (Yo[o - ny] - Uw) + zt * Dw;
+                    sZ = -th * (Yo[o] - Uc) - zt * Dc;
+                    sP = th * (Yo[o + ny] - Ue) - zt * De;
+                    sW = -zt * Dc;
+                    sMt = zt * Ds;
+                    sPt = zt * Dn;
+                } else {
+                    // Craig-Sneyd: no extra term, only M, Z, P, C depend on this stage's residual
+                    sM = th * (Yo[o - ny] - Uw);
+                    sZ = -th * (Yo[o] - Uc);
+                    sP = th * (Yo[o + ny] - Ue);
+                    sW = 0.0;
+                    sMt = 0.0;
+                    sPt = 0.0;
+                }
                 const double mix = ((Y2[o - ny - 1] - U[o - ny - 1]) - (Y2[o - ny + 1] - U[o - ny + 1])) +
                                    ((Y2[o + ny + 1] - U[o + ny + 1]) - (Y2[o + ny - 1] - U[o + ny - 1]));
                 sC = d.a_zeta * d.a_gamma * mix;
             }
             pA += mu * hx * (sP - sM);
             pB += mu * (sZ + sW);
-            pQ += mu * (sPt - sMt);
-            pD += mu * (sMt + sPt + 2.0 * sW);
+            if (KIND == 1 || zt != 0.0) {
+                pQ += mu * (sPt - sMt);
+                pD += mu * (sMt + sPt + 2.0 * sW);
+            }
             pE += mu * hx * sC;
             la_next = la;
         }
@@ -219,11 +231,11 @@ __device__ __forceinline__ void adj_gather(const inst_view<double> &v, const bde
             const long long o = (long long)p * ny + q;
             double val = 0.0;
             if constexpr (KIND == 2) {
-                const double db = W(SL_X1, p + 1, q) * F(p + 1, q) + W(SL_X2, p, q) * F(p, q) +
-                                  W(SL_X3, p - 1, q) * F(p - 1, q) + W(SL_X4, p, q + 1) * F(p, q + 1) +
-                                  W(SL_X5, p, q - 1) * F(p, q - 1) + W(SL_S2MZ, p + 1, q + 1) * F(p + 1, q + 1) -
-                                  W(SL_S2MZ, p + 1, q - 1) * F(p + 1, q - 1) - W(SL_S2MZ, p - 1, q + 1) * F(p - 1, q + 1) +
-                                  W(SL_S2MZ, p - 1, q - 1) * F(p - 1, q - 1);
+                double db = W(SL_S2MZ, p + 1, q + 1) * F(p + 1, q + 1) - W(SL_S2MZ, p + 1, q - 1) * F(p + 1, q - 1) -
+                            W(SL_S2MZ, p - 1, q + 1) * F(p - 1, q + 1) + W(SL_S2MZ, p - 1, q - 1) * F(p - 1, q - 1);
+                if (d.scheme == LSS_ADI_MODIFIED_CRAIG_SNEYD)
+                    db += W(SL_X1, p + 1, q) * F(p + 1, q) + W(SL_X2, p, q) * F(p, q) + W(SL_X3, p - 1, q) * F(p - 1, q) +
+                          W(SL_X4, p, q + 1) * F(p, q + 1) + W(SL_X5, p, q - 1) * F(p, q - 1);
                 Y2B[o] = db;
                 val -= db;
             } else {

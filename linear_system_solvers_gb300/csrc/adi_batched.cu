@@ -813,6 +813,10 @@ template <typename T> int batch_typed<T>::create(const lss_adi_problem *ps, int 
                         yh[Y_B2C * total_y + d.oy + j] = static_cast<T>(2.0 * h1 * static_cast<double>(tt.s_hi_neu[j]) / 3.0);
                         jmh[d.oy + j] = tt.jmap[j];
                     }
+                    // modified Craig-Sneyd with zeta == theta adds (zeta - theta) * (...) = 0: it is
+                    // Craig-Sneyd (the reference's surfaces are bit-identical), so run the CS stencil
+                    if (ps[k].scheme == LSS_ADI_MODIFIED_CRAIG_SNEYD && tt.sc.zeta == tt.sc.theta)
+                        desc[k].scheme = LSS_ADI_CRAIG_SNEYD;
                     const double DN = tt.coef_v0[d.nx - 1];
                     desc[k].bnc = -dl * (2.0 * h1 * static_cast<double>(tt.s_hi_neu[0])) * DN;
                     const bilinear b = make_bilinear(tt.x.data(), d.nx, tt.y.data(), d.ny, ps[k].eval_s, ps[k].eval_v);

@@ -55,6 +55,7 @@ CASES = {
     "cs_60x30": dict(BASE, scheme="cs", nx=60, ny=30, nt=31, rho=-0.2),
     "dr_70x35": dict(BASE, scheme="dr", nx=70, ny=35, nt=41),
     "mcs_z08_theta80": dict(BASE, scheme="mcs", zeta=0.8, theta_scheme="theta80", nx=48, ny=24, nt=31, rho=-0.4),
+    "mcs_z08_cn": dict(BASE, scheme="mcs", zeta=0.8, nx=52, ny=26, nt=31, rho=-0.4),
 }
 
 
@@ -69,7 +70,7 @@ def test_parameter_gradients_match_device_finite_differences(lss, key):
         assert abs(grads[k] - fd) <= 1e-6 * max(abs(fd), 1e-3 * abs(val)), (name, grads[k], fd)
 
 
-@pytest.mark.parametrize("key", ["mcs_64x32", "dr_70x35"])
+@pytest.mark.parametrize("key", ["mcs_64x32", "dr_70x35", "mcs_z08_cn"])
 def test_parameter_gradients_match_reference_bump_and_revalue(lss, oracle, key):
     p = lss.HestonProblem(**CASES[key])
     val, grads, _ = lss.ImplicitHestonSolver(p, precision="f64", arith="fast").adjoint(want_payoff_grad=False)

@@ -18,7 +18,8 @@ def mixed_batch(lss, schemes=("dr", "cs", "mcs", "hv"), seed=3, count=12):
             kappa=float(rng.uniform(0.5, 5)), theta_v=float(rng.uniform(0.01, 0.1)), sigma=float(rng.uniform(0.1, 1)),
             rho=float(rng.uniform(-0.95, 0)), rate=float(rng.uniform(0, 0.05)), maturity=float(rng.uniform(0.25, 2)),
             strike=K, acc_point=K, nx=int(rng.choice([4, 17, 64, 96, 130, 256])), ny=int(rng.choice([4, 9, 32, 48, 128])),
-            nt=int(rng.integers(2, 40)), scheme=schemes[k % len(schemes)], **NU))
+            nt=int(rng.integers(2, 40)), scheme=schemes[k % len(schemes)],
+            zeta=0.8 if (schemes[k % len(schemes)] == "mcs" and k % 8 < 4) else 0.5, **NU))
     return out
 
 
@@ -114,7 +115,8 @@ def test_wide_path_large_grid(lss, oracle, fp):
 @pytest.mark.parametrize("mode", [0, 1])
 def test_cta_size_does_not_change_bits(lss, mode):
     """Each line is solved by one thread whatever the CTA size, so every size the autotuner
-    may pick gives the same bits."""
+    may pick gives the same surfaces and values bit for bit; the parameter sensitivities are
+    sums over lines whose order follows the thread layout (rounding-level differences)."""
     from linear_system_solvers_gb300.batch import draw_batch
 
     probs = draw_batch(10, seed=77)
@@ -130,6 +132,7 @@ def test_cta_size_does_not_change_bits(lss, mode):
         if ref is None:
             ref = (v, g, surf)
         else:
-            assert np.array_equal(v, ref[0]) and np.array_equal(g, ref[1])
+            assert np.array_equal(v, ref[0])
+            np.testing.assert_allclose(g, ref[1], rtol=1e-11, atol=1e-14)
             assert all(np.array_equal(a, c) for a, c in zip(surf, ref[2]))
     assert b.autotune(mode=mode) in (64, 128, 256)
