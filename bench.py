@@ -42,8 +42,8 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=32, help="instances timed on the host cores")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip timing the plain per-instance device path")
-    ap.add_argument("--configs", default="", help="comma list of single-instance configurations to measure instead "
-                    "of the batched headline: c1, c2, c5, c5sabr (one JSON line each)")
+    ap.add_argument("--configs", default="", help="comma list of configurations to measure instead of the batched "
+                    "headline: c1, c2, c4, c5, c5sabr (one JSON line each)")
     return ap.parse_args()
 
 
@@ -100,6 +100,13 @@ def run_cpu_baseline(problems, m, cores, kind):
 def reference_kind():
     from oracle import oracle as O
 
+    if not O.reference_available() and os.path.exists(os.path.join(ROOT, "oracle", "_ref", "src", ".patched")):
+        # rebuild the reference driver for this host from the patched copy that travelled here
+        try:
+            subprocess.run(["bash", os.path.join(ROOT, "oracle", "build_ref.sh")], check=True, timeout=900,
+                           capture_output=True)
+        except Exception:
+            pass
     if O.reference_available():
         try:
             O.run_reference(O.Problem(nx=8, ny=8, nt=3), "f64")
@@ -196,9 +203,11 @@ def main():
         problems = draw_batch(args.count, seed=SEED)
         kind = reference_kind()
         cores = os.cpu_count() or 1
+        # the compiled reference is ~50x slower than the port: smaller bounded samples per step
+        m = args.cpu_sample if kind == "port" else max(4, args.cpu_sample // 4)
         for _ in range(args.warmup):
-            run_cpu_baseline(problems, max(4, args.cpu_sample // 4), cores, kind)
-        vals = [run_cpu_baseline(problems, args.cpu_sample, cores, kind) for _ in range(max(1, args.steps))]
+            run_cpu_baseline(problems, max(2, m // 4), cores, kind)
+        vals = [run_cpu_baseline(problems, m, cores, kind) for _ in range(max(1, args.steps))]
         v = statistics.median(x["value"] for x in vals)
         cb = dict(vals[0])
         cb["value"] = v
@@ -206,7 +215,7 @@ def main():
                "n_gpus": 0, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
                "scaling": "none", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                "config": {"workload": f"batched MCS Heston, {args.count} uneven instances (seed {SEED}); "
-                                      f"each step times a {args.cpu_sample}-instance sample on the host cores",
+                                      f"each step times a bounded sample of the batch's instances on the host cores",
                           "global_batch": args.count},
                "cpu_baseline": cb,
                "e2e": {"value": v, "unit": "grid-point-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -423,6 +432,8 @@ def run_configs(args):
             # stable companion (rho = 0) on the same grid
             p = lss.HestonProblem(**dict(CONFIG1, scheme=scheme, rho=0.0, nx=400, ny=200, nt=501, **NU_K100))
             case(f"config2 {scheme.upper()} 400x200x500 rho=0 companion", p, "f64", 2)
+    if "c4" in wanted:
+        run_config4()
     if "c5" in wanted:
         for fp in ("f64", "f32"):
             p = lss.HestonProblem(**dict(CONFIG1, scheme="hv", nx=4096, ny=2048, nt=1001, **NU_K100))
@@ -433,6 +444,84 @@ def run_configs(args):
                               nonuniform=True, acc_point=0.05, alpha_scale=10.0, beta_scale=24.0, eval_s=0.05,
                               eval_v=0.2)
         case("config5 SABR DR 2048x1024x800", p, "f64", 1, oracle_nt=11)
+
+
+def _oracle_value(args):
+    """Bump-and-revalue leg: V(eval_s, eval_v) from the oracle surface (bilinear in S, v)."""
+    import numpy as np
+
+    from oracle import oracle as O
+
+    kw, s0, v0 = args
+    p = O.Problem(**kw)
+    surf = O.solve(p, "f64")
+    x, y = O.grid(p, "f64")
+    i = max(0, min(len(x) - 2, int(np.searchsorted(x, s0, side="right")) - 1))
+    j = max(0, min(len(y) - 2, int(np.searchsorted(y, v0, side="right")) - 1))
+    wx = min(1.0, max(0.0, (s0 - x[i]) / (x[i + 1] - x[i])))
+    wy = min(1.0, max(0.0, (v0 - y[j]) / (y[j + 1] - y[j])))
+    return float((1 - wx) * (1 - wy) * surf[i, j] + wx * (1 - wy) * surf[i + 1, j] + (1 - wx) * wy * surf[i, j + 1]
+                 + wx * wy * surf[i + 1, j + 1])
+
+
+def run_config4(count=1024, sample=16):
+    """Config 4: adjoint of 1024 uneven MCS instances (seed 20261204); gradients of a stable
+    16-instance sample against central finite differences (relative bump 1e-5) of the CPU
+    oracle, which is bit-exact with the reference's Thomas-LU path."""
+    import numpy as np
+    import torch
+
+    import linear_system_solvers_gb300 as lss
+    from linear_system_solvers_gb300.batch import draw_batch, grid_point_steps
+
+    probs = draw_batch(count, seed=20261204)
+    b = lss.BatchSolver(probs, precision="f64")
+    threads = b.autotune(mode=1)
+    b.run(1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b.run(1)
+    torch.cuda.synchronize()
+    secs = time.perf_counter() - t0
+    vals, grads, status = b.results()
+    names = ("kappa", "theta_v", "sigma", "rho", "rate")
+    picked = []
+    for k, p in enumerate(probs):
+        surf = b.surface(k)
+        if np.all(np.isfinite(surf)) and np.abs(surf).max() <= 10 * p.s_hi:
+            picked.append(k)
+        if len(picked) == sample:
+            break
+    jobs = []
+    for k in picked:
+        p = probs[k]
+        kw = oracle_kwargs(p)
+        for name in names:
+            h = 1e-5 * abs(kw[name])
+            for sgn in (+1, -1):
+                q = dict(kw)
+                q[name] = kw[name] + sgn * h
+                jobs.append((q, p.eval_s, p.eval_v))
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(os.cpu_count() or 1) as pool:
+        fdv = pool.map(_oracle_value, jobs, chunksize=1)
+    worst = 0.0
+    q = 0
+    for k in picked:
+        p = probs[k]
+        kw = oracle_kwargs(p)
+        for c, name in enumerate(names):
+            h = 1e-5 * abs(kw[name])
+            fd = (fdv[q] - fdv[q + 1]) / (2 * h)
+            q += 2
+            err = abs(grads[k, c] - fd) / max(abs(fd), 1e-3 * abs(vals[k]))
+            worst = max(worst, err)
+    print(json.dumps({"config": "config4 adjoint, 1024 uneven MCS instances (seed 20261204)",
+                      "device_gps_fwd_adj": grid_point_steps(probs) / secs, "device_seconds": secs,
+                      "threads_per_instance": threads, "nonfinite_instances": int(np.count_nonzero(status)),
+                      "fd_sample_instances": len(picked),
+                      "max_rel_err_grad_vs_reference_fd": worst, "fd": "central, relative bump 1e-5, CPU oracle"}),
+          flush=True)
 
 
 def time_plain_path(lss, problems, stream, batched_value, m=64):

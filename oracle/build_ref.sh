@@ -12,20 +12,27 @@ set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 REF="${LSS_REFERENCE_DIR:-/root/reference}"
 OUT="$HERE/_ref"
-if [ ! -d "$REF/pde_solvers" ]; then
-    echo "build_ref.sh: reference not found at $REF (skipping)" >&2
-    exit 0
-fi
 mkdir -p "$OUT"
-if [ -x "$OUT/ref_driver" ] && [ "$OUT/ref_driver" -nt "$HERE/ref_driver.cu" ] && [ "$OUT/ref_driver" -nt "$0" ]; then
+if [ -x "$OUT/ref_driver" ] && "$OUT/ref_driver" >/dev/null 2>&1; [ $? -eq 2 ] && \
+   [ "$OUT/ref_driver" -nt "$HERE/ref_driver.cu" ] && [ "$OUT/ref_driver" -nt "$0" ]; then
     echo "build_ref.sh: $OUT/ref_driver is up to date"
     exit 0
 fi
-rm -rf "$OUT/src"
-mkdir -p "$OUT/src"
-( cd "$REF" && find . \( -name '*.hpp' -o -name '*.cu' \) ! -path './.git/*' -print0 | \
-    while IFS= read -r -d '' f; do mkdir -p "$OUT/src/$(dirname "$f")"; cp "$f" "$OUT/src/$f"; done )
+if [ -d "$REF/pde_solvers" ]; then
+    rm -rf "$OUT/src"
+    mkdir -p "$OUT/src"
+    ( cd "$REF" && find . \( -name '*.hpp' -o -name '*.cu' \) ! -path './.git/*' -print0 | \
+        while IFS= read -r -d '' f; do mkdir -p "$OUT/src/$(dirname "$f")"; cp "$f" "$OUT/src/$f"; done )
+elif [ -d "$OUT/src/pde_solvers" ] && [ -f "$OUT/src/.patched" ]; then
+    # a machine without the reference checkout (the copy made where it was present travelled
+    # with the repository): rebuild the driver for this host from that patched copy
+    echo "build_ref.sh: reference not at $REF, rebuilding from the patched copy in $OUT/src" >&2
+else
+    echo "build_ref.sh: reference not found at $REF (skipping)" >&2
+    exit 0
+fi
 cd "$OUT/src"
+if [ ! -f .patched ]; then
 find . -name '*.hpp' -print0 | xargs -0 sed -i 's/std::exception(/std::runtime_error(/g'
 for f in sparse_solvers/general/core_sor_solver/lss_core_sor_solver.hpp \
          sparse_solvers/general/core_sor_solver_cuda/lss_core_sor_solver_cuda.hpp; do
@@ -33,6 +40,8 @@ for f in sparse_solvers/general/core_sor_solver/lss_core_sor_solver.hpp \
     sed -i 's/template <template <typename fp_type> typename traits>/template <template <typename> typename traits>/' "$f"
 done
 sed -i 's/decltype(errors)::value_type(0.0)/fp_type(0.0)/' sparse_solvers/general/core_sor_solver_cuda/lss_core_sor_solver_cuda.hpp
+touch .patched
+fi
 CUS=$(find . -name '*.cu' ! -name main.cu | sort)
 ARCH="${LSS_REF_ARCH:-sm_100}"
 nvcc -std=c++17 -O2 -arch="$ARCH" -Xcompiler -ffp-contract=off \
