@@ -42,8 +42,10 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=32, help="instances timed on the host cores")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip timing the plain per-instance device path")
+    ap.add_argument("--max-time-steps", type=int, default=0,
+                    help="cap every instance's time loop (a smaller workload for profiler captures; 0 = no cap)")
     ap.add_argument("--configs", default="", help="comma list of configurations to measure instead of the batched "
-                    "headline: c1, c2, c4, c5, c5sabr (one JSON line each)")
+                    "headline: c1, c2, c4, c5, c5sabr, mcsz (one JSON line each)")
     return ap.parse_args()
 
 
@@ -67,6 +69,13 @@ def _cpu_ref_one(kw):
     return secs, p.nx * p.ny * (p.nt - 1)
 
 
+def cap_time_steps(problems, cap):
+    if cap > 0:
+        for p in problems:
+            p.nt = min(p.nt, cap + 1)
+    return problems
+
+
 def cpu_sample(problems, m):
     """Stratified bounded sample: every (count // m)-th instance of the batch."""
     step = max(1, len(problems) // m)
@@ -79,11 +88,19 @@ def oracle_kwargs(p):
     return {k: v for k, v in dataclasses.asdict(p).items() if k not in ("eval_s", "eval_v", "fp64_tables")}
 
 
-def run_cpu_baseline(problems, m, cores, kind):
+def run_cpu_baseline(problems, m, cores, kind, max_steps=None):
+    """Time `m` instances of the batch on `cores` host processes; with `max_steps` each
+    instance's backward time loop stops after that many steps (the per-step work of an
+    instance is the same at every step, so the rate is that of the full loop)."""
     from oracle import oracle as O
 
     O.build()
     sample = [oracle_kwargs(p) for p in cpu_sample(problems, m)]
+    if max_steps is not None:
+        for kw in sample:
+            kw["nt"] = min(kw["nt"], max_steps + 1)
+    cores = max(1, min(cores, len(sample)))
+    sample.sort(key=lambda kw: -kw["nx"] * kw["ny"] * kw["nt"])  # largest first: the pool's tail stays short
     fn = _cpu_ref_one if kind == "reference" else _cpu_one
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
@@ -92,7 +109,8 @@ def run_cpu_baseline(problems, m, cores, kind):
     wall = time.perf_counter() - t0
     gps = sum(r[1] for r in res)
     return {"value": gps / wall, "unit": "grid-point-steps/s", "cores": cores, "kind": kind,
-            "sample": f"{len(sample)} of the batch's instances (every {max(1, len(problems) // m)}-th), full time loops, "
+            "sample": f"{len(sample)} of the batch's instances (every {max(1, len(problems) // m)}-th), "
+                      f"{'full time loops' if max_steps is None else f'first {max_steps} steps of each time loop'}, "
                       f"{gps:.3e} grid-point-steps in {wall:.1f} s wall on {cores} host threads",
             "single_core_gps": gps / sum(r[0] for r in res)}
 
@@ -203,11 +221,15 @@ def main():
         problems = draw_batch(args.count, seed=SEED)
         kind = reference_kind()
         cores = os.cpu_count() or 1
-        # the compiled reference is ~50x slower than the port: smaller bounded samples per step
-        m = args.cpu_sample if kind == "port" else max(4, args.cpu_sample // 4)
+        # the compiled reference is ~50x slower than the port: four instances per host thread, each
+        # on its full grid but only the first 25 steps of its time loop (5-10 s per step)
+        if kind == "port":
+            m, max_steps = args.cpu_sample, None
+        else:
+            m, max_steps = 4 * cores, 25
         for _ in range(args.warmup):
-            run_cpu_baseline(problems, max(2, m // 4), cores, kind)
-        vals = [run_cpu_baseline(problems, m, cores, kind) for _ in range(max(1, args.steps))]
+            run_cpu_baseline(problems, max(2, m // 4), cores, kind, max_steps=10)
+        vals = [run_cpu_baseline(problems, m, cores, kind, max_steps=max_steps) for _ in range(max(1, args.steps))]
         v = statistics.median(x["value"] for x in vals)
         cb = dict(vals[0])
         cb["value"] = v
@@ -218,7 +240,9 @@ def main():
                                       f"each step times a bounded sample of the batch's instances on the host cores",
                           "global_batch": args.count},
                "cpu_baseline": cb,
-               "e2e": {"value": v, "unit": "grid-point-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+               "e2e": {"value": v, "unit": "grid-point-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+               "note": "the reference has no adjoint: this is its forward rate; a value with five parameter "
+                       "gradients by central bump-and-revalue costs it 11 forward solves per instance"}
         print(json.dumps(out))
         return
 
@@ -229,6 +253,7 @@ def main():
     from linear_system_solvers_gb300 import _lib as L
 
     problems_all = draw_batch(args.count, seed=SEED)
+    cap_time_steps(problems_all, args.max_time_steps)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         # spawn-context pool before the first GPU call
@@ -241,7 +266,8 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     from linear_system_solvers_gb300.sharding import max_over_ranks, rank_seed
 
-    problems = problems_all if rank == 0 else draw_batch(args.count, seed=rank_seed(SEED, rank))
+    problems = problems_all if rank == 0 else cap_time_steps(draw_batch(args.count, seed=rank_seed(SEED, rank)),
+                                                             args.max_time_steps)
     gps = grid_point_steps(problems)
 
     lib = L.load()
@@ -314,7 +340,8 @@ def main():
         "ms_per_step": t_max, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
         "config": {"workload": f"batched modified Craig-Sneyd Heston calls, {len(problems)} uneven instances per GPU "
-                               f"(seed {SEED}), Nx 64-256, Ny 32-128, 100-400 steps, "
+                               f"(seed {SEED}), Nx 64-256, Ny 32-128, "
+                               f"{f'100-400 steps capped at {args.max_time_steps}' if args.max_time_steps else '100-400 steps'}, "
                                f"{'forward + adjoint' if mode == 1 else 'forward'}, one persistent kernel per step, "
                                "graph-launched",
                    "global_batch": len(problems) * world, "grid_point_steps_per_gpu": gps,
@@ -432,12 +459,40 @@ def run_configs(args):
             # stable companion (rho = 0) on the same grid
             p = lss.HestonProblem(**dict(CONFIG1, scheme=scheme, rho=0.0, nx=400, ny=200, nt=501, **NU_K100))
             case(f"config2 {scheme.upper()} 400x200x500 rho=0 companion", p, "f64", 2)
+        # MCS with a genuine weight (zeta = 1/3 != theta = 1/2: the full MCS stencil)
+        p = lss.HestonProblem(**dict(CONFIG1, scheme="mcs", zeta=1.0 / 3.0, nx=400, ny=200, nt=501, **NU_K100))
+        case("config2 MCS(zeta=1/3) 400x200x500", p, "f64", 2)
     if "c4" in wanted:
         run_config4()
     if "c5" in wanted:
         for fp in ("f64", "f32"):
             p = lss.HestonProblem(**dict(CONFIG1, scheme="hv", nx=4096, ny=2048, nt=1001, **NU_K100))
             case("config5 HV 4096x2048x1000", p, fp, 1, oracle_nt=11)
+    if "mcsz" in wanted:
+        # the batch of the headline with a genuine modified Craig-Sneyd weight (zeta = 1/3 != theta):
+        # the full MCS stencil, forward and forward + adjoint
+        from linear_system_solvers_gb300.batch import draw_batch, grid_point_steps
+
+        probs = draw_batch(4096, seed=SEED)
+        for p in probs:
+            p.zeta = 1.0 / 3.0
+        b = lss.BatchSolver(probs, precision="f64")
+        for mode in (0, 1):
+            threads = b.autotune(mode=mode)
+            b.run(mode, graph=True)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            b.run(mode, graph=True)
+            e1.record()
+            torch.cuda.synchronize()
+            secs = e0.elapsed_time(e1) / 1e3
+            status = b.results()[2]
+            print(json.dumps({"config": "batched MCS zeta=1/3, 4096 uneven instances (seed 20261203)",
+                              "mode": ["forward", "forward + adjoint"][mode], "device_gps": grid_point_steps(probs) / secs,
+                              "device_seconds": secs, "threads_per_instance": threads,
+                              "nonfinite_instances": int(np.count_nonzero(status))}), flush=True)
     if "c5sabr" in wanted:
         p = lss.HestonProblem(model="sabr", sigma=0.4, rho=-0.3, sabr_beta=0.5, rate=0.0, strike=0.05, maturity=2.0,
                               s_lo=0.0, s_hi=0.2, v_lo=0.0, v_hi=1.0, nx=2048, ny=1024, nt=801, scheme="dr",
