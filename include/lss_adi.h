@@ -111,6 +111,14 @@ typedef struct lss_adi_problem {
  *   (e.g. 7 of 150 S indices differ), so its FP32 surfaces differ from its FP64 ones by
  *   up to ~10% at those boundary points; this option follows the FP64 problem instead. */
 #define LSS_ADI_OPT_FP64_TABLES 1
+/* DOUBLE_SWEEP: tridiagonal_method_enum::DoubleSweepSolver (common/lss_enumerations.hpp:46-52).
+ *   The line solves run the double-sweep L/K recurrences of double_sweep_solver
+ *   (sparse_solvers/tridiagonal/double_sweep_solver/lss_double_sweep_solver.hpp:114-155,
+ *   lss_double_sweep_boundary.hpp:90-190) instead of Thomas LU; with LSS_ADI_ARITH_REFERENCE
+ *   the surface is bit-identical to the reference's host double-sweep policy.  Both policies
+ *   solve the same systems, so LSS_ADI_ARITH_FAST (one precomputed factorisation) serves
+ *   both and ignores this bit. */
+#define LSS_ADI_OPT_DOUBLE_SWEEP 2
 
 /*
  * Tabulated drop-in: time-invariant scheme coefficients already sampled on the grid by
@@ -130,6 +138,7 @@ typedef struct lss_adi_tables {
     const void *s_hi_neumann;   /* ny: transformed Neumann data dV/dzeta at S_hi (value * A(1)) */
     const void *v_hi_dirichlet; /* nx: V(S_i, v_hi) */
     const void *payoff;         /* nx*ny terminal/initial condition */
+    int options;                /* LSS_ADI_OPT_DOUBLE_SWEEP or 0 */
 } lss_adi_tables;
 
 typedef struct lss_adi_handle lss_adi_handle;

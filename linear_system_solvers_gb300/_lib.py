@@ -19,6 +19,7 @@ DEVICE_POINTERS = 1
 FP64, FP32 = 0, 1
 ARITH_FAST, ARITH_REFERENCE = 0, 1
 OPT_FP64_TABLES = 1
+OPT_DOUBLE_SWEEP = 2
 HESTON, SABR = 0, 1
 SCHEMES = {"dr": 0, "cs": 1, "mcs": 2, "hv": 3}
 THETAS = {"euler": 0, "theta30": 1, "cn": 2, "theta80": 3}
@@ -48,7 +49,7 @@ class LssAdiTables(ctypes.Structure):
         ("scheme", c_int), ("theta_scheme", c_int), ("forward", c_int), ("precision", c_int), ("arith", c_int),
         ("zeta", c_double),
         ("coef", c_void_p), ("coef_v0", c_void_p), ("s_lo_dirichlet", c_void_p), ("s_hi_neumann", c_void_p),
-        ("v_hi_dirichlet", c_void_p), ("payoff", c_void_p),
+        ("v_hi_dirichlet", c_void_p), ("payoff", c_void_p), ("options", c_int),
     ]
 
 

@@ -43,8 +43,7 @@ int validate_problem(const lss_adi_problem &p, std::string &why)
     const double vals[] = {p.kappa, p.theta_v, p.sigma, p.rho, p.rate, p.sabr_beta, p.strike, p.zeta, p.neumann_value, p.acc_point};
     for (double v : vals)
         if (!std::isfinite(v)) return why = "non-finite model parameter", LSS_ADI_EINVAL;
-    if (p.model == LSS_ADI_SABR && p.rate != 0.0)
-        return why = "SABR with r != 0 has time-dependent coefficients; the device path supports r = 0 only", LSS_ADI_EUNSUPPORTED;
+    if (p.options & ~(LSS_ADI_OPT_FP64_TABLES | LSS_ADI_OPT_DOUBLE_SWEEP)) return why = "unknown option bits", LSS_ADI_EINVAL;
     return LSS_ADI_OK;
 }
 
@@ -98,7 +97,9 @@ int lss_adi_create(const lss_adi_problem *p, lss_adi_handle **h)
     hh->parametric = true;
     hh->prob = *p;
     try {
-        if (p->arith == LSS_ADI_ARITH_FAST)
+        // time-dependent coefficients (SABR, r != 0) re-evaluate their tables every step on the
+        // kernel-per-sweep path; the factorised paths precompute time-invariant line factors
+        if (p->arith == LSS_ADI_ARITH_FAST && !time_dependent(*p))
             rc = make_wide_solver(*p, hh->wide);
         else
             rc = p->precision == LSS_ADI_FP64 ? make_plain<double>(*p, p->arith, p->eval_s, p->eval_v, hh->s64)
@@ -126,6 +127,7 @@ int lss_adi_create_tabulated(const lss_adi_tables *t, lss_adi_handle **h)
     if (t->arith != LSS_ADI_ARITH_FAST && t->arith != LSS_ADI_ARITH_REFERENCE)
         return set_error(LSS_ADI_EINVAL, "lss_adi_create_tabulated: unknown arithmetic mode");
     if (!(t->t_hi > t->t_lo)) return set_error(LSS_ADI_EINVAL, "lss_adi_create_tabulated: empty time range");
+    if (t->options & ~LSS_ADI_OPT_DOUBLE_SWEEP) return set_error(LSS_ADI_EINVAL, "lss_adi_create_tabulated: unknown option bits");
     std::unique_ptr<lss_adi_handle> hh(new (std::nothrow) lss_adi_handle());
     if (!hh) return set_error(LSS_ADI_ENOMEM, "host allocation failed");
     hh->precision = t->precision;

@@ -1198,6 +1198,8 @@ adjoint_solver::~adjoint_solver() = default;
 int adjoint_solver::init(const lss_adi_problem &p)
 {
     if (p.nx > 256) return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_adjoint: nx > 256 not supported");
+    if (time_dependent(p))
+        return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_adjoint: SABR with r != 0 (time-dependent coefficients) not supported");
     if (p.scheme == LSS_ADI_HUNDSDORFER_VERWER)
         return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_adjoint: no adjoint for Hundsdorfer-Verwer yet");
     impl.reset(new (std::nothrow) adjoint_impl());
@@ -1311,6 +1313,9 @@ int lss_adi_batch_create(const lss_adi_problem *problems, int count, lss_adi_bat
         if (rc) return set_error(rc, "lss_adi_batch_create: instance " + std::to_string(k) + ": " + why);
         if (problems[k].precision != prec) return set_error(LSS_ADI_EINVAL, "lss_adi_batch_create: mixed precisions");
         if (problems[k].nx > 256) return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_batch_create: nx > 256 (use lss_adi_create)");
+        if (time_dependent(problems[k]))
+            return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_batch_create: instance " + std::to_string(k) +
+                                                       ": SABR with r != 0 has time-dependent coefficients (use lss_adi_create)");
     }
     std::unique_ptr<lss_adi_batch> h(new (std::nothrow) lss_adi_batch());
     if (!h) return set_error(LSS_ADI_ENOMEM, "host allocation failed");

@@ -38,6 +38,7 @@ template <typename T> struct dev_instance {
     const T *D0, *E0, *F0;                 // nx each: D, E, F on the v = v_lo line
     const T *s_lo, *s_hi_neu, *v_hi;       // ny, ny, nx
     const int *imap, *jmap;                // nx, ny
+    int ds;                                // 1: double-sweep line solves, 0: Thomas LU
 };
 
 // Stage selectors of the S-direction sweeps.

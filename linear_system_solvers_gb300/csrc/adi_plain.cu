@@ -50,10 +50,25 @@ __global__ void k_boundary1(dev_instance<T> d, const T *__restrict__ U, T *__res
 }
 
 // ------------------------------------------------------------------------------------------
+// One forward step of double_sweep_solver (lss_double_sweep_solver.hpp:114-155 with the
+// Dirichlet start L = 0, K = lo of lss_double_sweep_boundary.hpp:90-190):
+//   tmp = b + a*L;  L' = (-1*c)/tmp;  K' = (f - a*K)/tmp
+// and back substitution x_t = L_t*x_{t+1} + K_t from x_{n-1} = hi.
+// ------------------------------------------------------------------------------------------
+template <bool X, typename T> __device__ __forceinline__ void ds_forward(T a, T b, T c, T f, T &L, T &K)
+{
+    using R = ar<X>;
+    const T tmp = R::add(b, R::mul(a, L));
+    L = R::div(R::mul(T(-1), c), tmp);
+    K = R::div(R::sub(f, R::mul(a, K)), tmp);
+}
+
+// ------------------------------------------------------------------------------------------
 // S-line sweep: line j = 1..ny-2 solves rows 1..nx-2 of column j with Dirichlet ends
 // prev(0, jmap[j]) and prev(nx-1, jmap[j]) (get_intermed_horizontal, implicit_kernel.hpp:86-101);
 // matrix split_0 (lss_heat_douglas_rachford_method.hpp:159-169); Thomas LU in the
-// reference order (lss_thomas_lu_solver.hpp:161-190).  Y receives the whole column incl. ends.
+// reference order (lss_thomas_lu_solver.hpp:161-190), or the double sweep when d.ds is set.
+// Y receives the whole column incl. ends.
 // ------------------------------------------------------------------------------------------
 template <typename T, bool X, int STAGE>
 __global__ void k_s_sweep(dev_instance<T> d, const T *__restrict__ Ub, const T *__restrict__ A,
@@ -67,6 +82,31 @@ __global__ void k_s_sweep(dev_instance<T> d, const T *__restrict__ Ub, const T *
     const T lo = Ub[jj], hi = Ub[(nx - 1) * ny + jj];
     const T one = T(1);
     const int e = nx - 2;
+    if (d.ds) {
+        // double_sweep_solver: L/K recurrences, L in G and K in Y
+        T L = T(0), K = lo;
+        for (int t = 1; t <= e; ++t) {
+            const int o = t * ny + j;
+            const T a = R::mul(-d.theta, d.M[o]);
+            const T tz = R::mul(d.theta, d.Z[o]);
+            const T b = R::add(one, tz);
+            const T tp = R::mul(d.theta, d.P[o]);
+            const T c = -tp;
+            const T f = s_rhs<T, X, STAGE>(d, t, j, A, B, Cc, a, tz, tp);
+            ds_forward<X>(a, b, c, f, L, K);
+            G[o] = L;
+            Y[o] = K;
+        }
+        T x = hi;
+        for (int t = e; t >= 1; --t) {
+            const int o = t * ny + j;
+            x = R::add(R::mul(G[o], x), Y[o]);
+            Y[o] = x;
+        }
+        Y[j] = lo;
+        Y[(nx - 1) * ny + j] = hi;
+        return;
+    }
     T gam = T(0), y = T(0);
     for (int t = 1; t <= e; ++t) {
         const int o = t * ny + j;
@@ -120,6 +160,30 @@ __global__ void k_v_sweep(dev_instance<T> d, const T *__restrict__ in, const T *
     const T one = T(1);
     const int e = ny - 2;
     const int row = i * ny;
+    if (d.ds) {
+        T L = T(0), K = lo;
+        for (int t = 1; t <= e; ++t) {
+            const int o = row + t;
+            const T a = R::mul(-d.theta, d.Mt[o]);
+            const T tw = R::mul(d.theta, d.W[o]);
+            const T b = R::add(one, tw);
+            const T tp = R::mul(d.theta, d.Pt[o]);
+            const T c = -tp;
+            const T f = R::add(R::sub(R::add(R::mul(a, in[o - 1]), R::mul(tw, in[o])), R::mul(tp, in[o + 1])), inh[o]);
+            ds_forward<X>(a, b, c, f, L, K);
+            G[o] = L;
+            out[o] = K;
+        }
+        T x = hi;
+        for (int t = e; t >= 1; --t) {
+            const int o = row + t;
+            x = R::add(R::mul(G[o], x), out[o]);
+            out[o] = x;
+        }
+        out[row] = lo;
+        out[row + ny - 1] = hi;
+        return;
+    }
     T gam = T(0), y = T(0);
     for (int t = 1; t <= e; ++t) {
         const int o = row + t;
@@ -221,6 +285,42 @@ __global__ void k_eval(const T *__restrict__ V, int ny, bilinear b, double *__re
 }
 
 // ------------------------------------------------------------------------------------------
+// Time-dependent coefficients: M, P, Z, C on the grid and D on the v = v_lo line at the time
+// of this step (general_heston_equation_coefficients, coefficients.hpp:89-98, on the
+// transformed data of lss_heat_data_transform.hpp:174-214), from the time-independent
+// factors and this step's D(t) powers da = D^(2(1-beta)), dc = D^(1-beta).
+// ------------------------------------------------------------------------------------------
+template <typename T> struct time_tables {
+    const double *a_static, *c_static; // nx*ny
+    const T *ab;                       // nx*ny
+    const T *per_i;                    // 5*nx: A, A*A, A*A*A, A', user d
+    T *M, *P, *Z, *C, *D0;
+    T alpha, delta, two_alpha, half_rho_f;
+};
+
+template <typename T, bool X>
+__global__ void k_refresh(time_tables<T> tt, int nx, int ny, double da, double dc)
+{
+    using R = ar<X>;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y;
+    if (j >= ny) return;
+    const size_t o = static_cast<size_t>(i) * ny + j;
+    const T aval = tt.per_i[i], aa = tt.per_i[nx + i], aaa = tt.per_i[2 * nx + i];
+    const T gc = tt.per_i[3 * nx + i], ud = tt.per_i[4 * nx + i];
+    const T A = static_cast<T>(__dmul_rn(tt.a_static[o], da));
+    const T ah = R::div(A, aa);
+    const T ch = R::div(static_cast<T>(__dmul_rn(tt.c_static[o], dc)), tt.ab[o]);
+    const T dh = R::sub(R::div(ud, aval), R::div(R::mul(A, gc), aaa));
+    const T aah = R::mul(tt.alpha, ah), ddh = R::mul(tt.delta, dh);
+    tt.M[o] = R::sub(aah, ddh);
+    tt.P[o] = R::add(aah, ddh);
+    tt.Z[o] = R::sub(R::mul(tt.two_alpha, ah), tt.half_rho_f);
+    tt.C[o] = ch;
+    if (j == 0) tt.D0[i] = dh;
+}
+
+// ------------------------------------------------------------------------------------------
 // host side
 // ------------------------------------------------------------------------------------------
 template <typename T> int plain_solver<T>::init(instance_tables<T> &&tab, int arith, double eval_s, double eval_v)
@@ -274,6 +374,18 @@ template <typename T> int plain_solver<T>::init(instance_tables<T> &&tab, int ar
     d_.v_hi = small_.p + 3 * nx + 2 * ny;
     d_.imap = maps_.p;
     d_.jmap = maps_.p + nx;
+    d_.ds = tab_.double_sweep;
+    if (tab_.tdep) {
+        LSS_CUDA_TRY(tdep_d_.alloc(2 * n), "allocating time-dependent tables");
+        LSS_CUDA_TRY(tdep_d_.upload(tab_.a_static.data(), n), "uploading time-dependent tables");
+        LSS_CUDA_TRY(cudaMemcpy(tdep_d_.p + n, tab_.c_static.data(), n * sizeof(double), cudaMemcpyHostToDevice),
+                     "uploading time-dependent tables");
+        LSS_CUDA_TRY(tdep_t_.alloc(n + 5 * static_cast<size_t>(nx)), "allocating time-dependent tables");
+        LSS_CUDA_TRY(tdep_t_.upload(tab_.ab.data(), n), "uploading time-dependent tables");
+        LSS_CUDA_TRY(cudaMemcpy(tdep_t_.p + n, tab_.per_i.data(), 5 * nx * sizeof(T), cudaMemcpyHostToDevice),
+                     "uploading time-dependent tables");
+        LSS_CUDA_TRY(cudaDeviceSynchronize(), "uploading time-dependent tables");
+    }
     bil_ = make_bilinear(tab_.x.data(), nx, tab_.y.data(), ny, eval_s, eval_v);
     return LSS_ADI_OK;
 }
@@ -287,7 +399,28 @@ template <typename T> template <bool X> void plain_solver<T>::enqueue_steps(cuda
     const int bs = 64;
     const int gs = grid_for(ny - 2, bs), gv = grid_for(nx - 2, bs);
     const dim3 ghv(grid_for(ny - 2, 128), nx - 2);
+    time_tables<T> tt{};
+    if (tab_.tdep) {
+        tt.a_static = tdep_d_.p;
+        tt.c_static = tdep_d_.p + n;
+        tt.ab = tdep_t_.p;
+        tt.per_i = tdep_t_.p + n;
+        tt.M = coef_.p;
+        tt.P = coef_.p + n;
+        tt.Z = coef_.p + 2 * n;
+        tt.C = coef_.p + 6 * n;
+        tt.D0 = small_.p;
+        tt.alpha = tab_.sc.alpha;
+        tt.delta = tab_.sc.delta;
+        tt.two_alpha = tab_.two_alpha;
+        tt.half_rho_f = tab_.half_rho_f;
+    }
+    const dim3 gref(grid_for(ny, 128), nx);
     for (int step = 0; step < tab_.steps; ++step) {
+        if (tab_.tdep) {
+            k_refresh<T, X><<<gref, 128, 0, s>>>(tt, nx, ny, tab_.step_da[step], tab_.step_dc[step]);
+            launches_ += 1;
+        }
         k_boundary1<T, X><<<grid_for(nx, 128), 128, 0, s>>>(d_, U, bcol0, bcolN);
         k_s_sweep<T, X, S_STAGE1><<<gs, bs, 0, s>>>(d_, U, U, nullptr, nullptr, Y1, G);
         switch (tab_.scheme) {

@@ -11,7 +11,8 @@ template <typename T> struct plain_solver {
     instance_tables<T> tab_;
     int arith_ = LSS_ADI_ARITH_REFERENCE;
     dev_instance<T> d_{};
-    dbuf<T> coef_, small_, state_;
+    dbuf<T> coef_, small_, state_, tdep_t_;
+    dbuf<double> tdep_d_;
     dbuf<int> maps_;
     dbuf<double> value_;
     bilinear bil_{};

@@ -100,6 +100,7 @@ inline scheme_scalars<T> make_scalars(int nx, int ny, int nt, T t_lo, T t_hi, do
 // Host copy of everything the device time loop reads.
 template <typename T> struct instance_tables {
     int nx = 0, ny = 0, steps = 0, scheme = 0, forward = 0;
+    int double_sweep = 0;          // tridiagonal_method_enum::DoubleSweepSolver
     scheme_scalars<T> sc;
     T neu{};                       // Neumann data * A(1) (constant along S_hi on this path)
     std::vector<T> coef;           // 7*nx*ny: M, P, Z, Mt, Pt, W, C
@@ -111,7 +112,20 @@ template <typename T> struct instance_tables {
     std::vector<T> payoff;         // nx*ny
     std::vector<T> x, y;           // physical grid
     T t_first{};                   // time of the first step
+    // Time-dependent coefficients (SABR with r != 0: a and c carry D(t)^(2(1-beta)) and
+    // D(t)^(1-beta), D(t) = exp(-r (T - t))).  Each step re-evaluates M, P, Z, C and the
+    // D line from the time-independent factors below, in the reference's operation order.
+    int tdep = 0;
+    std::vector<double> a_static;  // nx*ny: (0.5 v) v S^(2 beta)            (double, as the lambda)
+    std::vector<double> c_static;  // nx*ny: ((rho nu) v) v S^beta            (double)
+    std::vector<T> ab;             // nx*ny: A(zeta_i) B(eta_j)
+    std::vector<T> per_i;          // 5*nx: A, A*A, A*A*A, A'(zeta_i), user d(S_i)
+    T two_alpha{}, half_rho_f{};   // 2*alpha, (0.5*rho)*f^
+    std::vector<double> step_da, step_dc; // per step: D^(2(1-beta)), D^(1-beta)
 };
+
+// SABR with r != 0 is the one parametric problem whose coefficients depend on time.
+inline bool time_dependent(const lss_adi_problem &p) { return p.model == LSS_ADI_SABR && p.rate != 0.0; }
 
 int validate_problem(const lss_adi_problem &p, std::string &why);
 
@@ -166,6 +180,51 @@ template <typename T> struct model_lambdas {
     }
 };
 
+// Time-independent factors of the SABR coefficients and the per-step D(t) powers.  The
+// lambdas evaluate ((((0.5 v) v) S^(2b)) D^(2(1-b))) and (((((rho nu) v) v) S^b) D^(1-b))
+// left to right in double, so splitting off the last factor keeps every rounding.
+template <typename T> inline void build_time_tables(const lss_adi_problem &p, const sinh_map<T> &g, instance_tables<T> &it)
+{
+    const auto &sc = it.sc;
+    const int nx = p.nx, ny = p.ny;
+    const std::size_t n = static_cast<std::size_t>(nx) * ny;
+    it.tdep = 1;
+    it.a_static.resize(n);
+    it.c_static.resize(n);
+    it.ab.resize(n);
+    it.per_i.resize(5 * static_cast<std::size_t>(nx));
+    for (int i = 0; i < nx; ++i) {
+        const T zeta = sc.h1 * static_cast<T>(i);
+        const T x = g.x(zeta), aval = g.a_der(zeta);
+        it.per_i[0 * nx + i] = aval;
+        it.per_i[1 * nx + i] = aval * aval;
+        it.per_i[2 * nx + i] = aval * aval * aval;
+        it.per_i[3 * nx + i] = g.c_der(zeta);
+        it.per_i[4 * nx + i] = static_cast<T>(p.rate * static_cast<double>(x));
+        for (int j = 0; j < ny; ++j) {
+            const T eta = sc.h2 * static_cast<T>(j);
+            const T y = g.y(eta), bval = g.b_der(eta);
+            const double s = static_cast<double>(x), v = static_cast<double>(y);
+            const std::size_t o = static_cast<std::size_t>(i) * ny + j;
+            it.a_static[o] = 0.5 * v * v * std::pow(s, 2.0 * p.sabr_beta);
+            it.c_static[o] = p.rho * p.sigma * v * v * std::pow(s, p.sabr_beta);
+            it.ab[o] = aval * bval;
+        }
+    }
+    const T two = T(2.0), half = T(0.5);
+    it.two_alpha = two * sc.alpha;
+    it.half_rho_f = half * sc.rho * static_cast<T>(-p.rate);
+    it.step_da.resize(it.steps);
+    it.step_dc.resize(it.steps);
+    T t = it.t_first;
+    for (int s = 0; s < it.steps; ++s) {
+        const double D = std::exp(-p.rate * (p.maturity - static_cast<double>(t)));
+        it.step_da[s] = std::pow(D, 2.0 * (1.0 - p.sabr_beta));
+        it.step_dc[s] = std::pow(D, (1.0 - p.sabr_beta));
+        t = p.forward ? (t + sc.k) : (t - sc.k);
+    }
+}
+
 // Builds the tables of a parametric problem at time t (coefficients) -- Heston
 // coefficients do not depend on t; SABR ones only through D(t) = exp(-r (T - t)).
 template <typename T> inline void build_tables(const lss_adi_problem &p, instance_tables<T> &it)
@@ -175,6 +234,7 @@ template <typename T> inline void build_tables(const lss_adi_problem &p, instanc
     it.steps = p.nt - 1;
     it.scheme = p.scheme;
     it.forward = p.forward;
+    it.double_sweep = (p.options & LSS_ADI_OPT_DOUBLE_SWEEP) ? 1 : 0;
     it.sc = make_scalars<T>(p.nx, p.ny, p.nt, T(0.0), static_cast<T>(p.maturity), p.zeta, p.theta_scheme);
     sinh_map<T> g;
     g.init(p);
@@ -230,6 +290,7 @@ template <typename T> inline void build_tables(const lss_adi_problem &p, instanc
     for (int i = 0; i < p.nx; ++i)
         for (int j = 0; j < p.ny; ++j) it.payoff[static_cast<std::size_t>(i) * p.ny + j] = m.payoff(it.x[i]);
     fill_index_maps(it);
+    if (time_dependent(p)) build_time_tables(p, g, it);
 }
 
 // Tables from caller-sampled coefficients (lss_adi_tables).
@@ -240,6 +301,7 @@ template <typename T> inline void build_tables(const lss_adi_tables &t, instance
     it.steps = t.nt - 1;
     it.scheme = t.scheme;
     it.forward = t.forward;
+    it.double_sweep = (t.options & LSS_ADI_OPT_DOUBLE_SWEEP) ? 1 : 0;
     it.sc = make_scalars<T>(t.nx, t.ny, t.nt, static_cast<T>(t.t_lo), static_cast<T>(t.t_hi), t.zeta, t.theta_scheme);
     const std::size_t n = static_cast<std::size_t>(t.nx) * t.ny;
     const T *c = static_cast<const T *>(t.coef);
@@ -270,6 +332,7 @@ template <typename T> inline void convert_tables(const instance_tables<double> &
     t.steps = d.steps;
     t.scheme = d.scheme;
     t.forward = d.forward;
+    t.double_sweep = d.double_sweep;
     t.sc.k = static_cast<T>(d.sc.k);
     t.sc.h1 = static_cast<T>(d.sc.h1);
     t.sc.h2 = static_cast<T>(d.sc.h2);
@@ -293,6 +356,15 @@ template <typename T> inline void convert_tables(const instance_tables<double> &
     t.x = cv(d.x);
     t.y = cv(d.y);
     t.t_first = static_cast<T>(d.t_first);
+    t.tdep = d.tdep;
+    t.a_static = d.a_static;
+    t.c_static = d.c_static;
+    t.ab = cv(d.ab);
+    t.per_i = cv(d.per_i);
+    t.two_alpha = static_cast<T>(d.two_alpha);
+    t.half_rho_f = static_cast<T>(d.half_rho_f);
+    t.step_da = d.step_da;
+    t.step_dc = d.step_dc;
 }
 
 // Parametric problem -> tables in T, honouring LSS_ADI_OPT_FP64_TABLES.

@@ -46,6 +46,7 @@ class HestonProblem:
     eval_s: float = 100.0
     eval_v: float = 0.04
     fp64_tables: bool = False  # FP32 only: tables and index_of remaps built in double
+    solver: str = "tlu"  # tridiagonal_method_enum: "tlu" ThomasLUSolver | "ds" DoubleSweepSolver
 
     @property
     def steps(self) -> int:
@@ -65,7 +66,9 @@ class HestonProblem:
         c.forward = int(bool(self.forward))
         c.precision = L.FP32 if precision == "f32" else L.FP64
         c.arith = L.ARITH_REFERENCE if arith == "reference" else L.ARITH_FAST
-        c.options = L.OPT_FP64_TABLES if self.fp64_tables else 0
+        if self.solver not in ("tlu", "ds"):
+            raise ValueError(f"solver must be 'tlu' or 'ds', not {self.solver!r}")
+        c.options = (L.OPT_FP64_TABLES if self.fp64_tables else 0) | (L.OPT_DOUBLE_SWEEP if self.solver == "ds" else 0)
         return c
 
 
@@ -137,7 +140,7 @@ class TabulatedHestonSolver(ImplicitHestonSolver):
     """
 
     def __init__(self, nt, t_lo, t_hi, scheme, theta_scheme, coef, coef_v0, s_lo, s_hi_neumann, v_hi, payoff,
-                 zeta=0.5, forward=False, precision="f64", arith="fast"):
+                 zeta=0.5, forward=False, precision="f64", arith="fast", solver="tlu"):
         self.lib = L.load()
         self.precision = precision
         self.dtype = _dtype(precision)
@@ -154,6 +157,7 @@ class TabulatedHestonSolver(ImplicitHestonSolver):
         t.precision = L.FP32 if precision == "f32" else L.FP64
         t.arith = L.ARITH_REFERENCE if arith == "reference" else L.ARITH_FAST
         t.zeta = float(zeta)
+        t.options = L.OPT_DOUBLE_SWEEP if solver == "ds" else 0
         t.coef, t.coef_v0, t.s_lo_dirichlet, t.s_hi_neumann, t.v_hi_dirichlet, t.payoff = [a.ctypes.data for a in arrs]
         h = ctypes.c_void_p()
         L.check(self.lib.lss_adi_create_tabulated(ctypes.byref(t), ctypes.byref(h)))

@@ -33,9 +33,7 @@ def problem_pair(kw):
     from oracle import oracle as O
     import linear_system_solvers_gb300 as lss
 
-    okw = dict(kw)
-    pkw = {k: v for k, v in kw.items() if k != "solver"}
-    return O.Problem(**okw), lss.HestonProblem(**pkw)
+    return O.Problem(**kw), lss.HestonProblem(**kw)
 
 
 def rel_err(a, ref):

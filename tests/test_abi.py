@@ -30,7 +30,7 @@ def test_library_exports_every_declared_symbol(lss):
 @pytest.mark.parametrize("bad,code", [
     (dict(nx=3), 1), (dict(ny=3), 1), (dict(nt=1), 1), (dict(scheme_id=7), 1), (dict(theta_id=9), 1),
     (dict(s_hi=-5.0), 1), (dict(maturity=0.0), 1), (dict(precision_id=5), 1), (dict(model_id=3), 1),
-    (dict(kappa=float("nan")), 1), (dict(sabr_rate=0.03), 2),
+    (dict(kappa=float("nan")), 1), (dict(options=64), 1),
 ])
 def test_create_rejects_invalid_problem_without_device(lss, bad, code):
     from linear_system_solvers_gb300 import _lib as L
@@ -46,9 +46,6 @@ def test_create_rejects_invalid_problem_without_device(lss, bad, code):
             c.precision = v
         elif k == "model_id":
             c.model = v
-        elif k == "sabr_rate":
-            c.model = L.SABR
-            c.rate = v
         else:
             setattr(c, k, v)
     h = ctypes.c_void_p()
@@ -56,6 +53,20 @@ def test_create_rejects_invalid_problem_without_device(lss, bad, code):
     assert rc == code
     assert h.value is None
     assert L.load().lss_adi_last_error().decode().startswith("lss_adi_create:")
+
+
+def test_time_dependent_sabr_is_single_instance_only(lss):
+    # SABR with r != 0 carries D(t) = exp(-r (T - t)) in its coefficients: lss_adi_create runs
+    # it (tables re-evaluated every step); the batch and the adjoint refuse it before any
+    # device work
+    from linear_system_solvers_gb300 import _lib as L
+
+    p = lss.HestonProblem(model="sabr", rate=0.03, sigma=0.4, rho=-0.3, strike=0.05, s_hi=0.2, v_hi=1.0, nx=16, ny=8, nt=5)
+    arr = (L.LssAdiProblem * 2)(p.to_c(), p.to_c())
+    b = ctypes.c_void_p()
+    assert L.load().lss_adi_batch_create(arr, 2, ctypes.byref(b)) == L.EUNSUPPORTED
+    assert b.value is None
+    assert "time-dependent" in L.load().lss_adi_last_error().decode()
 
 
 def test_null_arguments_are_rejected(lss):

@@ -3,13 +3,14 @@ against the CPU oracle, which is bit-exact with the reference's host Thomas-LU p
 import numpy as np
 import pytest
 
-from cases import CONFIG1, SMALL
+from cases import CONFIG1, GOLDEN, SMALL
 from conftest import fp32_ok, fp64_tol, problem_pair, rel_err
 
 pytestmark = pytest.mark.gpu
 
 NU = dict(nonuniform=True, acc_point=100.0, alpha_scale=10.0, beta_scale=24.0)
-CASES = {k: v for k, v in SMALL.items() if v[0].get("solver", "tlu") == "tlu"}
+SABR_T = dict(GOLDEN["ImplSABREquationDoubleSweepSolverCrankNicolson"], nx=44, ny=26, nt=31)
+CASES = dict(SMALL)
 CASES.update({
     "config1_dr_f64": (dict(CONFIG1), "f64"),
     "config1_dr_f32": (dict(CONFIG1), "f32"),
@@ -21,6 +22,15 @@ CASES.update({
     "hv_theta80_fwd_f64": (dict(CONFIG1, scheme="hv", theta_scheme="theta80", forward=True, nx=50, ny=40, nt=31), "f64"),
     "line_len4_f64": (dict(CONFIG1, scheme="mcs", nx=4, ny=5, nt=9), "f64"),
     "wide_f64": (dict(CONFIG1, scheme="cs", nx=300, ny=6, nt=11, **NU), "f64"),
+    # tridiagonal_method_enum::DoubleSweepSolver on every scheme
+    "cs_ds_f64": (dict(CONFIG1, scheme="cs", solver="ds", nx=48, ny=25, nt=31, **NU), "f64"),
+    "mcs_ds_f32": (dict(CONFIG1, scheme="mcs", solver="ds", nx=41, ny=19, nt=31, **NU), "f32"),
+    "hv_ds_f64": (dict(CONFIG1, scheme="hv", solver="ds", nx=50, ny=26, nt=33, **NU), "f64"),
+    # SABR with r != 0: coefficients re-evaluated at every step's time
+    "sabr_t_tlu_f64": (dict(SABR_T, solver="tlu"), "f64"),
+    "sabr_t_ds_f32": (dict(SABR_T), "f32"),
+    "sabr_t_hv_fwd_f64": (dict(SABR_T, scheme="hv", forward=True, solver="tlu"), "f64"),
+    "sabr_t_mcs_f64": (dict(SABR_T, scheme="mcs", solver="ds"), "f64"),
 })
 
 
@@ -35,7 +45,8 @@ def test_reference_arith_is_bitwise_identical_to_oracle(lss, oracle, key):
     assert np.array_equal(got, want, equal_nan=True), f"max rel err {rel_err(got, want):.3e}"
 
 
-@pytest.mark.parametrize("key", ["config1_dr_f64", "cs_nu_f64", "mcs_odd_f64", "hv_nu_f64", "hv_theta80_fwd_f64"])
+@pytest.mark.parametrize("key", ["config1_dr_f64", "cs_nu_f64", "mcs_odd_f64", "hv_nu_f64", "hv_theta80_fwd_f64",
+                                 "dr_ds_f64", "sabr_ds_f64", "sabr_t_tlu_f64", "sabr_t_hv_fwd_f64"])
 def test_fast_arith_within_1e10_of_oracle(lss, oracle, key):
     kw, fp = CASES[key]
     op, pp = problem_pair(kw)
@@ -163,3 +174,30 @@ def test_tabulated_drop_in_bitwise_equals_parametric(lss, oracle, scheme):
     got, _ = tab.solve()
     want = oracle.solve(op, "f64")
     assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("name", sorted(GOLDEN))
+def test_reference_golden_problems_on_device(lss, oracle, name):
+    """The problems of the reference's own print tests (outputs/*.txt): the device path in
+    reference arithmetic equals the oracle bit for bit (both precisions), and its surface
+    written in the reference's print format reproduces the golden file's 6-digit numbers."""
+    import os
+
+    from linear_system_solvers_gb300.printing import format_surface
+
+    op, pp = problem_pair(GOLDEN[name])
+    for fp in ("f64", "f32"):
+        want = oracle.solve(op, fp)
+        s = lss.ImplicitHestonSolver(pp, precision=fp, arith="reference")
+        got, _ = s.solve()
+        assert np.array_equal(got, want, equal_nan=True), (fp, rel_err(got, want))
+    gold = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_outputs.npz"))
+    key = f"{name}|f64|values"
+    if key in gold.files:
+        s = lss.ImplicitHestonSolver(pp, precision="f64", arith="reference")
+        x, y = s.grid()
+        text = format_surface(x, y, s.solve()[0])
+        rows = text.split("VALUES\n")[1].strip().split("\n")
+        vals = np.array([[float(t) for t in r.split(",")] for r in rows])
+        assert np.mean(vals == gold[key]) > 0.999
+        assert rel_err(vals, gold[key]) < 6e-6
