@@ -119,6 +119,11 @@ typedef struct lss_adi_problem {
  *   solve the same systems, so LSS_ADI_ARITH_FAST (one precomputed factorisation) serves
  *   both and ignores this bit. */
 #define LSS_ADI_OPT_DOUBLE_SWEEP 2
+/* LINE_PER_THREAD: LSS_ADI_ARITH_FAST single instance: solve every line with one thread (the
+ *   batched kernel's arithmetic, bit for bit) instead of the autotuned partitioned line
+ *   solves, which cut each line into chunks to occupy the whole GPU on one instance and
+ *   differ from it by rounding only. */
+#define LSS_ADI_OPT_LINE_PER_THREAD 4
 
 /*
  * Tabulated drop-in: time-invariant scheme coefficients already sampled on the grid by
@@ -174,6 +179,14 @@ int lss_adi_adjoint(lss_adi_handle *h, const void *payoff, double *out_value, do
 /* Grid of the handle: x (nx) = S_i, y (ny) = v_j, in the precision's type (host). */
 int lss_adi_grid(const lss_adi_handle *h, void *x, void *y);
 
+/* Partitioned line solves of a LSS_ADI_ARITH_FAST single instance: every S line is cut into
+ * s_chunks and every v line into v_chunks pieces solved concurrently (1 = thread per line;
+ * at most 32; at least 4 rows per chunk).  0 for either picks it by timing the sweeps (the
+ * autotuner lss_adi_create runs by default).  out_s / out_v (may be NULL) receive the
+ * counts in use.  LSS_ADI_EUNSUPPORTED for handles on the kernel-per-sweep path.  No
+ * counterpart in the reference, whose line solves are serial. */
+int lss_adi_line_chunks(lss_adi_handle *h, int s_chunks, int v_chunks, int *out_s, int *out_v, void *stream);
+
 void lss_adi_destroy(lss_adi_handle *h);
 
 /* --- batched uneven instances ---------------------------------------------------------- */
@@ -209,8 +222,8 @@ int lss_adi_batch_surface(lss_adi_batch *b, int index, void *out_surface);
 /* dV/d(initial condition grid) of instance `index` after a mode-1 run (host, FP64, Nx*Ny). */
 int lss_adi_batch_payoff_gradient(lss_adi_batch *b, int index, void *out);
 
-/* Lines-per-CTA autotuner: runs `mode` once per CTA size (64, 128, 256 threads per instance;
- * each thread owns one S-line or v-line at a time) and keeps the fastest for later runs of
+/* Lines-per-CTA autotuner: runs `mode` once per CTA size (32, 64, 128, 256 threads per
+ * instance; each thread owns one S-line or v-line at a time) and keeps the fastest for later runs of
  * that mode.  With *threads_per_instance > 0 on entry it sets that size without timing; on
  * return it holds the size in use.  The runs overwrite the batch's results. */
 int lss_adi_batch_autotune(lss_adi_batch *b, int mode, int *threads_per_instance, void *stream);

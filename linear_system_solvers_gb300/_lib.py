@@ -20,6 +20,7 @@ FP64, FP32 = 0, 1
 ARITH_FAST, ARITH_REFERENCE = 0, 1
 OPT_FP64_TABLES = 1
 OPT_DOUBLE_SWEEP = 2
+OPT_LINE_PER_THREAD = 4
 HESTON, SABR = 0, 1
 SCHEMES = {"dr": 0, "cs": 1, "mcs": 2, "hv": 3}
 THETAS = {"euler": 0, "theta30": 1, "cn": 2, "theta80": 3}
@@ -63,6 +64,7 @@ SIGNATURES = {
     "lss_adi_forward_graph": (c_int, [c_void_p, c_void_p, c_void_p, P(c_double), c_int, c_void_p]),
     "lss_adi_adjoint": (c_int, [c_void_p, c_void_p, P(c_double), P(c_double), c_void_p, c_int, c_int, c_void_p]),
     "lss_adi_grid": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "lss_adi_line_chunks": (c_int, [c_void_p, c_int, c_int, P(c_int), P(c_int), c_void_p]),
     "lss_adi_destroy": (None, [c_void_p]),
     "lss_adi_batch_create": (c_int, [P(LssAdiProblem), c_int, P(c_void_p)]),
     "lss_adi_batch_run": (c_int, [c_void_p, c_int, c_void_p]),

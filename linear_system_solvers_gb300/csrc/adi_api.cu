@@ -43,7 +43,8 @@ int validate_problem(const lss_adi_problem &p, std::string &why)
     const double vals[] = {p.kappa, p.theta_v, p.sigma, p.rho, p.rate, p.sabr_beta, p.strike, p.zeta, p.neumann_value, p.acc_point};
     for (double v : vals)
         if (!std::isfinite(v)) return why = "non-finite model parameter", LSS_ADI_EINVAL;
-    if (p.options & ~(LSS_ADI_OPT_FP64_TABLES | LSS_ADI_OPT_DOUBLE_SWEEP)) return why = "unknown option bits", LSS_ADI_EINVAL;
+    if (p.options & ~(LSS_ADI_OPT_FP64_TABLES | LSS_ADI_OPT_DOUBLE_SWEEP | LSS_ADI_OPT_LINE_PER_THREAD))
+        return why = "unknown option bits", LSS_ADI_EINVAL;
     return LSS_ADI_OK;
 }
 
@@ -196,6 +197,14 @@ int lss_adi_grid(const lss_adi_handle *h, void *x, void *y)
         std::copy(h->s32->tab_.y.begin(), h->s32->tab_.y.end(), static_cast<float *>(y));
     }
     return LSS_ADI_OK;
+}
+
+int lss_adi_line_chunks(lss_adi_handle *h, int s_chunks, int v_chunks, int *out_s, int *out_v, void *stream)
+{
+    clear_error();
+    if (!h) return set_error(LSS_ADI_EINVAL, "lss_adi_line_chunks: null handle");
+    if (!h->wide) return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_line_chunks: not a partitioned (fast single-instance) handle");
+    return h->wide->chunks(s_chunks, v_chunks, out_s, out_v, stream);
 }
 
 void lss_adi_destroy(lss_adi_handle *h) { delete h; }

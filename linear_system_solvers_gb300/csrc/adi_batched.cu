@@ -244,6 +244,89 @@ template <typename T> __device__ __forceinline__ void b2_stage(const inst_view<T
 // S-line sweeps.  KIND 1: explicit operator on U (Y1).  KIND 2: second S stage of
 // CS/MCS/HV on U, Y1, Y2 (scheme chooses the weights).  Thread per line j; every access
 // of a warp is one coalesced row segment.
+//
+// s_line_fwd: right-hand side and forward recurrence y_t = f_t - la_t y_{t-1} of line j over
+// rows t0..t1, starting from y = y_{t0-1}; writes y_t into Y and returns y_{t1}.
+template <typename T, int KIND>
+__device__ __forceinline__ T s_line_fwd(const inst_view<T> &v, int scheme, const T *__restrict__ U,
+                                        const T *__restrict__ Y1, const T *__restrict__ Y2, T *__restrict__ Y, int j,
+                                        int t0, int t1, T y, T hi)
+{
+    const int ny = v.ny, e = v.e_s;
+    const long long b = (long long)(t0 - 1) * ny + j;
+    if constexpr (KIND == 1) {
+        // sliding 3x3 window of U
+        T u0m = U[b - 1], u0c = U[b], u0p = U[b + 1];
+        T u1m = U[b + ny - 1], u1c = U[b + ny], u1p = U[b + ny + 1];
+#pragma unroll 4
+        for (int t = t0; t <= t1; ++t) {
+            const long long o = (long long)t * ny + j;
+            const T u2m = U[o + ny - 1], u2c = U[o + ny], u2p = U[o + ny + 1];
+            const T mix = (u0m - u0p) + (u2p - u2m);
+            T f = ldg(v.S(SL_WG) + o) * mix;
+            f += ldg(v.S(SL_WW) + o) * u0c;
+            f += ldg(v.S(SL_WS) + o) * u1m;
+            f += ldg(v.S(SL_WC) + o) * u1c;
+            f += ldg(v.S(SL_WN) + o) * u1p;
+            f += ldg(v.S(SL_WE) + o) * u2c;
+            y = f - ldg(v.S(SL_LA) + o) * y;
+            if (t == e) y -= ldg(v.Yv(Y_CHS) + j) * hi;
+            Y[o] = y;
+            u0m = u1m; u0c = u1c; u0p = u1p;
+            u1m = u2m; u1c = u2c; u1p = u2p;
+        }
+    } else {
+        // windows: U centre column, Y1 centre column, Delta = Y2 - U 3x3
+        T uc0 = U[b], uc1 = U[b + ny];
+        T y10 = Y1[b], y11 = Y1[b + ny];
+        T d0m = Y2[b - 1] - U[b - 1], d0c = Y2[b] - uc0, d0p = Y2[b + 1] - U[b + 1];
+        T d1m = Y2[b + ny - 1] - U[b + ny - 1], d1c = Y2[b + ny] - uc1, d1p = Y2[b + ny + 1] - U[b + ny + 1];
+#pragma unroll 4
+        for (int t = t0; t <= t1; ++t) {
+            const long long o = (long long)t * ny + j;
+            const T uc2 = U[o + ny];
+            const T y12 = Y1[o + ny];
+            const T d2m = Y2[o + ny - 1] - U[o + ny - 1];
+            const T d2c = Y2[o + ny] - uc2;
+            const T d2p = Y2[o + ny + 1] - U[o + ny + 1];
+            const T mix = (d0m - d0p) + (d2p - d2m);
+            T f;
+            if (scheme == LSS_ADI_HUNDSDORFER_VERWER) {
+                f = ldg(v.S(SL_LA) + o) * y10;
+                f += ldg(v.S(SL_S2SC) + o) * y11;
+                f += ldg(v.S(SL_S2SE) + o) * y12;
+                f += ldg(v.S(SL_S2MZ) + o) * mix;
+                f += ldg(v.S(SL_X1) + o) * d0c;
+                f += ldg(v.S(SL_X2) + o) * d1c;
+                f += ldg(v.S(SL_X3) + o) * d2c;
+                f += ldg(v.S(SL_X4) + o) * d1m;
+                f += ldg(v.S(SL_X5) + o) * d1p;
+            } else {
+                f = ldg(v.S(SL_LA) + o) * uc0;
+                f += ldg(v.S(SL_S2SC) + o) * uc1;
+                f += ldg(v.S(SL_S2SE) + o) * uc2;
+                f += ldg(v.S(SL_S2IB) + o) * y11;
+                f += ldg(v.S(SL_S2MZ) + o) * mix;
+                if (scheme == LSS_ADI_MODIFIED_CRAIG_SNEYD) {
+                    f += ldg(v.S(SL_X1) + o) * d0c;
+                    f += ldg(v.S(SL_X2) + o) * d1c;
+                    f += ldg(v.S(SL_X3) + o) * d2c;
+                    f += ldg(v.S(SL_X4) + o) * d1m;
+                    f += ldg(v.S(SL_X5) + o) * d1p;
+                }
+            }
+            y = f - ldg(v.S(SL_LA) + o) * y;
+            if (t == e) y -= ldg(v.Yv(Y_CHS) + j) * hi;
+            Y[o] = y;
+            uc0 = uc1; uc1 = uc2;
+            y10 = y11; y11 = y12;
+            d0m = d1m; d0c = d1c; d0p = d1p;
+            d1m = d2m; d1c = d2c; d1p = d2p;
+        }
+    }
+    return y;
+}
+
 template <typename T, int KIND>
 __device__ __forceinline__ void s_stage(const inst_view<T> &v, int scheme, const T *__restrict__ U,
                                         const T *__restrict__ Y1, const T *__restrict__ Y2, T *__restrict__ Y, int l0,
@@ -253,78 +336,7 @@ __device__ __forceinline__ void s_stage(const inst_view<T> &v, int scheme, const
     for (int j = 1 + l0; j <= ny - 2; j += ls) {
         const int jj = ldg(v.jmap() + j);
         const T lo = U[jj], hi = U[(long long)(nx - 1) * ny + jj];
-        T y = lo;
-        if constexpr (KIND == 1) {
-            // sliding 3x3 window of U
-            T u0m = U[j - 1], u0c = U[j], u0p = U[j + 1];
-            T u1m = U[ny + j - 1], u1c = U[ny + j], u1p = U[ny + j + 1];
-#pragma unroll 4
-            for (int t = 1; t <= e; ++t) {
-                const long long o = (long long)t * ny + j;
-                const T u2m = U[o + ny - 1], u2c = U[o + ny], u2p = U[o + ny + 1];
-                const T mix = (u0m - u0p) + (u2p - u2m);
-                T f = ldg(v.S(SL_WG) + o) * mix;
-                f += ldg(v.S(SL_WW) + o) * u0c;
-                f += ldg(v.S(SL_WS) + o) * u1m;
-                f += ldg(v.S(SL_WC) + o) * u1c;
-                f += ldg(v.S(SL_WN) + o) * u1p;
-                f += ldg(v.S(SL_WE) + o) * u2c;
-                y = f - ldg(v.S(SL_LA) + o) * y;
-                if (t == e) y -= ldg(v.Yv(Y_CHS) + j) * hi;
-                Y[o] = y;
-                u0m = u1m; u0c = u1c; u0p = u1p;
-                u1m = u2m; u1c = u2c; u1p = u2p;
-            }
-        } else {
-            // windows: U centre column, Y1 centre column, Delta = Y2 - U 3x3
-            T uc0 = U[j], uc1 = U[ny + j];
-            T y10 = Y1[j], y11 = Y1[ny + j];
-            T d0m = Y2[j - 1] - U[j - 1], d0c = Y2[j] - uc0, d0p = Y2[j + 1] - U[j + 1];
-            T d1m = Y2[ny + j - 1] - U[ny + j - 1], d1c = Y2[ny + j] - uc1, d1p = Y2[ny + j + 1] - U[ny + j + 1];
-#pragma unroll 4
-            for (int t = 1; t <= e; ++t) {
-                const long long o = (long long)t * ny + j;
-                const T uc2 = U[o + ny];
-                const T y12 = Y1[o + ny];
-                const T d2m = Y2[o + ny - 1] - U[o + ny - 1];
-                const T d2c = Y2[o + ny] - uc2;
-                const T d2p = Y2[o + ny + 1] - U[o + ny + 1];
-                const T mix = (d0m - d0p) + (d2p - d2m);
-                T f;
-                if (scheme == LSS_ADI_HUNDSDORFER_VERWER) {
-                    f = ldg(v.S(SL_LA) + o) * y10;
-                    f += ldg(v.S(SL_S2SC) + o) * y11;
-                    f += ldg(v.S(SL_S2SE) + o) * y12;
-                    f += ldg(v.S(SL_S2MZ) + o) * mix;
-                    f += ldg(v.S(SL_X1) + o) * d0c;
-                    f += ldg(v.S(SL_X2) + o) * d1c;
-                    f += ldg(v.S(SL_X3) + o) * d2c;
-                    f += ldg(v.S(SL_X4) + o) * d1m;
-                    f += ldg(v.S(SL_X5) + o) * d1p;
-                } else {
-                    f = ldg(v.S(SL_LA) + o) * uc0;
-                    f += ldg(v.S(SL_S2SC) + o) * uc1;
-                    f += ldg(v.S(SL_S2SE) + o) * uc2;
-                    f += ldg(v.S(SL_S2IB) + o) * y11;
-                    f += ldg(v.S(SL_S2MZ) + o) * mix;
-                    if (scheme == LSS_ADI_MODIFIED_CRAIG_SNEYD) {
-                        f += ldg(v.S(SL_X1) + o) * d0c;
-                        f += ldg(v.S(SL_X2) + o) * d1c;
-                        f += ldg(v.S(SL_X3) + o) * d2c;
-                        f += ldg(v.S(SL_X4) + o) * d1m;
-                        f += ldg(v.S(SL_X5) + o) * d1p;
-                    }
-                }
-                y = f - ldg(v.S(SL_LA) + o) * y;
-                if (t == e) y -= ldg(v.Yv(Y_CHS) + j) * hi;
-                Y[o] = y;
-                uc0 = uc1; uc1 = uc2;
-                y10 = y11; y11 = y12;
-                d0m = d1m; d0c = d1c; d0p = d1p;
-                d1m = d2m; d1c = d2c; d1p = d2p;
-            }
-        }
-        T x = y;
+        T x = s_line_fwd<T, KIND>(v, scheme, U, Y1, Y2, Y, j, 1, e, lo, hi);
 #pragma unroll 4
         for (int t = e - 1; t >= 1; --t) {
             const long long o = (long long)t * ny + j;
@@ -337,6 +349,30 @@ __device__ __forceinline__ void s_stage(const inst_view<T> &v, int scheme, const
 }
 
 // v-line sweep: line i reads row i of `in` (t-1, t, t+1) and `inh` (t); tables are [t][i].
+// v_line_fwd: right-hand side and forward recurrence over t0..t1 from y = y_{t0-1}.
+template <typename T>
+__device__ __forceinline__ T v_line_fwd(const inst_view<T> &v, const T *__restrict__ in, const T *__restrict__ inh,
+                                        T *__restrict__ out, int i, int t0, int t1, T y, T hi)
+{
+    const int nx = v.nx, ny = v.ny, e = v.e_v;
+    const long long row = (long long)i * ny;
+    T a0 = in[row + t0 - 1], a1 = in[row + t0];
+#pragma unroll 4
+    for (int t = t0; t <= t1; ++t) {
+        const long long ot = (long long)t * nx + i;
+        const T a2 = in[row + t + 1];
+        T f = ldg(v.Vt(VL_LA) + ot) * a0;
+        f += ldg(v.Vt(VL_VC) + ot) * a1;
+        f += ldg(v.Vt(VL_VN) + ot) * a2;
+        f += ldg(v.Vt(VL_IB) + ot) * inh[row + t];
+        y = f - ldg(v.Vt(VL_LA) + ot) * y;
+        if (t == e) y -= ldg(v.X(X_CHV) + i) * hi;
+        out[row + t] = y;
+        a0 = a1; a1 = a2;
+    }
+    return y;
+}
+
 template <typename T>
 __device__ __forceinline__ void v_stage(const inst_view<T> &v, const T *__restrict__ in, const T *__restrict__ inh,
                                         const T *__restrict__ sb0, T *__restrict__ out, int l0, int ls)
@@ -347,22 +383,7 @@ __device__ __forceinline__ void v_stage(const inst_view<T> &v, const T *__restri
         const T lo = sb0[ii];
         const T hi = ldg(v.X(X_VHI) + ii);
         const long long row = (long long)i * ny;
-        T a0 = in[row], a1 = in[row + 1];
-        T y = lo;
-#pragma unroll 4
-        for (int t = 1; t <= e; ++t) {
-            const long long ot = (long long)t * nx + i;
-            const T a2 = in[row + t + 1];
-            T f = ldg(v.Vt(VL_LA) + ot) * a0;
-            f += ldg(v.Vt(VL_VC) + ot) * a1;
-            f += ldg(v.Vt(VL_VN) + ot) * a2;
-            f += ldg(v.Vt(VL_IB) + ot) * inh[row + t];
-            y = f - ldg(v.Vt(VL_LA) + ot) * y;
-            if (t == e) y -= ldg(v.X(X_CHV) + i) * hi;
-            out[row + t] = y;
-            a0 = a1; a1 = a2;
-        }
-        T x = y;
+        T x = v_line_fwd<T>(v, in, inh, out, i, 1, e, lo, hi);
 #pragma unroll 4
         for (int t = e - 1; t >= 1; --t) {
             x = out[row + t] - ldg(v.Vt(VL_G) + (long long)t * nx + i) * x;
@@ -618,6 +639,156 @@ template <typename T> __global__ void k_wide_b2(const __grid_constant__ bparams<
     const inst_view<T> v = make_view(p, d);
     b2_stage<T>(v, Vn, gtid(), gstride());
 }
+// Partitioned line solves of the wide path.  A large single instance has only Nx or Ny
+// lines per sweep -- a few warps per SM, far below what the FP64 pipe needs -- so each line
+// is cut into P chunks solved concurrently (block: 32 lines x P chunks).  Both recurrences
+// of the factorised solve are first order and linear:
+//   y_t = f_t - la_t y_{t-1}:  y_t = yhat_t + hf_t y_in,  hf_t = prod_{s=t0..t} (-la_s)
+//   x_t = y_t - g_t x_{t+1}:   x_t = xhat_t + hb_t x_in,  hb_t = prod_{s=t..t1} (-g_s)
+// where yhat / xhat are the chunk-local solutions from a zero start and hf / hb the
+// time-invariant chunk products (k_wide_spikes).  A chunk's incoming value is composed
+// from the other chunks' end values in shared memory.  Three passes over the chunk: local
+// forward solve; forward fix-up fused with the local back substitution; back fix-up.
+__device__ __forceinline__ void chunk_range(int e, int P, int c, int &t0, int &t1)
+{
+    t0 = 1 + static_cast<int>((static_cast<long long>(c) * e) / P);
+    t1 = static_cast<int>((static_cast<long long>(c + 1) * e) / P);
+}
+
+// hf / hb of every chunk of every line; lines along j ([t][j] tables, S) or i ([t][i], v)
+template <typename T>
+__global__ void k_wide_spikes(const T *__restrict__ la, const T *__restrict__ g, T *__restrict__ hf,
+                              T *__restrict__ hb, int lines, int stride, int e, int P)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= (lines - 2) * P) return;
+    const int l = 1 + q / P, c = q % P;
+    int t0, t1;
+    chunk_range(e, P, c, t0, t1);
+    T pr = T(1);
+    for (int t = t0; t <= t1; ++t) {
+        const long long o = (long long)t * stride + l;
+        pr *= -la[o];
+        hf[o] = pr;
+    }
+    pr = T(1);
+    for (int t = t1; t >= t0; --t) {
+        const long long o = (long long)t * stride + l;
+        pr *= -g[o];
+        hb[o] = pr;
+    }
+}
+
+template <typename T, int KIND>
+__global__ void __launch_bounds__(1024) k_wide_s_chunk(const __grid_constant__ bparams<T> p, const T *U, const T *Y1,
+                                                        const T *Y2, T *Y, const T *__restrict__ hf,
+                                                        const T *__restrict__ hb)
+{
+    __shared__ T sa[32][33], sb[32][33];
+    const bdesc d = p.desc[0];
+    const inst_view<T> v = make_view(p, d);
+    const int nx = d.nx, ny = d.ny, e = nx - 2, P = blockDim.y, c = threadIdx.y, lane = threadIdx.x;
+    const int j = 1 + blockIdx.x * 32 + lane;
+    const bool act = j <= ny - 2;
+    int t0, t1;
+    chunk_range(e, P, c, t0, t1);
+    T lo = T(0), hi = T(0);
+    if (act) {
+        const int jj = ldg(v.jmap() + j);
+        lo = U[jj];
+        hi = U[(long long)(nx - 1) * ny + jj];
+        sb[c][lane] = s_line_fwd<T, KIND>(v, d.scheme, U, Y1, Y2, Y, j, t0, t1, c == 0 ? lo : T(0), hi);
+        sa[c][lane] = hf[(long long)t1 * ny + j];
+    }
+    __syncthreads();
+    T xh = T(0);
+    if (act) {
+        T yin = T(0);
+        if (c > 0) {
+            yin = sb[0][lane];
+            for (int q = 1; q < c; ++q) yin = sb[q][lane] + sa[q][lane] * yin;
+        }
+        for (int t = t1; t >= t0; --t) {
+            const long long o = (long long)t * ny + j;
+            const T y = (c > 0) ? Y[o] + hf[o] * yin : Y[o];
+            xh = y - ldg(v.S(SL_G) + o) * xh;
+            Y[o] = xh;
+        }
+    }
+    __syncthreads();
+    if (act) {
+        sb[c][lane] = xh;
+        sa[c][lane] = hb[(long long)t0 * ny + j];
+    }
+    __syncthreads();
+    if (act) {
+        if (c < P - 1) {
+            T xin = sb[P - 1][lane];
+            for (int q = P - 2; q > c; --q) xin = sb[q][lane] + sa[q][lane] * xin;
+            for (int t = t0; t <= t1; ++t) {
+                const long long o = (long long)t * ny + j;
+                Y[o] += hb[o] * xin;
+            }
+        }
+        if (c == 0) Y[j] = lo;
+        if (c == P - 1) Y[(long long)(nx - 1) * ny + j] = hi;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(1024) k_wide_v_chunk(const __grid_constant__ bparams<T> p, const T *in, const T *inh,
+                                                        const T *b0, T *out, const T *__restrict__ hf,
+                                                        const T *__restrict__ hb)
+{
+    __shared__ T sa[32][33], sb[32][33];
+    const bdesc d = p.desc[0];
+    const inst_view<T> v = make_view(p, d);
+    const int nx = d.nx, ny = d.ny, e = ny - 2, P = blockDim.y, c = threadIdx.y, lane = threadIdx.x;
+    const int i = 1 + blockIdx.x * 32 + lane;
+    const bool act = i <= nx - 2;
+    const long long row = (long long)i * ny;
+    int t0, t1;
+    chunk_range(e, P, c, t0, t1);
+    T lo = T(0), hi = T(0);
+    if (act) {
+        const int ii = ldg(v.imap() + i);
+        lo = b0[ii];
+        hi = ldg(v.X(X_VHI) + ii);
+        sb[c][lane] = v_line_fwd<T>(v, in, inh, out, i, t0, t1, c == 0 ? lo : T(0), hi);
+        sa[c][lane] = hf[(long long)t1 * nx + i];
+    }
+    __syncthreads();
+    T xh = T(0);
+    if (act) {
+        T yin = T(0);
+        if (c > 0) {
+            yin = sb[0][lane];
+            for (int q = 1; q < c; ++q) yin = sb[q][lane] + sa[q][lane] * yin;
+        }
+        for (int t = t1; t >= t0; --t) {
+            const long long ot = (long long)t * nx + i;
+            const T y = (c > 0) ? out[row + t] + hf[ot] * yin : out[row + t];
+            xh = y - ldg(v.Vt(VL_G) + ot) * xh;
+            out[row + t] = xh;
+        }
+    }
+    __syncthreads();
+    if (act) {
+        sb[c][lane] = xh;
+        sa[c][lane] = hb[(long long)t0 * nx + i];
+    }
+    __syncthreads();
+    if (act) {
+        if (c < P - 1) {
+            T xin = sb[P - 1][lane];
+            for (int q = P - 2; q > c; --q) xin = sb[q][lane] + sa[q][lane] * xin;
+            for (int t = t0; t <= t1; ++t) out[row + t] += hb[(long long)t * nx + i] * xin;
+        }
+        if (c == 0) out[row] = lo;
+        if (c == P - 1) out[row + ny - 1] = hi;
+    }
+}
+
 // value, finiteness flag and final-array flag of the single instance
 template <typename T> __global__ void k_wide_finish(const __grid_constant__ bparams<T> p, const T *U)
 {
@@ -660,8 +831,8 @@ template <typename T> struct batch_typed {
     bool adjoint_ok = false;      // FP64 Heston DR/CS/MCS only
     std::string adjoint_why;
     int ck_override = 0;          // checkpoint interval (0 = ceil(sqrt(steps)))
-    int grid_adj = 0;
-    long long ws_stride = 0;
+    int grid_adj = 0;                 // CTAs the workspace has slices for
+    long long ws_stride = 0, ws_need = 0;
     dbuf<double> d_grads, d_ws;
     int sms = 0;
     cudaGraphExec_t graph = nullptr;
@@ -703,6 +874,7 @@ template <typename T> struct batch_typed {
 
     int create(const lss_adi_problem *ps, int n);
     int prepare_adjoint(cudaStream_t s);
+    int ensure_ws(int bs);
     // threads per instance (CTA size) of the persistent kernels, per mode; chosen by autotune()
     int bs_mode[2] = {64, 64};
     template <int BS> int launch_forward(cudaStream_t s);
@@ -711,6 +883,12 @@ template <typename T> struct batch_typed {
     // wide path (count == 1)
     dbuf<T> d_b0;
     cudaGraphExec_t wide_graph = nullptr;
+    int wide_ps = 1, wide_pv = 1;   // chunks per S line / per v line (1: thread per line)
+    dbuf<T> d_spk;                  // chunk products: S hf, S hb, v hf, v hb (n each)
+    int set_wide_chunks(int ps, int pv, cudaStream_t s);
+    int autotune_wide(cudaStream_t s);
+    template <int KIND> void launch_wide_s(cudaStream_t s, const bparams<T> &p, const T *U, const T *Y1, const T *Y2, T *Y);
+    void launch_wide_v(cudaStream_t s, const bparams<T> &p, const T *in, const T *inh, const T *b0, T *out);
     int enqueue_wide(cudaStream_t s);
     int run_wide(cudaStream_t s, bool use_graph);
     int enqueue(int mode, cudaStream_t s);
@@ -935,14 +1113,31 @@ template <typename T> int batch_typed<T>::prepare_adjoint(cudaStream_t s)
         const long long nseg = (d.steps + c - 1) / c;
         need = std::max(need, (nseg + 4LL * (c + 1) + 2 + 7) * nn + d.nx + 2LL * d.ny);
     }
-    // workspace for the largest resident grid over the CTA sizes (64 threads: most CTAs)
+    ws_need = (need + 31) / 32 * 32;
+    return ensure_ws(bs_mode[1]);
+}
+
+// Adjoint workspace for every resident CTA of k_batch_fwdadj<bs> (one slice per CTA).
+template <typename T> int batch_typed<T>::ensure_ws(int bs)
+{
     int per_sm = 0;
-    LSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_fwdadj<64>, 64, 0), "occupancy");
+    switch (bs) {
+    case 32: LSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_fwdadj<32>, 32, 0), "occupancy"); break;
+    case 128: LSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_fwdadj<128>, 128, 0), "occupancy"); break;
+    case 256: LSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_fwdadj<256>, 256, 0), "occupancy"); break;
+    default: LSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_fwdadj<64>, 64, 0), "occupancy"); break;
+    }
     const int want = std::max(1, std::min(sms * std::max(1, per_sm), count));
-    if (d_ws.p && ws_stride >= need && grid_adj == want) return LSS_ADI_OK;
-    ws_stride = (need + 31) / 32 * 32;
-    grid_adj = want;
+    if (d_ws.p && ws_stride == ws_need && grid_adj >= want) return LSS_ADI_OK;
+    const int slices = (d_ws.p && ws_stride == ws_need) ? std::max(want, grid_adj) : want;
+    ws_stride = ws_need;
+    grid_adj = slices;
     LSS_CUDA_TRY(d_ws.alloc(static_cast<size_t>(ws_stride) * grid_adj), "batch: allocating adjoint workspace");
+    if (graph) { // a captured launch holds the old workspace pointer
+        cudaGraphExecDestroy(graph);
+        graph = nullptr;
+        graph_mode = -1;
+    }
     return LSS_ADI_OK;
 }
 
@@ -977,19 +1172,22 @@ template <typename T> int batch_typed<T>::enqueue(int mode, cudaStream_t s)
     const int bs = bs_mode[mode == 1 ? 1 : 0];
     if (mode == 1) {
         LSS_CUDA_TRY(cudaMemsetAsync(d_counter.p, 0, sizeof(int), s), "batch: counter reset");
-        rc = bs == 256 ? launch_fwdadj<256>(s) : bs == 128 ? launch_fwdadj<128>(s) : launch_fwdadj<64>(s);
+        rc = bs == 256 ? launch_fwdadj<256>(s) : bs == 128 ? launch_fwdadj<128>(s)
+                                               : bs == 32 ? launch_fwdadj<32>(s) : launch_fwdadj<64>(s);
     } else {
         LSS_CUDA_TRY(cudaMemcpyAsync(state.p, d_payoff.p, total_n * sizeof(T), cudaMemcpyDeviceToDevice, s),
                      "batch: initial state");
         LSS_CUDA_TRY(cudaMemsetAsync(d_counter.p, 0, sizeof(int), s), "batch: counter reset");
-        rc = bs == 256 ? launch_forward<256>(s) : bs == 128 ? launch_forward<128>(s) : launch_forward<64>(s);
+        rc = bs == 256 ? launch_forward<256>(s) : bs == 128 ? launch_forward<128>(s)
+                                                : bs == 32 ? launch_forward<32>(s) : launch_forward<64>(s);
     }
     launches = 1;
     return rc;
 }
 
-// Times one run per CTA size (64, 128, 256 threads per instance) and keeps the fastest for
-// `mode`; with *chosen > 0 on entry, sets that size without timing.
+// Times one run per CTA size (32, 64, 128, 256 threads per instance) and keeps the fastest
+// for `mode`; with *chosen > 0 on entry, sets that size without timing.  One warp per
+// instance trades longer instances for no cross-warp barriers and twice the resident CTAs.
 template <typename T> int batch_typed<T>::autotune(int mode, int *chosen, cudaStream_t s)
 {
     const int m = mode == 1 ? 1 : 0;
@@ -998,11 +1196,15 @@ template <typename T> int batch_typed<T>::autotune(int mode, int *chosen, cudaSt
         if (rc) return rc;
     }
     if (chosen && *chosen > 0) {
-        if (*chosen != 64 && *chosen != 128 && *chosen != 256)
-            return set_error(LSS_ADI_EINVAL, "autotune: threads per instance must be 64, 128 or 256");
+        if (*chosen != 32 && *chosen != 64 && *chosen != 128 && *chosen != 256)
+            return set_error(LSS_ADI_EINVAL, "autotune: threads per instance must be 32, 64, 128 or 256");
         bs_mode[m] = *chosen;
+        if (mode == 1) {
+            int rc = ensure_ws(*chosen);
+            if (rc) return rc;
+        }
     } else {
-        const int cand[3] = {64, 128, 256};
+        const int cand[4] = {32, 64, 128, 256};
         float best = 1e30f;
         int best_bs = bs_mode[m];
         cudaEvent_t e0, e1;
@@ -1010,6 +1212,14 @@ template <typename T> int batch_typed<T>::autotune(int mode, int *chosen, cudaSt
         LSS_CUDA_TRY(cudaEventCreate(&e1), "autotune: event");
         for (int c : cand) {
             bs_mode[m] = c;
+            if (mode == 1) {
+                int rc = ensure_ws(c);
+                if (rc) {
+                    cudaEventDestroy(e0);
+                    cudaEventDestroy(e1);
+                    return rc;
+                }
+            }
             cudaEventRecord(e0, s);
             int rc = enqueue(mode, s);
             cudaEventRecord(e1, s);
@@ -1039,30 +1249,124 @@ template <typename T> int batch_typed<T>::autotune(int mode, int *chosen, cudaSt
     return LSS_ADI_OK;
 }
 
+// S and v sweeps of the wide path: thread per line (P = 1, bit-identical to the batched
+// kernel) or the partitioned solve with the autotuned chunk counts.
+template <typename T>
+template <int KIND>
+void batch_typed<T>::launch_wide_s(cudaStream_t s, const bparams<T> &p, const T *U, const T *Y1, const T *Y2, T *Y)
+{
+    const bdesc &d = desc[0];
+    if (wide_ps <= 1) {
+        k_wide_s<T, KIND><<<grid_for(d.ny - 2, 32), 32, 0, s>>>(p, U, Y1, Y2, Y);
+    } else {
+        const long long n = total_n;
+        k_wide_s_chunk<T, KIND><<<grid_for(d.ny - 2, 32), dim3(32, wide_ps), 0, s>>>(p, U, Y1, Y2, Y, d_spk.p, d_spk.p + n);
+    }
+}
+
+template <typename T>
+void batch_typed<T>::launch_wide_v(cudaStream_t s, const bparams<T> &p, const T *in, const T *inh, const T *b0, T *out)
+{
+    const bdesc &d = desc[0];
+    if (wide_pv <= 1) {
+        k_wide_v<T><<<grid_for(d.nx - 2, 32), 32, 0, s>>>(p, in, inh, b0, out);
+    } else {
+        const long long n = total_n;
+        k_wide_v_chunk<T><<<grid_for(d.nx - 2, 32), dim3(32, wide_pv), 0, s>>>(p, in, inh, b0, out, d_spk.p + 2 * n,
+                                                                               d_spk.p + 3 * n);
+    }
+}
+
+template <typename T> int batch_typed<T>::set_wide_chunks(int ps, int pv, cudaStream_t s)
+{
+    const bdesc &d = desc[0];
+    const long long n = total_n;
+    auto ok = [](int P, int e) { return P >= 1 && P <= 32 && (P == 1 || e >= 4 * P); };
+    if (!ok(ps, d.nx - 2) || !ok(pv, d.ny - 2)) return set_error(LSS_ADI_EINVAL, "wide: chunk count out of range");
+    if ((ps > 1 || pv > 1) && !d_spk.p) LSS_CUDA_TRY(d_spk.alloc(4 * n), "wide: allocating chunk products");
+    const bparams<T> p = params();
+    if (ps > 1)
+        k_wide_spikes<T><<<grid_for((d.ny - 2) * ps, 128), 128, 0, s>>>(p.S[SL_LA], p.S[SL_G], d_spk.p, d_spk.p + n, d.ny,
+                                                                         d.ny, d.nx - 2, ps);
+    if (pv > 1)
+        k_wide_spikes<T><<<grid_for((d.nx - 2) * pv, 128), 128, 0, s>>>(p.Vt[VL_LA], p.Vt[VL_G], d_spk.p + 2 * n,
+                                                                         d_spk.p + 3 * n, d.nx, d.nx, d.ny - 2, pv);
+    LSS_CUDA_TRY(cudaGetLastError(), "wide: chunk products");
+    wide_ps = ps;
+    wide_pv = pv;
+    if (wide_graph) cudaGraphExecDestroy(wide_graph);
+    wide_graph = nullptr;
+    return LSS_ADI_OK;
+}
+
+// Chunk counts of the two sweeps, each timed on its own (first S stage, first v stage) over
+// P = 1, 2, 4, ..., 32 with at least 4 rows per chunk.
+template <typename T> int batch_typed<T>::autotune_wide(cudaStream_t s)
+{
+    const bdesc &d = desc[0];
+    bparams<T> p = params();
+    LSS_CUDA_TRY(cudaMemcpyAsync(p.U, d_payoff.p, total_n * sizeof(T), cudaMemcpyDeviceToDevice, s), "wide: tuning state");
+    cudaEvent_t e0, e1;
+    LSS_CUDA_TRY(cudaEventCreate(&e0), "wide: tuning events");
+    LSS_CUDA_TRY(cudaEventCreate(&e1), "wide: tuning events");
+    float best_s = 1e30f, best_v = 1e30f;
+    int ps = 1, pv = 1;
+    int rc = LSS_ADI_OK;
+    for (int P = 1; P <= 32 && rc == LSS_ADI_OK; P *= 2) {
+        const bool okS = (P == 1 || d.nx - 2 >= 4 * P), okV = (P == 1 || d.ny - 2 >= 4 * P);
+        if (!okS && !okV) break;
+        rc = set_wide_chunks(okS ? P : 1, okV ? P : 1, s);
+        if (rc) break;
+        float ms = 0.f;
+        if (okS) {
+            launch_wide_s<1>(s, p, p.U, nullptr, nullptr, p.Y1);
+            cudaEventRecord(e0, s);
+            for (int r = 0; r < 3; ++r) launch_wide_s<1>(s, p, p.U, nullptr, nullptr, p.Y1);
+            cudaEventRecord(e1, s);
+            cudaEventSynchronize(e1);
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms < best_s) { best_s = ms; ps = P; }
+        }
+        if (okV) {
+            k_wide_b1<T><<<grid_for(d.nx, 128), 128, 0, s>>>(p, p.U, d_b0.p);
+            launch_wide_v(s, p, p.U, p.Y1, d_b0.p, p.Y2);
+            cudaEventRecord(e0, s);
+            for (int r = 0; r < 3; ++r) launch_wide_v(s, p, p.U, p.Y1, d_b0.p, p.Y2);
+            cudaEventRecord(e1, s);
+            cudaEventSynchronize(e1);
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms < best_v) { best_v = ms; pv = P; }
+        }
+        const cudaError_t err = cudaGetLastError();
+        if (err != cudaSuccess) rc = set_error(LSS_ADI_ECUDA, std::string("wide: tuning: ") + cudaGetErrorString(err));
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    return set_wide_chunks(ps, pv, s);
+}
+
 template <typename T> int batch_typed<T>::enqueue_wide(cudaStream_t s)
 {
     const bdesc &d = desc[0];
     bparams<T> p = params();
     T *U = p.U, *V = p.V, *Y1 = p.Y1, *Y2 = p.Y2, *Y3 = p.Y3, *b0 = d_b0.p;
     LSS_CUDA_TRY(cudaMemcpyAsync(U, d_payoff.p, total_n * sizeof(T), cudaMemcpyDeviceToDevice, s), "wide: initial state");
-    // small blocks spread the few hundred to few thousand lines over as many SMs as possible
-    const int bs = 32;
-    const int gS = grid_for(d.ny - 2, bs), gV = grid_for(d.nx - 2, bs);
     const int gX = grid_for(d.nx, 128), gY = grid_for(d.ny, 128);
     long long nl = 0;
     for (int step = 0; step < d.steps; ++step) {
         k_wide_b1<T><<<gX, 128, 0, s>>>(p, U, b0);
-        k_wide_s<T, 1><<<gS, bs, 0, s>>>(p, U, nullptr, nullptr, Y1);
+        launch_wide_s<1>(s, p, U, nullptr, nullptr, Y1);
         if (d.scheme == LSS_ADI_DOUGLAS_RACHFORD) {
-            k_wide_v<T><<<gV, bs, 0, s>>>(p, U, Y1, b0, V);
+            launch_wide_v(s, p, U, Y1, b0, V);
             nl += 3;
         } else {
-            k_wide_v<T><<<gV, bs, 0, s>>>(p, U, Y1, b0, Y2);
-            k_wide_s<T, 2><<<gS, bs, 0, s>>>(p, U, Y1, Y2, Y3);
+            launch_wide_v(s, p, U, Y1, b0, Y2);
+            launch_wide_s<2>(s, p, U, Y1, Y2, Y3);
             if (d.scheme == LSS_ADI_HUNDSDORFER_VERWER)
-                k_wide_v<T><<<gV, bs, 0, s>>>(p, Y2, Y3, b0, V);
+                launch_wide_v(s, p, Y2, Y3, b0, V);
             else
-                k_wide_v<T><<<gV, bs, 0, s>>>(p, U, Y3, b0, V);
+                launch_wide_v(s, p, U, Y3, b0, V);
             nl += 5;
         }
         k_wide_b2<T><<<gY, 128, 0, s>>>(p, V);
@@ -1136,7 +1440,15 @@ template <typename T> struct wide_solver : wide_solver_base {
         x = tt.x;
         y = tt.y;
         pay0 = tt.payoff;
-        return b.create(&p, 1);
+        int rc = b.create(&p, 1);
+        if (rc) return rc;
+        if (p.options & LSS_ADI_OPT_LINE_PER_THREAD) return LSS_ADI_OK;
+        LSS_CUDA_TRY(cudaMemcpy(b.d_payoff.p, pay0.data(), pay0.size() * sizeof(T), cudaMemcpyHostToDevice),
+                     "wide: initial state");
+        rc = b.autotune_wide(nullptr);
+        if (rc) return rc;
+        LSS_CUDA_TRY(cudaDeviceSynchronize(), "wide: tuning");
+        return LSS_ADI_OK;
     }
     int forward(const void *payoff, void *out_surface, double *out_value, int flags, void *stream, bool use_graph) override
     {
@@ -1163,6 +1475,24 @@ template <typename T> struct wide_solver : wide_solver_base {
     {
         std::copy(x.begin(), x.end(), static_cast<T *>(gx));
         std::copy(y.begin(), y.end(), static_cast<T *>(gy));
+        return LSS_ADI_OK;
+    }
+    int chunks(int s_chunks, int v_chunks, int *out_s, int *out_v, void *stream) override
+    {
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        if (s_chunks < 0 || v_chunks < 0) return set_error(LSS_ADI_EINVAL, "lss_adi_line_chunks: negative chunk count");
+        int rc = LSS_ADI_OK;
+        if (s_chunks == 0 || v_chunks == 0) {
+            LSS_CUDA_TRY(cudaMemcpyAsync(b.d_payoff.p, pay0.data(), pay0.size() * sizeof(T), cudaMemcpyHostToDevice, s),
+                         "wide: initial state");
+            rc = b.autotune_wide(s);
+            if (rc) return rc;
+        }
+        rc = b.set_wide_chunks(s_chunks ? s_chunks : b.wide_ps, v_chunks ? v_chunks : b.wide_pv, s);
+        if (rc) return rc;
+        LSS_CUDA_TRY(cudaStreamSynchronize(s), "lss_adi_line_chunks");
+        if (out_s) *out_s = b.wide_ps;
+        if (out_v) *out_v = b.wide_pv;
         return LSS_ADI_OK;
     }
 };

@@ -30,6 +30,7 @@ struct wide_solver_base {
     virtual int forward(const void *payoff, void *out_surface, double *out_value, int flags, void *stream,
                         bool use_graph) = 0;
     virtual int grid(void *x, void *y) const = 0;
+    virtual int chunks(int s_chunks, int v_chunks, int *out_s, int *out_v, void *stream) = 0;
 };
 int make_wide_solver(const lss_adi_problem &p, std::unique_ptr<wide_solver_base> &out);
 

@@ -47,6 +47,7 @@ class HestonProblem:
     eval_v: float = 0.04
     fp64_tables: bool = False  # FP32 only: tables and index_of remaps built in double
     solver: str = "tlu"  # tridiagonal_method_enum: "tlu" ThomasLUSolver | "ds" DoubleSweepSolver
+    line_per_thread: bool = False  # fast single instance: no partitioned line solves (batched-kernel bits)
 
     @property
     def steps(self) -> int:
@@ -68,7 +69,8 @@ class HestonProblem:
         c.arith = L.ARITH_REFERENCE if arith == "reference" else L.ARITH_FAST
         if self.solver not in ("tlu", "ds"):
             raise ValueError(f"solver must be 'tlu' or 'ds', not {self.solver!r}")
-        c.options = (L.OPT_FP64_TABLES if self.fp64_tables else 0) | (L.OPT_DOUBLE_SWEEP if self.solver == "ds" else 0)
+        c.options = ((L.OPT_FP64_TABLES if self.fp64_tables else 0) | (L.OPT_DOUBLE_SWEEP if self.solver == "ds" else 0)
+                     | (L.OPT_LINE_PER_THREAD if self.line_per_thread else 0))
         return c
 
 
@@ -99,6 +101,13 @@ class ImplicitHestonSolver:
             self.close()
         except Exception:
             pass
+
+    def line_chunks(self, s_chunks: int = 0, v_chunks: int = 0, stream: int = 0):
+        """Chunks per S line / v line of the partitioned solves (0 = autotune); returns those in use."""
+        a, b = ctypes.c_int(), ctypes.c_int()
+        L.check(self.lib.lss_adi_line_chunks(self._h, int(s_chunks), int(v_chunks), ctypes.byref(a), ctypes.byref(b),
+                                             ctypes.c_void_p(stream)))
+        return a.value, b.value
 
     def grid(self):
         x = np.empty(self.problem.nx, dtype=self.dtype)

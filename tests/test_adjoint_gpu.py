@@ -36,7 +36,7 @@ def device_value(lss, p):
 
 
 def oracle_value(oracle, lss, p):
-    kw = {k: v for k, v in dataclasses.asdict(p).items() if k not in ("eval_s", "eval_v", "fp64_tables")}
+    kw = {k: v for k, v in dataclasses.asdict(p).items() if k not in ("eval_s", "eval_v", "fp64_tables", "line_per_thread")}
     op = oracle.Problem(**kw)
     surf = oracle.solve(op, "f64")
     x, y = oracle.grid(op, "f64")

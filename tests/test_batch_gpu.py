@@ -1,4 +1,6 @@
 """GPU parity of the batched persistent kernel (lss_adi_batch_*) against the CPU oracle."""
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -27,7 +29,7 @@ def oracle_of(oracle, p):
     import dataclasses
 
     return oracle.Problem(**{k: v for k, v in dataclasses.asdict(p).items()
-                             if k not in ("eval_s", "eval_v", "fp64_tables")})
+                             if k not in ("eval_s", "eval_v", "fp64_tables", "line_per_thread")})
 
 
 @pytest.mark.parametrize("graph", [False, True])
@@ -92,6 +94,7 @@ def test_wide_single_instance_path_is_bitwise_the_batched_kernel(lss):
     b.run(0)
     values, _, _ = b.results()
     for k, p in enumerate(probs):
+        p.line_per_thread = True
         got, v = lss.ImplicitHestonSolver(p, precision="f64", arith="fast").solve()
         assert np.array_equal(got, b.surface(k), equal_nan=True)
         assert v == values[k] or (np.isnan(v) and np.isnan(values[k]))
@@ -112,6 +115,43 @@ def test_wide_path_large_grid(lss, oracle, fp):
         assert ok, (e_dev, e_ref)
 
 
+@pytest.mark.parametrize("scheme", ["dr", "cs", "mcs", "hv"])
+@pytest.mark.parametrize("chunks", [(2, 3), (8, 4), (32, 16), (5, 32)])
+def test_partitioned_line_solves_match_line_per_thread(lss, oracle, scheme, chunks):
+    """Chunked S and v line solves (chunk products hf / hb and composed carries) against the
+    thread-per-line solve of the same instance: rounding-level agreement, and the oracle bound."""
+    kw = dict(model="heston", kappa=2.0, theta_v=0.05, sigma=0.4, rho=-0.3, rate=0.02, strike=100.0, maturity=0.5,
+              s_lo=0.0, s_hi=200.0, v_lo=0.0, v_hi=1.2, nx=203, ny=131, nt=9, scheme=scheme, zeta=1.0 / 3.0,
+              acc_point=100.0, **NU)
+    p = lss.HestonProblem(**kw)
+    s = lss.ImplicitHestonSolver(p, precision="f64", arith="fast")
+    assert s.line_chunks(*chunks) == chunks
+    got, val = s.solve(graph=True)
+    ref, rval = lss.ImplicitHestonSolver(dataclasses.replace(p, line_per_thread=True), precision="f64",
+                                         arith="fast").solve()
+    assert rel_err(got, ref) < 1e-13
+    assert abs(val - rval) <= 1e-13 * max(1.0, abs(rval))
+    want = oracle.solve(oracle_of(oracle, p), "f64")
+    assert rel_err(got, want) < fp64_tol(want, p.s_hi)
+
+
+def test_partition_autotuner_and_limits(lss):
+    p = lss.HestonProblem(scheme="hv", nx=300, ny=140, nt=5, nonuniform=True, acc_point=100.0, alpha_scale=10.0,
+                          beta_scale=24.0)
+    s = lss.ImplicitHestonSolver(p, precision="f64", arith="fast")
+    ps, pv = s.line_chunks(0, 0)
+    assert 1 <= ps <= 32 and 1 <= pv <= 32
+    from linear_system_solvers_gb300 import _lib as L
+
+    with pytest.raises(L.LssError):
+        s.line_chunks(64, 1)  # more than 32 chunks
+    with pytest.raises(L.LssError):
+        s.line_chunks(1, 32)  # 138 rows: fewer than 4 per chunk
+    ref = lss.ImplicitHestonSolver(p, precision="f64", arith="reference")
+    with pytest.raises(L.LssError):
+        ref.line_chunks(2, 2)
+
+
 @pytest.mark.parametrize("mode", [0, 1])
 def test_cta_size_does_not_change_bits(lss, mode):
     """Each line is solved by one thread whatever the CTA size, so every size the autotuner
@@ -124,7 +164,7 @@ def test_cta_size_does_not_change_bits(lss, mode):
         p.nt = 15
     b = lss.BatchSolver(probs, precision="f64")
     ref = None
-    for threads in (64, 128, 256):
+    for threads in (32, 64, 128, 256):
         assert b.autotune(mode=mode, threads=threads) == threads
         b.run(mode)
         v, g, _ = b.results()
@@ -135,4 +175,4 @@ def test_cta_size_does_not_change_bits(lss, mode):
             assert np.array_equal(v, ref[0])
             np.testing.assert_allclose(g, ref[1], rtol=1e-11, atol=1e-14)
             assert all(np.array_equal(a, c) for a, c in zip(surf, ref[2]))
-    assert b.autotune(mode=mode) in (64, 128, 256)
+    assert b.autotune(mode=mode) in (32, 64, 128, 256)
