@@ -302,10 +302,9 @@ template <typename T, bool X>
 __global__ void k_refresh(time_tables<T> tt, int nx, int ny, double da, double dc)
 {
     using R = ar<X>;
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = blockIdx.y;
-    if (j >= ny) return;
-    const size_t o = static_cast<size_t>(i) * ny + j;
+    const size_t o = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (o >= static_cast<size_t>(nx) * ny) return;
+    const int i = static_cast<int>(o / ny), j = static_cast<int>(o % ny);
     const T aval = tt.per_i[i], aa = tt.per_i[nx + i], aaa = tt.per_i[2 * nx + i];
     const T gc = tt.per_i[3 * nx + i], ud = tt.per_i[4 * nx + i];
     const T A = static_cast<T>(__dmul_rn(tt.a_static[o], da));
@@ -415,10 +414,10 @@ template <typename T> template <bool X> void plain_solver<T>::enqueue_steps(cuda
         tt.two_alpha = tab_.two_alpha;
         tt.half_rho_f = tab_.half_rho_f;
     }
-    const dim3 gref(grid_for(ny, 128), nx);
+    const int gref = grid_for(static_cast<long long>(nx) * ny, 256);
     for (int step = 0; step < tab_.steps; ++step) {
         if (tab_.tdep) {
-            k_refresh<T, X><<<gref, 128, 0, s>>>(tt, nx, ny, tab_.step_da[step], tab_.step_dc[step]);
+            k_refresh<T, X><<<gref, 256, 0, s>>>(tt, nx, ny, tab_.step_da[step], tab_.step_dc[step]);
             launches_ += 1;
         }
         k_boundary1<T, X><<<grid_for(nx, 128), 128, 0, s>>>(d_, U, bcol0, bcolN);
