@@ -13,7 +13,8 @@
 // derivative, neighbouring lines) by a gather pass over columns.  Parameter
 // sensitivities dV/d(kappa, theta, sigma, rho, r) use, per stage and grid point,
 //   mu_t * (d f_t/dp - d a_t/dp x_{t-1} - d b_t/dp x_t - d c_t/dp x_{t+1}),  mu_t = w_t / beta_t,
-// with the Heston coefficient derivatives (all separable into 1-D tables).
+// with the coefficient derivatives of the model (Heston, or SABR at r = 0 whose D(t) terms add
+// a per-step factor tau = T - t), all separable into 1-D tables.
 #pragma once
 // Included by adi_batched.cu inside namespace lss_gb300, after the forward stage functions.
 
@@ -104,9 +105,10 @@ __device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d
                                       const double *__restrict__ Yo, const double *__restrict__ XB,
                                       double *__restrict__ FB, double *__restrict__ TMP, double *__restrict__ LS,
                                       double *__restrict__ HS, double *__restrict__ UB, double *__restrict__ Y1B,
-                                      adj_acc &acc, int l0, int ls)
+                                      adj_acc &acc, double tau, int l0, int ls)
 {
     const int nx = v.nx, ny = v.ny, e = nx - 2;
+    const bool sabr = d.model == LSS_ADI_SABR;
     const double th = d.a_theta;
     const double zt = (d.scheme == LSS_ADI_MODIFIED_CRAIG_SNEYD) ? (d.a_zeta - th) : 0.0;
     for (int j = 1 + l0; j <= ny - 2; j += ls) {
@@ -120,7 +122,7 @@ __device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d
         }
         double w = 0.0, la_next = 0.0, w_e = 0.0;
         double acc_t1 = 0.0, acc_t = 0.0;
-        double pA = 0.0, pB = 0.0, pQ = 0.0, pD = 0.0, pE = 0.0;
+        double pA = 0.0, pB = 0.0, pQ = 0.0, pD = 0.0, pE = 0.0, pAa = 0.0, pDd = 0.0;
 #pragma unroll 2
         for (int t = e; t >= 1; --t) {
             const long long o = (long long)t * ny + j;
@@ -178,7 +180,11 @@ __device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d
                 pQ += mu * (sPt - sMt);
                 pD += mu * (sMt + sPt + 2.0 * sW);
             }
-            pE += mu * hx * sC;
+            pE += mu * __ldg(v.X(X_HC) + t) * sC;
+            if (sabr) {
+                pAa += mu * __ldg(v.X(X_HA) + t) * (sM + sP + 2.0 * sZ);
+                pDd += mu * __ldg(v.X(X_HDD) + t) * (sP - sM);
+            }
             la_next = la;
         }
         if constexpr (KIND == 2) {
@@ -190,6 +196,9 @@ __device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d
         const double ek = __ldg(v.Yv(Y_EK) + j), et = __ldg(v.Yv(Y_ET) + j), es = __ldg(v.Yv(Y_ES) + j);
         const double bs = __ldg(v.Yv(Y_BS) + j), hy = __ldg(v.Yv(Y_HY) + j);
         acc.s[0] += d.a_delta * pA + d.a_halfk * pB;
+        if (sabr) // D(t) terms of a^, d^ and c^
+            acc.s[0] += tau * d.a_omb *
+                        (__ldg(v.Yv(Y_HV2) + j) * (2.0 * d.a_delta * pDd - 2.0 * d.a_alphat * pAa) - d.a_rho * d.a_sigma * hy * pE);
         acc.s[1] += d.a_ni * ek * pQ;
         acc.s[2] += d.a_ni * et * pQ;
         acc.s[3] += d.a_ni * es * pQ + d.a_betat * bs * pD + d.a_rho * hy * pE;
@@ -204,8 +213,8 @@ template <int KIND>
 __device__ __forceinline__ void adj_gather(const inst_view<double> &v, const bdesc &d, const double *__restrict__ U,
                                            const double *__restrict__ FB, const double *__restrict__ LS,
                                            const double *__restrict__ HS, const double *__restrict__ LV,
-                                           double *__restrict__ UB, double *__restrict__ Y2B, adj_acc &acc, int l0,
-                                           int ls)
+                                           double *__restrict__ UB, double *__restrict__ Y2B, adj_acc &acc, double tau,
+                                           int l0, int ls)
 {
     const int nx = v.nx, ny = v.ny;
     auto F = [&](int p, int q) -> double {
@@ -253,7 +262,10 @@ __device__ __forceinline__ void adj_gather(const inst_view<double> &v, const bde
                                 const double u0 = U[o], u1 = U[o + 1], u2 = U[o + 2];
                                 const double um = U[o - ny], up = U[o + ny];
                                 const double ee = d.a_ni * bb * (4.0 * u1 - 3.0 * u0 - u2);
-                                acc.s[0] += bb * (d.a_delta * __ldg(v.X(X_HX) + p) * (up - um) - d.a_k * u0);
+                                double hd = __ldg(v.X(X_HX) + p);
+                                if (d.model == LSS_ADI_SABR)
+                                    hd += 2.0 * d.a_omb * tau * __ldg(v.Yv(Y_HV2)) * __ldg(v.X(X_HDD) + p);
+                                acc.s[0] += bb * (d.a_delta * hd * (up - um) - d.a_k * u0);
                                 acc.s[1] += ee * __ldg(v.Yv(Y_EK));
                                 acc.s[2] += ee * __ldg(v.Yv(Y_ET));
                                 acc.s[3] += ee * __ldg(v.Yv(Y_ES));
@@ -279,7 +291,7 @@ template <int BS>
 __device__ __forceinline__ void adj_step(const inst_view<double> &v, const bdesc &d, const double *U, const double *Y1,
                                          const double *Y2, const double *Y3, const double *Vo, double *VB, double *UB,
                                          double *Y1B, double *Y2B, double *Y3B, double *FB, double *TMP, double *LV,
-                                         double *LS, double *HS, adj_acc &acc)
+                                         double *LS, double *HS, adj_acc &acc, double tau)
 {
     const int l0 = threadIdx.x;
     adj_b2(v, VB, UB, l0, BS);
@@ -290,16 +302,16 @@ __device__ __forceinline__ void adj_step(const inst_view<double> &v, const bdesc
     } else {
         adj_v<true>(v, U, Vo, VB, UB, Y3B, TMP, LV, acc, l0, BS);
         __syncthreads();
-        adj_s<2>(v, d, U, Y1, Y2, Y3, Y3B, FB, TMP, LS, HS, UB, Y1B, acc, l0, BS);
+        adj_s<2>(v, d, U, Y1, Y2, Y3, Y3B, FB, TMP, LS, HS, UB, Y1B, acc, tau, l0, BS);
         __syncthreads();
-        adj_gather<2>(v, d, U, FB, LS, HS, LV, UB, Y2B, acc, l0, BS);
+        adj_gather<2>(v, d, U, FB, LS, HS, LV, UB, Y2B, acc, tau, l0, BS);
         __syncthreads();
         adj_v<false>(v, U, Y2, Y2B, UB, Y1B, TMP, LV, acc, l0, BS);
         __syncthreads();
     }
-    adj_s<1>(v, d, U, Y1, Y2, Y1, Y1B, FB, TMP, LS, HS, UB, Y1B, acc, l0, BS);
+    adj_s<1>(v, d, U, Y1, Y2, Y1, Y1B, FB, TMP, LS, HS, UB, Y1B, acc, tau, l0, BS);
     __syncthreads();
-    adj_gather<1>(v, d, U, FB, LS, HS, LV, UB, Y2B, acc, l0, BS);
+    adj_gather<1>(v, d, U, FB, LS, HS, LV, UB, Y2B, acc, tau, l0, BS);
     __syncthreads();
 }
 

@@ -28,12 +28,14 @@ enum {
 };
 // slots of the v-direction tables ([t][i] layout: i fastest)
 enum { VL_LA = 0, VL_G, VL_VC, VL_VN, VL_IB, VL_COUNT };
-// per-instance 1-D arrays along S (nx each)
-// X_HX: X/A = dd^/dr (adjoint only)
-enum { XB_M = 0, XB_C, XB_P, XB_2, XB_1, X_VHI, X_CHV, X_HX, X_COUNT };
-// per-instance 1-D arrays along v (ny each)
-// Y_HY = v/B, Y_BS = db^/dsigma, Y_EK = de^/dkappa, Y_ET = de^/dtheta, Y_ES = de^/dsigma (adjoint only)
-enum { Y_SLO = 0, Y_B2C, Y_CHS, Y_HY, Y_BS, Y_EK, Y_ET, Y_ES, Y_COUNT };
+// per-instance 1-D arrays along S (nx each).  Adjoint only, coefficient derivatives split into
+// S and v factors: X_HX = S/A (dd^/dr), X_HC = S-factor of c^ (Heston S/A, SABR F^beta/A),
+// X_HA = F^(2 beta)/A^2 and X_HDD = F^(2 beta) A''/A^3 (SABR D(t) terms of a^ and d^)
+enum { XB_M = 0, XB_C, XB_P, XB_2, XB_1, X_VHI, X_CHV, X_HX, X_HC, X_HA, X_HDD, X_COUNT };
+// per-instance 1-D arrays along v (ny each).  Adjoint only: Y_HY = v-factor of c^ (Heston v/B,
+// SABR v^2/B), Y_BS = db^/dsigma, Y_EK = de^/dkappa, Y_ET = de^/dtheta, Y_ES = de^/dsigma,
+// Y_HV2 = v^2/2 (SABR D(t) terms)
+enum { Y_SLO = 0, Y_B2C, Y_CHS, Y_HY, Y_BS, Y_EK, Y_ET, Y_ES, Y_HV2, Y_COUNT };
 
 struct bdesc {
     int nx, ny, steps, scheme;
@@ -46,6 +48,9 @@ struct bdesc {
     int pad_;
     // scalars of the parameter derivatives: delta, k/2, ni, beta~, sigma, rho, theta, zeta, gamma, k
     double a_delta, a_halfk, a_ni, a_betat, a_sigma, a_rho, a_theta, a_zeta, a_gamma, a_k;
+    // SABR (r = 0): dD^p/dr = -p tau with tau = T - t = a_tau0 + a_dtau * step; alpha~, 1 - beta
+    int model, pad2_;
+    double a_alphat, a_omb, a_tau0, a_dtau;
 };
 
 template <typename T> struct bparams {
@@ -574,7 +579,7 @@ template <int BS> __global__ void __launch_bounds__(BS, 512 / BS) k_batch_fwdadj
             for (int m = L - 1; m >= 0; --m) {
                 const double *um = (m == 0) ? u0 : slot(m, 0);
                 adj_step<BS>(v, d, um, slot(m, 1), slot(m, 2), slot(m, 3), slot(m + 1, 0), vb, ub, Y1B, Y2B, Y3B, FB,
-                             TMP, LV, LS, HS, acc);
+                             TMP, LV, LS, HS, acc, d.a_tau0 + d.a_dtau * (n0 + m));
                 double *t = ub;
                 ub = vb;
                 vb = t;
@@ -828,7 +833,7 @@ template <typename T> struct batch_typed {
     int grid_blocks = 0;
     long long launches = 0;
     // forward + adjoint
-    bool adjoint_ok = false;      // FP64 Heston DR/CS/MCS only
+    bool adjoint_ok = false;      // FP64 DR/CS/MCS, Heston and SABR with r = 0
     std::string adjoint_why;
     int ck_override = 0;          // checkpoint interval (0 = ceil(sqrt(steps)))
     int grid_adj = 0;                 // CTAs the workspace has slices for
@@ -956,24 +961,39 @@ template <typename T> int batch_typed<T>::create(const lss_adi_problem *ps, int 
                     }
                     const double h1 = tt.sc.h1;
                     {
-                        // Heston coefficient derivatives (adjoint): X/A, v/B, db^/dsigma, de^/dkappa,
-                        // de^/dtheta, de^/dsigma on the grid (double)
+                        // coefficient derivatives (adjoint), double.  Heston: a = vS^2/2, b = sigma^2 v/2,
+                        // c = rho sigma v S, d = rS, e = kappa (theta - v), f = -r.  SABR (r = 0, D = 1):
+                        // a = v^2 F^(2 beta) D^(2(1-beta))/2, b = nu^2 v^2/2, c = rho nu v^2 F^beta D^(1-beta),
+                        // d = rF, e = 0, f = -r (sigma carries nu).
                         sinh_map<double> g;
                         g.init(ps[k]);
-                        const double sg = ps[k].sigma;
+                        const double sg = ps[k].sigma, bt = ps[k].sabr_beta;
+                        const bool sabr = ps[k].model == LSS_ADI_SABR;
                         for (int i = 0; i < d.nx; ++i) {
                             const double z = static_cast<double>(tt.sc.h1) * i;
-                            xh[X_HX * total_x + d.ox + i] = static_cast<T>(g.x(z) / g.a_der(z));
+                            const double x = g.x(z), A = g.a_der(z), Add = g.c_der(z);
+                            xh[X_HX * total_x + d.ox + i] = static_cast<T>(x / A);
+                            xh[X_HC * total_x + d.ox + i] = static_cast<T>(sabr ? std::pow(x, bt) / A : x / A);
+                            xh[X_HA * total_x + d.ox + i] = static_cast<T>(sabr ? std::pow(x, 2.0 * bt) / (A * A) : 0.0);
+                            xh[X_HDD * total_x + d.ox + i] = static_cast<T>(sabr ? std::pow(x, 2.0 * bt) * Add / (A * A * A) : 0.0);
                         }
                         for (int j = 0; j < d.ny; ++j) {
                             const double e = static_cast<double>(tt.sc.h2) * j;
                             const double B = g.b_der(e), Bdd = g.d_der(e), vv = g.y(e);
-                            yh[Y_HY * total_y + d.oy + j] = static_cast<T>(vv / B);
-                            yh[Y_BS * total_y + d.oy + j] = static_cast<T>(sg * vv / (B * B));
-                            yh[Y_EK * total_y + d.oy + j] = static_cast<T>((ps[k].theta_v - vv) / B);
-                            yh[Y_ET * total_y + d.oy + j] = static_cast<T>(ps[k].kappa / B);
-                            yh[Y_ES * total_y + d.oy + j] = static_cast<T>(-sg * vv * Bdd / (B * B * B));
+                            const double vb = sabr ? vv * vv : vv; // the v factor of b and c
+                            yh[Y_HY * total_y + d.oy + j] = static_cast<T>(vb / B);
+                            yh[Y_BS * total_y + d.oy + j] = static_cast<T>(sg * vb / (B * B));
+                            yh[Y_EK * total_y + d.oy + j] = static_cast<T>(sabr ? 0.0 : (ps[k].theta_v - vv) / B);
+                            yh[Y_ET * total_y + d.oy + j] = static_cast<T>(sabr ? 0.0 : ps[k].kappa / B);
+                            yh[Y_ES * total_y + d.oy + j] = static_cast<T>(-sg * vb * Bdd / (B * B * B));
+                            yh[Y_HV2 * total_y + d.oy + j] = static_cast<T>(sabr ? 0.5 * vv * vv : 0.0);
                         }
+                        desc[k].model = ps[k].model;
+                        desc[k].a_alphat = static_cast<double>(tt.sc.alpha);
+                        desc[k].a_omb = 1.0 - bt;
+                        const double kk = static_cast<double>(tt.sc.k);
+                        desc[k].a_tau0 = ps[k].forward ? ps[k].maturity - kk : kk;
+                        desc[k].a_dtau = ps[k].forward ? -kk : kk;
                         desc[k].a_delta = static_cast<double>(tt.sc.delta);
                         desc[k].a_halfk = 0.5 * static_cast<double>(tt.sc.k);
                         desc[k].a_ni = static_cast<double>(tt.sc.ni);
@@ -1047,7 +1067,7 @@ template <typename T> int batch_typed<T>::create(const lss_adi_problem *ps, int 
     adjoint_ok = std::is_same<T, double>::value;
     adjoint_why = adjoint_ok ? "" : "the adjoint is FP64 only";
     for (int k = 0; k < n && adjoint_ok; ++k) {
-        if (ps[k].model != LSS_ADI_HESTON) { adjoint_ok = false; adjoint_why = "the adjoint covers the Heston model only"; }
+        if (time_dependent(ps[k])) { adjoint_ok = false; adjoint_why = "no adjoint for SABR with r != 0"; }
         if (ps[k].scheme == LSS_ADI_HUNDSDORFER_VERWER) { adjoint_ok = false; adjoint_why = "no adjoint for Hundsdorfer-Verwer yet"; }
     }
 

@@ -22,6 +22,11 @@ BASE = dict(model="heston", kappa=1.5, theta_v=0.04, sigma=0.3, rho=-0.6, rate=0
             beta_scale=24.0, eval_s=100.0, eval_v=0.04)
 
 
+SABR = dict(model="sabr", sigma=0.4, rho=-0.3, sabr_beta=0.5, rate=0.0, strike=0.05, maturity=1.0, s_lo=0.0,
+            s_hi=0.2, v_lo=0.0, v_hi=1.0, nonuniform=True, acc_point=0.05, alpha_scale=10.0, beta_scale=24.0,
+            eval_s=0.05, eval_v=0.2)
+
+
 def bilinear_value(surface, x, y, s0, v0):
     i = max(0, min(len(x) - 2, int(np.searchsorted(x, s0, side="right")) - 1))
     j = max(0, min(len(y) - 2, int(np.searchsorted(y, v0, side="right")) - 1))
@@ -51,7 +56,7 @@ def fd_grad(fn, p, name, rel=1e-5):
         dn = dataclasses.replace(p, **{name: base - h})
         return (fn(up) - fn(dn)) / (2 * h)
 
-    h = rel * abs(base)
+    h = rel * (abs(base) if base != 0.0 else 1e-2)  # r = 0: absolute bump 1e-7
     return (4.0 * central(h / 2) - central(h)) / 3.0
 
 
@@ -62,6 +67,11 @@ CASES = {
     "dr_70x35": dict(BASE, scheme="dr", nx=70, ny=35, nt=41),
     "mcs_z08_theta80": dict(BASE, scheme="mcs", zeta=0.8, theta_scheme="theta80", nx=48, ny=24, nt=31, rho=-0.4),
     "mcs_z08_cn": dict(BASE, scheme="mcs", zeta=0.8, nx=52, ny=26, nt=31, rho=-0.4),
+    # SABR at r = 0 (sigma carries nu; kappa and theta do not enter): the r sensitivity comes
+    # from d = rF, f = -r and the discount factors D(t) = exp(-r (T - t)) inside a and c
+    "sabr_dr": dict(SABR, scheme="dr", nx=48, ny=26, nt=31),
+    "sabr_cs": dict(SABR, scheme="cs", nx=44, ny=24, nt=25, rho=0.3),
+    "sabr_mcs_z08": dict(SABR, scheme="mcs", zeta=0.8, theta_scheme="theta80", nx=40, ny=22, nt=21),
 }
 
 
@@ -76,7 +86,7 @@ def test_parameter_gradients_match_device_finite_differences(lss, key):
         assert abs(grads[k] - fd) <= 1e-6 * max(abs(fd), 1e-3 * abs(val)), (name, grads[k], fd)
 
 
-@pytest.mark.parametrize("key", ["mcs_64x32", "dr_70x35", "mcs_z08_cn"])
+@pytest.mark.parametrize("key", ["mcs_64x32", "dr_70x35", "mcs_z08_cn", "sabr_dr", "sabr_mcs_z08"])
 def test_parameter_gradients_match_reference_bump_and_revalue(lss, oracle, key):
     p = lss.HestonProblem(**CASES[key])
     val, grads, _ = lss.ImplicitHestonSolver(p, precision="f64", arith="fast").adjoint(want_payoff_grad=False)
@@ -85,7 +95,7 @@ def test_parameter_gradients_match_reference_bump_and_revalue(lss, oracle, key):
         assert abs(grads[k] - fd) <= 1e-6 * max(abs(fd), 1e-3 * abs(val)), (name, grads[k], fd)
 
 
-@pytest.mark.parametrize("key", ["mcs_64x32", "cs_60x30", "dr_70x35"])
+@pytest.mark.parametrize("key", ["mcs_64x32", "cs_60x30", "dr_70x35", "sabr_cs"])
 def test_payoff_gradient_is_the_linear_response(lss, key):
     p = lss.HestonProblem(**CASES[key])
     s = lss.ImplicitHestonSolver(p, precision="f64", arith="fast")
