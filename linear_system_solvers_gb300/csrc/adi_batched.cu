@@ -794,6 +794,135 @@ __global__ void __launch_bounds__(1024) k_wide_v_chunk(const __grid_constant__ b
     }
 }
 
+// ------------------------------------------------------------------------------------------
+// wide forward + adjoint of one large FP64 instance: the adjoint stages of adi_adjoint.cuh as
+// one kernel each over all threads (thread per line / column), host-sequenced like the
+// forward; each thread's parameter sums live in `acc` (structure of arrays, 10 x nthr) between
+// kernels and are reduced once at the end.
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ void acc_load(adj_acc &acc, const double *a, long long nthr, long long t)
+{
+    for (int q = 0; q < 5; ++q) acc.s[q] = a[q * nthr + t];
+    acc.vk = a[5 * nthr + t];
+    acc.vt = a[6 * nthr + t];
+    acc.vs1 = a[7 * nthr + t];
+    acc.vs2 = a[8 * nthr + t];
+    acc.vb = a[9 * nthr + t];
+}
+__device__ __forceinline__ void acc_store(const adj_acc &acc, double *a, long long nthr, long long t)
+{
+    for (int q = 0; q < 5; ++q) a[q * nthr + t] = acc.s[q];
+    a[5 * nthr + t] = acc.vk;
+    a[6 * nthr + t] = acc.vt;
+    a[7 * nthr + t] = acc.vs1;
+    a[8 * nthr + t] = acc.vs2;
+    a[9 * nthr + t] = acc.vb;
+}
+
+__global__ void k_wadj_b2(const __grid_constant__ bparams<double> p, double *VB, double *UB)
+{
+    const bdesc d = p.desc[0];
+    const inst_view<double> v = make_view(p, d);
+    adj_b2(v, VB, UB, gtid(), gstride());
+}
+
+template <bool FIRST>
+__global__ void k_wadj_v(const __grid_constant__ bparams<double> p, const double *in, const double *out, const double *XB,
+                         double *INB, double *INHB, double *TMP, double *LV, double *acc_a)
+{
+    const bdesc d = p.desc[0];
+    const inst_view<double> v = make_view(p, d);
+    const long long nthr = gstride(), t = gtid();
+    adj_acc acc;
+    acc_load(acc, acc_a, nthr, t);
+    adj_v<FIRST>(v, in, out, XB, INB, INHB, TMP, LV, acc, gtid(), gstride());
+    acc_store(acc, acc_a, nthr, t);
+}
+
+template <int KIND>
+__global__ void k_wadj_s(const __grid_constant__ bparams<double> p, const double *U, const double *Y1, const double *Y2,
+                         const double *Yo, const double *XB, double *FB, double *TMP, double *LS, double *HS, double *UB,
+                         double *Y1B, double *acc_a, double tau)
+{
+    const bdesc d = p.desc[0];
+    const inst_view<double> v = make_view(p, d);
+    const long long nthr = gstride(), t = gtid();
+    adj_acc acc;
+    acc_load(acc, acc_a, nthr, t);
+    adj_s<KIND>(v, d, U, Y1, Y2, Yo, XB, FB, TMP, LS, HS, UB, Y1B, acc, tau, gtid(), gstride());
+    acc_store(acc, acc_a, nthr, t);
+}
+
+template <int KIND>
+__global__ void k_wadj_gather(const __grid_constant__ bparams<double> p, const double *U, const double *FB, const double *LS,
+                              const double *HS, const double *LV, double *UB, double *Y2B, double *acc_a, double tau)
+{
+    const bdesc d = p.desc[0];
+    const inst_view<double> v = make_view(p, d);
+    const long long nthr = gstride(), t = gtid();
+    adj_acc acc;
+    acc_load(acc, acc_a, nthr, t);
+    adj_gather<KIND>(v, d, U, FB, LS, HS, LV, UB, Y2B, acc, tau, gtid(), gstride());
+    acc_store(acc, acc_a, nthr, t);
+}
+
+// final surface out, adjoint arrays cleared, finiteness of the final surface
+__global__ void k_wadj_begin(const __grid_constant__ bparams<double> p, const double *cur, double *VB, double *FB,
+                             double *Y1B, double *Y3B)
+{
+    const bdesc d = p.desc[0];
+    const long long n = (long long)d.nx * d.ny;
+    int bad = 0;
+    for (long long q = gtid(); q < n; q += gstride()) {
+        const double val = cur[q];
+        bad |= !isfinite(val);
+        p.U[q] = val;
+        VB[q] = 0.0;
+        FB[q] = 0.0;
+        Y1B[q] = 0.0;
+        Y3B[q] = 0.0;
+    }
+    if (bad) atomicOr(p.status, 1);
+}
+// value and its bilinear weights as the adjoint seed
+__global__ void k_wadj_seed(const __grid_constant__ bparams<double> p, const double *cur, double *VB)
+{
+    const bdesc d = p.desc[0];
+    const long long o = (long long)d.i0 * d.ny + d.j0;
+    p.values[0] = d.w00 * cur[o] + d.w10 * cur[o + d.ny] + d.w01 * cur[o + 1] + d.w11 * cur[o + d.ny + 1];
+    p.final_in_v[0] = 0;
+    VB[o] = d.w00;
+    VB[o + d.ny] = d.w10;
+    VB[o + 1] = d.w01;
+    VB[o + d.ny + 1] = d.w11;
+}
+// sum of the per-thread parameter sums; output order kappa, theta, sigma, rho, r
+__global__ void __launch_bounds__(256) k_wadj_reduce(const __grid_constant__ bparams<double> p, const double *acc_a,
+                                                     long long nthr)
+{
+    __shared__ double red[10][256];
+    for (int q = 0; q < 10; ++q) {
+        double sum = 0.0;
+        for (long long t = threadIdx.x; t < nthr; t += 256) sum += acc_a[q * nthr + t];
+        red[q][threadIdx.x] = sum;
+    }
+    __syncthreads();
+    for (int h = 128; h > 0; h >>= 1) {
+        if (threadIdx.x < h)
+            for (int q = 0; q < 10; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const bdesc d = p.desc[0];
+        const double th = d.a_theta, ni = d.a_ni;
+        p.grads[0] = red[1][0] + ni * th * red[5][0];
+        p.grads[1] = red[2][0] + ni * th * red[6][0];
+        p.grads[2] = red[3][0] + ni * th * red[7][0] + d.a_betat * th * red[8][0];
+        p.grads[3] = red[4][0];
+        p.grads[4] = red[0][0] + d.a_halfk * th * red[9][0];
+    }
+}
+
 // value, finiteness flag and final-array flag of the single instance
 template <typename T> __global__ void k_wide_finish(const __grid_constant__ bparams<T> p, const T *U)
 {
@@ -894,8 +1023,13 @@ template <typename T> struct batch_typed {
     int autotune_wide(cudaStream_t s);
     template <int KIND> void launch_wide_s(cudaStream_t s, const bparams<T> &p, const T *U, const T *Y1, const T *Y2, T *Y);
     void launch_wide_v(cudaStream_t s, const bparams<T> &p, const T *in, const T *inh, const T *b0, T *out);
+    void enqueue_wide_step(cudaStream_t s, const bparams<T> &p, const T *U, T *Y1, T *Y2, T *Y3, T *V);
     int enqueue_wide(cudaStream_t s);
     int run_wide(cudaStream_t s, bool use_graph);
+    // wide forward + adjoint (count == 1, FP64)
+    dbuf<double> d_wws;
+    long long wws_need = 0;
+    int enqueue_wide_adjoint(cudaStream_t s);
     int enqueue(int mode, cudaStream_t s);
     int run(int mode, cudaStream_t s, bool use_graph);
 };
@@ -1366,37 +1500,134 @@ template <typename T> int batch_typed<T>::autotune_wide(cudaStream_t s)
     return set_wide_chunks(ps, pv, s);
 }
 
+// One time step U -> V of the wide path (stage outputs in Y1, Y2, Y3).
+template <typename T>
+void batch_typed<T>::enqueue_wide_step(cudaStream_t s, const bparams<T> &p, const T *U, T *Y1, T *Y2, T *Y3, T *V)
+{
+    const bdesc &d = desc[0];
+    T *b0 = d_b0.p;
+    k_wide_b1<T><<<grid_for(d.nx, 128), 128, 0, s>>>(p, U, b0);
+    launch_wide_s<1>(s, p, U, nullptr, nullptr, Y1);
+    if (d.scheme == LSS_ADI_DOUGLAS_RACHFORD) {
+        launch_wide_v(s, p, U, Y1, b0, V);
+    } else {
+        launch_wide_v(s, p, U, Y1, b0, Y2);
+        launch_wide_s<2>(s, p, U, Y1, Y2, Y3);
+        if (d.scheme == LSS_ADI_HUNDSDORFER_VERWER)
+            launch_wide_v(s, p, Y2, Y3, b0, V);
+        else
+            launch_wide_v(s, p, U, Y3, b0, V);
+    }
+    k_wide_b2<T><<<grid_for(d.ny, 128), 128, 0, s>>>(p, V);
+}
+
 template <typename T> int batch_typed<T>::enqueue_wide(cudaStream_t s)
 {
     const bdesc &d = desc[0];
     bparams<T> p = params();
-    T *U = p.U, *V = p.V, *Y1 = p.Y1, *Y2 = p.Y2, *Y3 = p.Y3, *b0 = d_b0.p;
+    T *U = p.U, *V = p.V, *Y1 = p.Y1, *Y2 = p.Y2, *Y3 = p.Y3;
     LSS_CUDA_TRY(cudaMemcpyAsync(U, d_payoff.p, total_n * sizeof(T), cudaMemcpyDeviceToDevice, s), "wide: initial state");
-    const int gX = grid_for(d.nx, 128), gY = grid_for(d.ny, 128);
     long long nl = 0;
     for (int step = 0; step < d.steps; ++step) {
-        k_wide_b1<T><<<gX, 128, 0, s>>>(p, U, b0);
-        launch_wide_s<1>(s, p, U, nullptr, nullptr, Y1);
-        if (d.scheme == LSS_ADI_DOUGLAS_RACHFORD) {
-            launch_wide_v(s, p, U, Y1, b0, V);
-            nl += 3;
-        } else {
-            launch_wide_v(s, p, U, Y1, b0, Y2);
-            launch_wide_s<2>(s, p, U, Y1, Y2, Y3);
-            if (d.scheme == LSS_ADI_HUNDSDORFER_VERWER)
-                launch_wide_v(s, p, Y2, Y3, b0, V);
-            else
-                launch_wide_v(s, p, U, Y3, b0, V);
-            nl += 5;
-        }
-        k_wide_b2<T><<<gY, 128, 0, s>>>(p, V);
-        nl += 1;
+        enqueue_wide_step(s, p, U, Y1, Y2, Y3, V);
+        nl += d.scheme == LSS_ADI_DOUGLAS_RACHFORD ? 4 : 6;
         std::swap(U, V);
     }
     k_wide_finish<T><<<1, 256, 0, s>>>(p, U);
     LSS_CUDA_TRY(cudaGetLastError(), "wide: launching the time loop");
     launches = nl + 1;
     return LSS_ADI_OK;
+}
+
+// Forward + adjoint of the single instance with the wide kernels: forward pass keeping a
+// checkpoint every d.ck steps, then per segment (last first) a forward recomputation keeping
+// every step's stage values and the adjoint steps in reverse order (as k_batch_fwdadj).
+template <typename T> int batch_typed<T>::enqueue_wide_adjoint(cudaStream_t s)
+{
+    if constexpr (!std::is_same<T, double>::value) {
+        (void)s;
+        return set_error(LSS_ADI_EUNSUPPORTED, "wide adjoint: FP64 only");
+    } else {
+        if (count != 1) return set_error(LSS_ADI_EINVAL, "wide adjoint: one instance only");
+        if (!adjoint_ok) return set_error(LSS_ADI_EUNSUPPORTED, "wide adjoint: " + adjoint_why);
+        bdesc &d = desc[0];
+        const int c0 = ck_override > 0 ? std::min(ck_override, d.steps) : d.ck;
+        if (c0 != d.ck) {
+            d.ck = c0;
+            LSS_CUDA_TRY(cudaMemcpy(d_desc.p, &d, sizeof(bdesc), cudaMemcpyHostToDevice), "wide adjoint: descriptor");
+        }
+        const int nx = d.nx, ny = d.ny, c = d.ck;
+        const long long n = total_n;
+        const int nseg = (d.steps + c - 1) / c;
+        const int threads = 128, grid = grid_for(std::max(nx, ny), threads);
+        const long long nthr = static_cast<long long>(grid) * threads;
+        const long long need = (nseg + 4LL * (c + 1) + 9) * n + nx + 2LL * ny + 10 * nthr;
+        if (!d_wws.p || wws_need != need) {
+            LSS_CUDA_TRY(d_wws.alloc(need), "wide adjoint: allocating workspace");
+            wws_need = need;
+        }
+        double *CK = d_wws.p;
+        double *SEG = CK + static_cast<long long>(nseg) * n;
+        double *W0 = SEG + (c + 1) * 4LL * n, *W1 = W0 + n;
+        double *UB = W1 + n, *VB = UB + n, *Y1B = VB + n, *Y2B = Y1B + n, *Y3B = Y2B + n, *FB = Y3B + n, *TMP = FB + n;
+        double *LV = TMP + n, *LS = LV + nx, *HS = LS + ny, *ACC = HS + ny;
+        auto slot = [&](int m, int a) -> double * { return SEG + (static_cast<long long>(m) * 4 + a) * n; };
+        const bparams<double> p = params();
+        // stage arrays start at zero (rows 0 and nx-1 of Y2 are never written by the sweeps)
+        LSS_CUDA_TRY(cudaMemsetAsync(SEG, 0, (c + 1) * 4LL * n * sizeof(double), s), "wide adjoint: clearing");
+        LSS_CUDA_TRY(cudaMemsetAsync(ACC, 0, 10 * nthr * sizeof(double), s), "wide adjoint: clearing");
+        LSS_CUDA_TRY(cudaMemsetAsync(d_status.p, 0, sizeof(int), s), "wide adjoint: clearing");
+        LSS_CUDA_TRY(cudaMemcpyAsync(CK, d_payoff.p, n * sizeof(double), cudaMemcpyDeviceToDevice, s), "wide adjoint: initial state");
+        long long nl = 0;
+        const int per_step = d.scheme == LSS_ADI_DOUGLAS_RACHFORD ? 4 : 6;
+        const double *cur = CK;
+        for (int step = 0; step < d.steps; ++step) {
+            double *next = ((step + 1) % c == 0 && step + 1 < d.steps) ? CK + static_cast<long long>((step + 1) / c) * n
+                                                                        : ((step & 1) ? W1 : W0);
+            enqueue_wide_step(s, p, cur, slot(0, 1), slot(0, 2), slot(0, 3), next);
+            nl += per_step;
+            cur = next;
+        }
+        k_wadj_begin<<<grid_for(n, 256), 256, 0, s>>>(p, cur, VB, FB, Y1B, Y3B);
+        k_wadj_seed<<<1, 1, 0, s>>>(p, cur, VB);
+        nl += 2;
+        double *ub = UB, *vb = VB;
+        for (int sgi = nseg - 1; sgi >= 0; --sgi) {
+            const int n0 = sgi * c;
+            const int L = std::min(c, d.steps - n0);
+            const double *u0 = CK + static_cast<long long>(sgi) * n;
+            for (int m = 0; m < L; ++m) {
+                const double *um = (m == 0) ? u0 : slot(m, 0);
+                enqueue_wide_step(s, p, um, slot(m, 1), slot(m, 2), slot(m, 3), slot(m + 1, 0));
+                nl += per_step;
+            }
+            for (int m = L - 1; m >= 0; --m) {
+                const double *um = (m == 0) ? u0 : slot(m, 0);
+                const double *Y1 = slot(m, 1), *Y2 = slot(m, 2), *Y3 = slot(m, 3), *Vo = slot(m + 1, 0);
+                const double tau = d.a_tau0 + d.a_dtau * (n0 + m);
+                k_wadj_b2<<<grid, threads, 0, s>>>(p, vb, ub);
+                if (d.scheme == LSS_ADI_DOUGLAS_RACHFORD) {
+                    k_wadj_v<true><<<grid, threads, 0, s>>>(p, um, Vo, vb, ub, Y1B, TMP, LV, ACC);
+                    nl += 2;
+                } else {
+                    k_wadj_v<true><<<grid, threads, 0, s>>>(p, um, Vo, vb, ub, Y3B, TMP, LV, ACC);
+                    k_wadj_s<2><<<grid, threads, 0, s>>>(p, um, Y1, Y2, Y3, Y3B, FB, TMP, LS, HS, ub, Y1B, ACC, tau);
+                    k_wadj_gather<2><<<grid, threads, 0, s>>>(p, um, FB, LS, HS, LV, ub, Y2B, ACC, tau);
+                    k_wadj_v<false><<<grid, threads, 0, s>>>(p, um, Y2, Y2B, ub, Y1B, TMP, LV, ACC);
+                    nl += 5;
+                }
+                k_wadj_s<1><<<grid, threads, 0, s>>>(p, um, Y1, Y2, Y1, Y1B, FB, TMP, LS, HS, ub, Y1B, ACC, tau);
+                k_wadj_gather<1><<<grid, threads, 0, s>>>(p, um, FB, LS, HS, LV, ub, Y2B, ACC, tau);
+                nl += 2;
+                std::swap(ub, vb);
+            }
+        }
+        k_wadj_reduce<<<1, 256, 0, s>>>(p, ACC, nthr);
+        LSS_CUDA_TRY(cudaMemcpyAsync(p.V, vb, n * sizeof(double), cudaMemcpyDeviceToDevice, s), "wide adjoint: payoff gradient");
+        LSS_CUDA_TRY(cudaGetLastError(), "wide adjoint: launching");
+        launches = nl + 1;
+        return LSS_ADI_OK;
+    }
 }
 
 template <typename T> int batch_typed<T>::run_wide(cudaStream_t s, bool use_graph)
@@ -1540,6 +1771,7 @@ int make_wide_solver(const lss_adi_problem &p, std::unique_ptr<wide_solver_base>
 // lss_adi_adjoint: one parametric FP64 Heston instance through the batched forward+adjoint kernel.
 struct adjoint_impl {
     batch_typed<double> b;
+    bool wide = false; // large instance: the wide kernels instead of one CTA
 };
 
 adjoint_solver::adjoint_solver() = default;
@@ -1547,16 +1779,24 @@ adjoint_solver::~adjoint_solver() = default;
 
 int adjoint_solver::init(const lss_adi_problem &p)
 {
-    if (p.nx > 256) return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_adjoint: nx > 256 not supported");
-    if (time_dependent(p))
-        return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_adjoint: SABR with r != 0 (time-dependent coefficients) not supported");
     if (p.scheme == LSS_ADI_HUNDSDORFER_VERWER)
         return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_adjoint: no adjoint for Hundsdorfer-Verwer yet");
+    if (time_dependent(p))
+        return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_adjoint: SABR with r != 0 (time-dependent coefficients) not supported");
     impl.reset(new (std::nothrow) adjoint_impl());
     if (!impl) return set_error(LSS_ADI_ENOMEM, "host allocation failed");
     lss_adi_problem q = p;
     q.arith = LSS_ADI_ARITH_FAST;
-    return impl->b.create(&q, 1);
+    int rc = impl->b.create(&q, 1);
+    if (rc) return rc;
+    // one CTA carries an instance of up to 256 x 160 points well; larger ones run wide
+    impl->wide = p.nx > 256 || static_cast<long long>(p.nx) * p.ny > 40960;
+    if (impl->wide && !(p.options & LSS_ADI_OPT_LINE_PER_THREAD)) {
+        rc = impl->b.autotune_wide(nullptr);
+        if (rc) return rc;
+        LSS_CUDA_TRY(cudaDeviceSynchronize(), "lss_adi_adjoint: tuning");
+    }
+    return LSS_ADI_OK;
 }
 
 int adjoint_solver::run(const void *payoff, double *out_value, double *dv_dparams, void *dv_dpayoff, int checkpoint_every,
@@ -1571,7 +1811,7 @@ int adjoint_solver::run(const void *payoff, double *out_value, double *dv_dparam
                                      dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s),
                      "lss_adi_adjoint: copying the terminal condition");
     b.ck_override = checkpoint_every;
-    int rc = b.run(1, s, false);
+    int rc = impl->wide ? b.enqueue_wide_adjoint(s) : b.run(1, s, false);
     if (rc) return rc;
     if (out_value)
         LSS_CUDA_TRY(cudaMemcpyAsync(out_value, b.d_values.p, sizeof(double), cudaMemcpyDeviceToHost, s), "lss_adi_adjoint: value");

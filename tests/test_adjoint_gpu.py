@@ -72,6 +72,10 @@ CASES = {
     "sabr_dr": dict(SABR, scheme="dr", nx=48, ny=26, nt=31),
     "sabr_cs": dict(SABR, scheme="cs", nx=44, ny=24, nt=25, rho=0.3),
     "sabr_mcs_z08": dict(SABR, scheme="mcs", zeta=0.8, theta_scheme="theta80", nx=40, ny=22, nt=21),
+    # large instances: the adjoint runs as one kernel per stage over the whole GPU
+    "wide_heston_cs": dict(BASE, scheme="cs", nx=300, ny=64, nt=21, rho=-0.3),
+    "wide_heston_mcs": dict(BASE, scheme="mcs", zeta=1.0 / 3.0, nx=264, ny=160, nt=9, rho=-0.2),
+    "wide_sabr_dr": dict(SABR, scheme="dr", nx=280, ny=90, nt=17),
 }
 
 
@@ -86,7 +90,8 @@ def test_parameter_gradients_match_device_finite_differences(lss, key):
         assert abs(grads[k] - fd) <= 1e-6 * max(abs(fd), 1e-3 * abs(val)), (name, grads[k], fd)
 
 
-@pytest.mark.parametrize("key", ["mcs_64x32", "dr_70x35", "mcs_z08_cn", "sabr_dr", "sabr_mcs_z08"])
+@pytest.mark.parametrize("key", ["mcs_64x32", "dr_70x35", "mcs_z08_cn", "sabr_dr", "sabr_mcs_z08", "wide_heston_cs",
+                                 "wide_sabr_dr"])
 def test_parameter_gradients_match_reference_bump_and_revalue(lss, oracle, key):
     p = lss.HestonProblem(**CASES[key])
     val, grads, _ = lss.ImplicitHestonSolver(p, precision="f64", arith="fast").adjoint(want_payoff_grad=False)
@@ -95,7 +100,7 @@ def test_parameter_gradients_match_reference_bump_and_revalue(lss, oracle, key):
         assert abs(grads[k] - fd) <= 1e-6 * max(abs(fd), 1e-3 * abs(val)), (name, grads[k], fd)
 
 
-@pytest.mark.parametrize("key", ["mcs_64x32", "cs_60x30", "dr_70x35", "sabr_cs"])
+@pytest.mark.parametrize("key", ["mcs_64x32", "cs_60x30", "dr_70x35", "sabr_cs", "wide_heston_mcs"])
 def test_payoff_gradient_is_the_linear_response(lss, key):
     p = lss.HestonProblem(**CASES[key])
     s = lss.ImplicitHestonSolver(p, precision="f64", arith="fast")
@@ -110,8 +115,9 @@ def test_payoff_gradient_is_the_linear_response(lss, key):
     assert abs((v1 - v0) - pred) <= 1e-9 * max(1.0, np.sum(np.abs(lam * delta)))
 
 
-def test_checkpoint_interval_does_not_change_results(lss):
-    p = lss.HestonProblem(**CASES["mcs_64x32"])
+@pytest.mark.parametrize("key", ["mcs_64x32", "wide_heston_cs"])
+def test_checkpoint_interval_does_not_change_results(lss, key):
+    p = lss.HestonProblem(**CASES[key])
     s = lss.ImplicitHestonSolver(p, precision="f64", arith="fast")
     ref = None
     for ck in (0, 1, 3, 7, 50, 1000):
