@@ -119,9 +119,11 @@ def test_wide_path_large_grid(lss, oracle, fp):
 @pytest.mark.parametrize("chunks", [(2, 3), (8, 4), (32, 16), (5, 32)])
 def test_partitioned_line_solves_match_line_per_thread(lss, oracle, scheme, chunks):
     """Chunked S and v line solves (chunk products hf / hb and composed carries) against the
-    thread-per-line solve of the same instance: rounding-level agreement, and the oracle bound."""
-    kw = dict(model="heston", kappa=2.0, theta_v=0.05, sigma=0.4, rho=-0.3, rate=0.02, strike=100.0, maturity=0.5,
-              s_lo=0.0, s_hi=200.0, v_lo=0.0, v_hi=1.2, nx=203, ny=131, nt=9, scheme=scheme, zeta=1.0 / 3.0,
+    thread-per-line solve of the same instance.  They differ by rounding only, which the
+    reference's own scheme amplifies: the bound is 100x the spread that a 1e-15 relative
+    perturbation of the terminal condition causes in the oracle (floor 1e-13)."""
+    kw = dict(model="heston", kappa=2.0, theta_v=0.05, sigma=0.4, rho=-0.3, rate=0.02, strike=100.0, maturity=0.25,
+              s_lo=0.0, s_hi=200.0, v_lo=0.0, v_hi=1.2, nx=203, ny=131, nt=17, scheme=scheme, zeta=1.0 / 3.0,
               acc_point=100.0, **NU)
     p = lss.HestonProblem(**kw)
     s = lss.ImplicitHestonSolver(p, precision="f64", arith="fast")
@@ -129,14 +131,20 @@ def test_partitioned_line_solves_match_line_per_thread(lss, oracle, scheme, chun
     got, val = s.solve(graph=True)
     ref, rval = lss.ImplicitHestonSolver(dataclasses.replace(p, line_per_thread=True), precision="f64",
                                          arith="fast").solve()
-    assert rel_err(got, ref) < 1e-13
-    assert abs(val - rval) <= 1e-13 * max(1.0, abs(rval))
-    want = oracle.solve(oracle_of(oracle, p), "f64")
+    op = oracle_of(oracle, p)
+    want = oracle.solve(op, "f64")
+    x, _ = oracle.grid(op, "f64")
+    pay = np.maximum(x[:, None] - p.strike, 0.0) * np.ones((1, p.ny))
+    noisy = pay * (1.0 + 1e-15 * np.random.default_rng(1).standard_normal(pay.shape))
+    amp = rel_err(oracle.solve(op, "f64", payoff=noisy), want)
+    tol = max(1e-13, 100.0 * amp)
+    assert rel_err(got, ref) < tol
+    assert abs(val - rval) <= tol * max(1.0, abs(rval))
     assert rel_err(got, want) < fp64_tol(want, p.s_hi)
 
 
 def test_partition_autotuner_and_limits(lss):
-    p = lss.HestonProblem(scheme="hv", nx=300, ny=140, nt=5, nonuniform=True, acc_point=100.0, alpha_scale=10.0,
+    p = lss.HestonProblem(scheme="hv", nx=300, ny=100, nt=5, nonuniform=True, acc_point=100.0, alpha_scale=10.0,
                           beta_scale=24.0)
     s = lss.ImplicitHestonSolver(p, precision="f64", arith="fast")
     ps, pv = s.line_chunks(0, 0)
@@ -146,7 +154,7 @@ def test_partition_autotuner_and_limits(lss):
     with pytest.raises(L.LssError):
         s.line_chunks(64, 1)  # more than 32 chunks
     with pytest.raises(L.LssError):
-        s.line_chunks(1, 32)  # 138 rows: fewer than 4 per chunk
+        s.line_chunks(1, 32)  # 98 rows: fewer than 4 per chunk
     ref = lss.ImplicitHestonSolver(p, precision="f64", arith="reference")
     with pytest.raises(L.LssError):
         ref.line_chunks(2, 2)
