@@ -48,12 +48,17 @@ extern "C" {
 #define LSS_ADI_ENOMEM (-2)     /* device allocation failed */
 #define LSS_ADI_ENONFINITE (-3) /* an instance produced NaN/Inf (status array says which) */
 
-/* splitting_method_enum (common/lss_enumerations.hpp:35-41) */
+/* splitting_method_enum (common/lss_enumerations.hpp:35-41); EXPLICIT_EULER is the reference's
+ * explicit_solvers::general_heston_equation with explicit_pde_schemes_enum::Euler
+ * (pde_solvers/two_dimensional/heat_type/lss_2d_general_heston_equation.hpp:317-510,
+ * explicit_schemes/lss_heston_euler_*_scheme.hpp): one explicit 9-point step per time step,
+ * same boundaries; kernel-per-step path only, no adjoint, stability is the caller's (small k). */
 enum lss_adi_scheme {
     LSS_ADI_DOUGLAS_RACHFORD = 0,
     LSS_ADI_CRAIG_SNEYD = 1,
     LSS_ADI_MODIFIED_CRAIG_SNEYD = 2,
-    LSS_ADI_HUNDSDORFER_VERWER = 3
+    LSS_ADI_HUNDSDORFER_VERWER = 3,
+    LSS_ADI_EXPLICIT_EULER = 4
 };
 /* implicit_pde_schemes_enum (common/lss_enumerations.hpp:102-108) */
 enum lss_adi_theta { LSS_ADI_EULER = 0, LSS_ADI_THETA_30 = 1, LSS_ADI_CRANK_NICOLSON = 2, LSS_ADI_THETA_80 = 3 };

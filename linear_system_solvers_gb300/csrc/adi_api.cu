@@ -32,7 +32,7 @@ int validate_problem(const lss_adi_problem &p, std::string &why)
     if (p.nx < 4 || p.ny < 4) return why = "nx and ny must be >= 4", LSS_ADI_EINVAL;
     if (p.nt < 2) return why = "nt (number of time points) must be >= 2", LSS_ADI_EINVAL;
     if (static_cast<long long>(p.nx) * p.ny > (1LL << 30)) return why = "grid larger than 2^30 points", LSS_ADI_EINVAL;
-    if (p.scheme < LSS_ADI_DOUGLAS_RACHFORD || p.scheme > LSS_ADI_HUNDSDORFER_VERWER) return why = "unknown splitting scheme", LSS_ADI_EINVAL;
+    if (p.scheme < LSS_ADI_DOUGLAS_RACHFORD || p.scheme > LSS_ADI_EXPLICIT_EULER) return why = "unknown splitting scheme", LSS_ADI_EINVAL;
     if (p.theta_scheme < LSS_ADI_EULER || p.theta_scheme > LSS_ADI_THETA_80) return why = "unknown theta scheme", LSS_ADI_EINVAL;
     if (p.precision != LSS_ADI_FP64 && p.precision != LSS_ADI_FP32) return why = "precision must be LSS_ADI_FP64 or LSS_ADI_FP32", LSS_ADI_EINVAL;
     if (p.arith != LSS_ADI_ARITH_FAST && p.arith != LSS_ADI_ARITH_REFERENCE) return why = "unknown arithmetic mode", LSS_ADI_EINVAL;
@@ -99,8 +99,9 @@ int lss_adi_create(const lss_adi_problem *p, lss_adi_handle **h)
     hh->prob = *p;
     try {
         // time-dependent coefficients (SABR, r != 0) re-evaluate their tables every step on the
-        // kernel-per-sweep path; the factorised paths precompute time-invariant line factors
-        if (p->arith == LSS_ADI_ARITH_FAST && !time_dependent(*p))
+        // kernel-per-sweep path; the factorised paths precompute time-invariant line factors.
+        // The explicit Euler scheme has no line solves: kernel-per-step path as well.
+        if (p->arith == LSS_ADI_ARITH_FAST && !time_dependent(*p) && p->scheme != LSS_ADI_EXPLICIT_EULER)
             rc = make_wide_solver(*p, hh->wide);
         else
             rc = p->precision == LSS_ADI_FP64 ? make_plain<double>(*p, p->arith, p->eval_s, p->eval_v, hh->s64)
@@ -121,7 +122,7 @@ int lss_adi_create_tabulated(const lss_adi_tables *t, lss_adi_handle **h)
     if (t->nx < 4 || t->ny < 4 || t->nt < 2) return set_error(LSS_ADI_EINVAL, "lss_adi_create_tabulated: nx, ny >= 4 and nt >= 2 required");
     if (!t->coef || !t->coef_v0 || !t->s_lo_dirichlet || !t->s_hi_neumann || !t->v_hi_dirichlet || !t->payoff)
         return set_error(LSS_ADI_EINVAL, "lss_adi_create_tabulated: null table");
-    if (t->scheme < 0 || t->scheme > 3 || t->theta_scheme < 0 || t->theta_scheme > 3)
+    if (t->scheme < 0 || t->scheme > LSS_ADI_EXPLICIT_EULER || t->theta_scheme < 0 || t->theta_scheme > 3)
         return set_error(LSS_ADI_EINVAL, "lss_adi_create_tabulated: unknown scheme");
     if (t->precision != LSS_ADI_FP64 && t->precision != LSS_ADI_FP32)
         return set_error(LSS_ADI_EINVAL, "lss_adi_create_tabulated: unknown precision");

@@ -1781,6 +1781,8 @@ int adjoint_solver::init(const lss_adi_problem &p)
 {
     if (p.scheme == LSS_ADI_HUNDSDORFER_VERWER)
         return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_adjoint: no adjoint for Hundsdorfer-Verwer yet");
+    if (p.scheme == LSS_ADI_EXPLICIT_EULER)
+        return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_adjoint: no adjoint for the explicit Euler scheme");
     if (time_dependent(p))
         return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_adjoint: SABR with r != 0 (time-dependent coefficients) not supported");
     impl.reset(new (std::nothrow) adjoint_impl());
@@ -1903,6 +1905,9 @@ int lss_adi_batch_create(const lss_adi_problem *problems, int count, lss_adi_bat
         if (rc) return set_error(rc, "lss_adi_batch_create: instance " + std::to_string(k) + ": " + why);
         if (problems[k].precision != prec) return set_error(LSS_ADI_EINVAL, "lss_adi_batch_create: mixed precisions");
         if (problems[k].nx > 256) return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_batch_create: nx > 256 (use lss_adi_create)");
+        if (problems[k].scheme == LSS_ADI_EXPLICIT_EULER)
+            return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_batch_create: instance " + std::to_string(k) +
+                                                       ": the explicit Euler scheme runs on lss_adi_create");
         if (time_dependent(problems[k]))
             return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_batch_create: instance " + std::to_string(k) +
                                                        ": SABR with r != 0 has time-dependent coefficients (use lss_adi_create)");

@@ -19,14 +19,18 @@ namespace lss_gb300 {
 // ------------------------------------------------------------------------------------------
 // boundary#1: explicit_heston_boundary_scheme::rhs (explicit_boundary.hpp:39-84) + v_hi column
 // ------------------------------------------------------------------------------------------
+// Results go to bcol0[i * stride], bcolN[i * stride]: the boundary columns of the v lines
+// (stride 1) or, for the explicit Euler step, columns 0 and ny-1 of the next state (stride ny).
 template <typename T, bool X>
-__global__ void k_boundary1(dev_instance<T> d, const T *__restrict__ U, T *__restrict__ bcol0, T *__restrict__ bcolN)
+__global__ void k_boundary1(dev_instance<T> d, const T *__restrict__ U, T *__restrict__ bcol0, T *__restrict__ bcolN,
+                            int stride)
 {
     using R = ar<X>;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int nx = d.nx, ny = d.ny, N = nx - 1;
     if (i >= nx) return;
     const T one = T(1), two = T(2), three = T(3), four = T(4);
+    const long long w = static_cast<long long>(i) * stride;
     if (i == 0) {
         bcol0[0] = d.s_lo[0];
     } else if (i == N) {
@@ -36,7 +40,7 @@ __global__ void k_boundary1(dev_instance<T> d, const T *__restrict__ U, T *__res
         const T t2 = R::mul(R::mul(R::mul(four, d.ni), E), U[N * ny + 1]);
         const T t3 = R::mul(R::mul(d.ni, E), U[N * ny + 2]);
         const T t4 = R::mul(R::mul(d.delta, dlt), D);
-        bcol0[N] = R::sub(R::sub(R::add(t1, t2), t3), t4);
+        bcol0[w] = R::sub(R::sub(R::add(t1, t2), t3), t4);
     } else {
         const T D = d.D0[i], E = d.E0[i], F = d.F0[i];
         const T t1 = R::mul(R::mul(-d.delta, D), U[(i - 1) * ny]);
@@ -44,9 +48,9 @@ __global__ void k_boundary1(dev_instance<T> d, const T *__restrict__ U, T *__res
         const T t3 = R::mul(R::mul(d.delta, D), U[(i + 1) * ny]);
         const T t4 = R::mul(R::mul(d.ni, E), U[i * ny + 2]);
         const T t5 = R::mul(R::mul(R::mul(four, d.ni), E), U[i * ny + 1]);
-        bcol0[i] = R::add(R::sub(R::add(R::add(t1, t2), t3), t4), t5);
+        bcol0[w] = R::add(R::sub(R::add(R::add(t1, t2), t3), t4), t5);
     }
-    bcolN[i] = d.v_hi[i];
+    bcolN[w] = d.v_hi[i];
 }
 
 // ------------------------------------------------------------------------------------------
@@ -216,6 +220,34 @@ __global__ void k_v_sweep(dev_instance<T> d, const T *__restrict__ in, const T *
     }
     out[row] = lo;
     out[row + ny - 1] = hi;
+}
+
+// ------------------------------------------------------------------------------------------
+// Explicit Euler interior (explicit_heston_scheme::rhs, solver_method/
+// lss_heston_euler_solver_method.hpp:24-52, in its evaluation order): the 9-point operator on
+// `U` with the Euler mixed weight gamma * C (explicit_coefficients/lss_heston_euler_coefficients.hpp:53).
+// ------------------------------------------------------------------------------------------
+template <typename T, bool X>
+__global__ void k_euler(dev_instance<T> d, const T *__restrict__ U, T *__restrict__ V)
+{
+    using R = ar<X>;
+    const int j = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = 1 + blockIdx.y;
+    const int ny = d.ny;
+    if (j > ny - 2) return;
+    const long long o = static_cast<long long>(i) * ny + j;
+    const T one = T(1);
+    const T C = R::mul(d.gamma, d.C[o]);
+    T v = R::mul(C, U[o - ny - 1]);
+    v = R::add(v, R::mul(d.M[o], U[o - ny]));
+    v = R::sub(v, R::mul(C, U[o - ny + 1]));
+    v = R::add(v, R::mul(d.Mt[o], U[o - 1]));
+    v = R::add(v, R::mul(R::sub(R::sub(one, d.Z[o]), d.W[o]), U[o]));
+    v = R::add(v, R::mul(d.Pt[o], U[o + 1]));
+    v = R::sub(v, R::mul(C, U[o + ny - 1]));
+    v = R::add(v, R::mul(d.P[o], U[o + ny]));
+    v = R::add(v, R::mul(C, U[o + ny + 1]));
+    V[o] = v;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -420,7 +452,17 @@ template <typename T> template <bool X> void plain_solver<T>::enqueue_steps(cuda
             k_refresh<T, X><<<gref, 256, 0, s>>>(tt, nx, ny, tab_.step_da[step], tab_.step_dc[step]);
             launches_ += 1;
         }
-        k_boundary1<T, X><<<grid_for(nx, 128), 128, 0, s>>>(d_, U, bcol0, bcolN);
+        if (tab_.scheme == LSS_ADI_EXPLICIT_EULER) {
+            // heston_euler_time_loop::run: interior, then boundary #1 into columns 0 / ny-1 of
+            // the next state, then boundary #2 (its rows 0 / nx-1)
+            k_euler<T, X><<<ghv, 128, 0, s>>>(d_, U, V);
+            k_boundary1<T, X><<<grid_for(nx, 128), 128, 0, s>>>(d_, U, V, V + (ny - 1), ny);
+            k_boundary2<T, X><<<grid_for(ny, 128), 128, 0, s>>>(d_, V);
+            launches_ += 3;
+            std::swap(U, V);
+            continue;
+        }
+        k_boundary1<T, X><<<grid_for(nx, 128), 128, 0, s>>>(d_, U, bcol0, bcolN, 1);
         k_s_sweep<T, X, S_STAGE1><<<gs, bs, 0, s>>>(d_, U, U, nullptr, nullptr, Y1, G);
         switch (tab_.scheme) {
         case LSS_ADI_DOUGLAS_RACHFORD:

@@ -34,7 +34,7 @@ class HestonProblem:
     nx: int = 100
     ny: int = 50
     nt: int = 201  # time points (steps = nt - 1)
-    scheme: str = "dr"  # dr | cs | mcs | hv
+    scheme: str = "dr"  # dr | cs | mcs | hv (splittings) | euler (explicit Euler)
     zeta: float = 0.5
     theta_scheme: str = "cn"  # euler | theta30 | cn | theta80
     nonuniform: bool = False

@@ -37,7 +37,7 @@ extern "C" {
 #endif
 
 enum { LSSO_HESTON = 0, LSSO_SABR = 1 };
-enum { LSSO_DR = 0, LSSO_CS = 1, LSSO_MCS = 2, LSSO_HV = 3 };
+enum { LSSO_DR = 0, LSSO_CS = 1, LSSO_MCS = 2, LSSO_HV = 3, LSSO_EXPLICIT_EULER = 4 };
 enum { LSSO_EULER = 0, LSSO_THETA30 = 1, LSSO_CN = 2, LSSO_THETA80 = 3 };
 enum { LSSO_THOMAS_LU = 0, LSSO_DOUBLE_SWEEP = 1 };
 
@@ -49,7 +49,7 @@ typedef struct lsso_problem {
     double s_lo, s_hi, v_lo, v_hi;
     int nx, ny;           /* space points */
     int nt;               /* time points: steps = nt - 1 */
-    int scheme;           /* LSSO_DR .. LSSO_HV */
+    int scheme;           /* LSSO_DR .. LSSO_HV, or LSSO_EXPLICIT_EULER (explicit_solvers) */
     double zeta;          /* splitting weighting value */
     int theta_scheme;     /* LSSO_EULER .. LSSO_THETA80 */
     int nonuniform;       /* grid_enum::Nonuniform */

@@ -159,7 +159,7 @@ static int SFX(validate)(const lsso_problem *p)
     if (!p) return 1;
     if (p->nx < 4 || p->ny < 4) return 2;
     if (p->nt < 2) return 3;
-    if (p->scheme < LSSO_DR || p->scheme > LSSO_HV) return 4;
+    if (p->scheme < LSSO_DR || p->scheme > LSSO_EXPLICIT_EULER) return 4;
     if (p->theta_scheme < 0 || p->theta_scheme > 3) return 5;
     if (p->solver != LSSO_THOMAS_LU && p->solver != LSSO_DOUBLE_SWEEP) return 6;
     if (!(p->s_hi > p->s_lo) || !(p->v_hi > p->v_lo) || !(p->maturity > 0.0)) return 7;
@@ -457,6 +457,22 @@ static void SFX(boundary1)(const SFX(ctx) *c, const REAL *prev, REAL *bcol0, REA
     for (int t = 0; t <= N; ++t) bcolN[t] = SFX(gt_x)(&c->g, c->h1 * (REAL)t);
 }
 
+/* Explicit Euler interior (explicit_heston_scheme::rhs, solver_method/lss_heston_euler_solver_method.hpp:24-52):
+ * the heston_euler_coefficients C is gamma * C (explicit_coefficients/lss_heston_euler_coefficients.hpp:53) */
+static void SFX(euler_interior)(const SFX(ctx) *c, const REAL *in, REAL *out)
+{
+    const int nx = c->nx, ny = c->ny;
+    const REAL one = (REAL)1.0;
+    for (int r = 1; r < nx - 1; ++r)
+        for (int q = 1; q < ny - 1; ++q) {
+            const size_t o = IX(r, q);
+            const REAL C = c->gamma * c->C[o];
+            out[o] = C * in[IX(r - 1, q - 1)] + c->M[o] * in[IX(r - 1, q)] - C * in[IX(r - 1, q + 1)] +
+                     c->Mt[o] * in[IX(r, q - 1)] + (one - c->Z[o] - c->W[o]) * in[o] + c->Pt[o] * in[IX(r, q + 1)] -
+                     C * in[IX(r + 1, q - 1)] + c->P[o] * in[IX(r + 1, q)] + C * in[IX(r + 1, q + 1)];
+        }
+}
+
 /* explicit_boundary::solve #2: row S = 0 and the S_max extrapolation row (:202-238) */
 static void SFX(boundary2)(const SFX(ctx) *c, REAL *next)
 {
@@ -500,6 +516,20 @@ static int SFX(solve_impl)(const lsso_problem *p, const REAL *payoff, REAL *out)
     for (int s = 0; s < steps; ++s) {
         if (tdep && s > 0) SFX(fill_tables)(&c, time);
         SFX(boundary1)(&c, prev, bcol0, bcolN);
+        if (p->scheme == LSSO_EXPLICIT_EULER) {
+            /* heston_euler_time_loop::run (explicit_schemes/lss_heston_euler_solver_scheme.hpp:44-89): interior,
+             * then boundary #1 writes the v = v_lo and v = v_hi columns of next
+             * (explicit_boundary.hpp:181-199), then boundary #2 its first and last rows */
+            SFX(euler_interior)(&c, prev, next);
+            for (int i = 0; i < nx; ++i) {
+                next[IX(i, 0)] = bcol0[i];
+                next[IX(i, ny - 1)] = bcolN[i];
+            }
+            SFX(boundary2)(&c, next);
+            memcpy(prev, next, sizeof(REAL) * n);
+            time = p->forward ? (time + k) : (time - k);
+            continue;
+        }
         memset(Y1, 0, sizeof(REAL) * n);
         memset(Y2, 0, sizeof(REAL) * n);
         memset(Y3, 0, sizeof(REAL) * n);

@@ -24,7 +24,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liblss_oracle.so")
 REF_DRIVER = os.path.join(HERE, "_ref", "ref_driver")
 
-SCHEMES = {"dr": 0, "cs": 1, "mcs": 2, "hv": 3}
+SCHEMES = {"dr": 0, "cs": 1, "mcs": 2, "hv": 3, "euler": 4}
 THETAS = {"euler": 0, "theta30": 1, "cn": 2, "theta80": 3}
 
 

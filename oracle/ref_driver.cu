@@ -8,7 +8,7 @@
 // reference CPU baseline.  The problem is set up exactly like the reference's tests
 // (unit_tests/common/lss_print_t.hpp:1850-1974 Heston, :1976-2102 SABR).
 //
-// usage: ref_driver <f32|f64> <heston|sabr> <dr|cs|mcs|hv> <tlu|ds> nx ny nt
+// usage: ref_driver <f32|f64> <heston|sabr> <dr|cs|mcs|hv|euler> <tlu|ds> nx ny nt
 //        kappa theta_v sigma rho rate sabr_beta strike maturity s_lo s_hi v_lo v_hi
 //        zeta theta_scheme(0..3) nonuniform acc_point alpha_scale beta_scale neumann
 //        forward(0|1) repeat out.bin
@@ -120,9 +120,20 @@ template <typename T> static int run(const args_t &a)
     double secs = 0.0;
     for (int r = 0; r < a.repeat; ++r) {
         auto t0 = std::chrono::steady_clock::now();
-        pde_solver pdesolver(heat_data_ptr, discretization_ptr, vertical_upper_boundary_ptr, horizontal_boundary_pair,
-                             splitting_config_ptr, grid_config_hints_ptr, solver_cfg);
-        pdesolver.solve(solution);
+        if (a.scheme == "euler") {
+            // explicit_solvers::general_heston_equation with the host explicit Euler scheme
+            typedef two_dimensional::explicit_solvers::general_heston_equation<T, std::vector, std::allocator<T>> expl_solver;
+            auto const expl_cfg = std::make_shared<heat_explicit_solver_config>(
+                memory_space_enum::Host, a.forward ? traverse_direction_enum::Forward : traverse_direction_enum::Backward,
+                lss_enumerations::explicit_pde_schemes_enum::Euler);
+            expl_solver pdesolver(heat_data_ptr, discretization_ptr, vertical_upper_boundary_ptr, horizontal_boundary_pair,
+                                  grid_config_hints_ptr, expl_cfg);
+            pdesolver.solve(solution);
+        } else {
+            pde_solver pdesolver(heat_data_ptr, discretization_ptr, vertical_upper_boundary_ptr, horizontal_boundary_pair,
+                                 splitting_config_ptr, grid_config_hints_ptr, solver_cfg);
+            pdesolver.solve(solution);
+        }
         secs += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     }
     std::vector<T> flat(a.nx * a.ny);

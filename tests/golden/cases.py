@@ -61,4 +61,11 @@ SMALL = {
     "dr_ds_f64": (dict(CONFIG1, solver="ds", nx=33, ny=21, nt=26), "f64"),
     "sabr_ds_f64": (dict(GOLDEN["ImplSABREquationDoubleSweepSolverCrankNicolson"], nx=40, ny=24, nt=30), "f64"),
     "cs_tiny4_f64": (dict(CONFIG1, scheme="cs", nx=4, ny=4, nt=5), "f64"),
+    # explicit_solvers::general_heston_equation, host explicit Euler (stable: small time steps)
+    "euler_f64": (dict(CONFIG1, scheme="euler", rho=-0.5, nx=30, ny=20, nt=401, maturity=0.25), "f64"),
+    "euler_nu_f32": (dict(CONFIG1, scheme="euler", rho=-0.5, nx=24, ny=16, nt=301, maturity=0.2, nonuniform=True,
+                          acc_point=100.0, alpha_scale=3.0, beta_scale=50.0), "f32"),
+    "euler_fwd_f64": (dict(CONFIG1, scheme="euler", rho=-0.5, nx=20, ny=14, nt=201, maturity=0.1, forward=True), "f64"),
+    "euler_sabr_f64": (dict(GOLDEN["ImplSABREquationDoubleSweepSolverCrankNicolson"], scheme="euler", nx=22, ny=16,
+                            nt=301, maturity=0.2), "f64"),
 }

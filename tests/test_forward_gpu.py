@@ -46,7 +46,8 @@ def test_reference_arith_is_bitwise_identical_to_oracle(lss, oracle, key):
 
 
 @pytest.mark.parametrize("key", ["config1_dr_f64", "cs_nu_f64", "mcs_odd_f64", "hv_nu_f64", "hv_theta80_fwd_f64",
-                                 "dr_ds_f64", "sabr_ds_f64", "sabr_t_tlu_f64", "sabr_t_hv_fwd_f64"])
+                                 "dr_ds_f64", "sabr_ds_f64", "sabr_t_tlu_f64", "sabr_t_hv_fwd_f64", "euler_f64",
+                                 "euler_sabr_f64"])
 def test_fast_arith_within_1e10_of_oracle(lss, oracle, key):
     kw, fp = CASES[key]
     op, pp = problem_pair(kw)
