@@ -1,5 +1,6 @@
 // adi_adjoint.cuh -- reverse-mode (adjoint) of one ADI time step in the factorised form
-// used by the batched kernel, for Douglas-Rachford, Craig-Sneyd and modified Craig-Sneyd.
+// used by the batched kernel, for Douglas-Rachford, Craig-Sneyd, modified Craig-Sneyd and
+// Hundsdorfer-Verwer.
 //
 // Forward step (see adi_batched.cu): B1 -> S1 -> V1 -> S2 -> V2 -> B2, where each S/V stage
 // solves  a x_{t-1} + b x_t + c x_{t+1} = f_t  per line through the precomputed factors
@@ -25,9 +26,10 @@ struct adj_acc {
     double vk, vt, vs1, vs2, vb;
 };
 
-// B2^T: fold the S_max extrapolation row into rows nx-2 / nx-3; clear rows 0 and nx-1 of UB.
-__device__ __forceinline__ void adj_b2(const inst_view<double> &v, double *__restrict__ VB, double *__restrict__ UB, int l0,
-                                       int ls)
+// B2^T: fold the S_max extrapolation row into rows nx-2 / nx-3; clear rows 0 and nx-1 of UB
+// (all of UB for Hundsdorfer-Verwer, whose last v stage feeds Y2B instead of UB).
+__device__ __forceinline__ void adj_b2(const inst_view<double> &v, double *__restrict__ VB, double *__restrict__ UB,
+                                       bool clear_all, int l0, int ls)
 {
     const int nx = v.nx, ny = v.ny, lri = nx - 1;
     const double four3 = 4.0 / 3.0, third = 1.0 / 3.0;
@@ -37,8 +39,12 @@ __device__ __forceinline__ void adj_b2(const inst_view<double> &v, double *__res
         if (q + 1 < ny && __ldg(v.jmap() + q + 1) == q) add += VB[(long long)lri * ny + q + 1];
         VB[(long long)(lri - 1) * ny + q] += four3 * add;
         VB[(long long)(lri - 2) * ny + q] -= third * add;
-        UB[q] = 0.0;
-        UB[(long long)lri * ny + q] = 0.0;
+        if (clear_all) {
+            for (int p = 0; p < nx; ++p) UB[(long long)p * ny + q] = 0.0;
+        } else {
+            UB[q] = 0.0;
+            UB[(long long)lri * ny + q] = 0.0;
+        }
     }
 }
 
@@ -97,8 +103,10 @@ __device__ __forceinline__ void adj_v(const inst_view<double> &v, const double *
 }
 
 // S-line stage adjoint.  KIND 1: S1 (explicit operator on U, output Y1).  KIND 2: second S
-// stage of CS/MCS (output Y3).  XB: adjoint of the stage output; FB receives the scaled
-// right-hand-side adjoint w; LS/HS the lo/hi adjoints of the line.
+// stage of CS/MCS/HV (output Y3).  XB: adjoint of the stage output; FB receives the scaled
+// right-hand-side adjoint w; LS/HS the lo/hi adjoints of the line.  The along-line terms of
+// the second stage act on U for CS/MCS and on Y1 for HV, whose right-hand side is
+// (I - theta k A1) Y1 + (zeta k A - theta k A1)(Y2 - U) (hundsdorfer_verwer_method.hpp:128-194).
 template <int KIND>
 __device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d, const double *__restrict__ U,
                                       const double *__restrict__ Y1, const double *__restrict__ Y2,
@@ -110,7 +118,9 @@ __device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d
     const int nx = v.nx, ny = v.ny, e = nx - 2;
     const bool sabr = d.model == LSS_ADI_SABR;
     const double th = d.a_theta;
-    const double zt = (d.scheme == LSS_ADI_MODIFIED_CRAIG_SNEYD) ? (d.a_zeta - th) : 0.0;
+    const bool hv = d.scheme == LSS_ADI_HUNDSDORFER_VERWER;
+    // weight of the extra Delta = Y2 - U terms: zeta - theta (MCS), zeta (HV), none (CS)
+    const double zt = (d.scheme == LSS_ADI_MODIFIED_CRAIG_SNEYD) ? (d.a_zeta - th) : hv ? d.a_zeta : 0.0;
     for (int j = 1 + l0; j <= ny - 2; j += ls) {
         double z = 0.0;
 #pragma unroll 4
@@ -145,14 +155,25 @@ __device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d
                 sPt = Un;
                 sC = d.a_gamma * ((U[o - ny - 1] - U[o - ny + 1]) + (U[o + ny + 1] - U[o + ny - 1]));
             } else {
-                // along-line terms of the second S stage: la U(t-1) + sc U(t) + se U(t+1) + ib Y1(t)
+                // along-line terms of the second S stage: la A(t-1) + sc A(t) + se A(t+1) (+ ib Y1(t)),
+                // A = U for CS/MCS, A = Y1 for HV (its rows are written once here: no accumulation)
                 const double sc = __ldg(v.S(SL_S2SC) + o), se = __ldg(v.S(SL_S2SE) + o);
                 const double fin = acc_t1 + se * w;
-                UB[o + ny] += fin;
                 acc_t1 = acc_t + sc * w;
                 acc_t = la * w;
-                Y1B[o] = mu;
-                if (zt != 0.0) {
+                if (hv) {
+                    Y1B[o + ny] = fin;
+                    const double Dw = Y2[o - ny] - Uw, Dc = Y2[o] - Uc, De = Y2[o + ny] - Ue;
+                    const double Ds = Y2[o - 1] - Us, Dn = Y2[o + 1] - Un;
+                    sM = th * (Yo[o - ny] - Y1[o - ny] - Dw) + zt * Dw;
+                    sZ = -th * (Yo[o] - Y1[o] - Dc) - zt * Dc;
+                    sP = th * (Yo[o + ny] - Y1[o + ny] - De) + zt * De;
+                    sW = -zt * Dc;
+                    sMt = zt * Ds;
+                    sPt = zt * Dn;
+                } else if (zt != 0.0) {
+                    UB[o + ny] += fin;
+                    Y1B[o] = mu;
                     const double Dw = Y2[o - ny] - Uw, Dc = Y2[o] - Uc, De = Y2[o + ny] - Ue;
                     const double Ds = Y2[o - 1] - Us, Dn = Y2[o + 1] - Un;
                     sM = th * (Yo[o - ny] - Uw) + zt * Dw;
@@ -163,6 +184,8 @@ __device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d
                     sPt = zt * Dn;
                 } else {
                     // Craig-Sneyd: no extra term, only M, Z, P, C depend on this stage's residual
+                    UB[o + ny] += fin;
+                    Y1B[o] = mu;
                     sM = th * (Yo[o - ny] - Uw);
                     sZ = -th * (Yo[o] - Uc);
                     sP = th * (Yo[o + ny] - Ue);
@@ -188,8 +211,13 @@ __device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d
             la_next = la;
         }
         if constexpr (KIND == 2) {
-            UB[(long long)ny + j] += acc_t1;
-            UB[j] += acc_t;
+            if (hv) {
+                Y1B[(long long)ny + j] = acc_t1;
+                Y1B[j] = acc_t;
+            } else {
+                UB[(long long)ny + j] += acc_t1;
+                UB[j] += acc_t;
+            }
         }
         LS[j] = -la_next * w + XB[j];
         HS[j] = -__ldg(v.Yv(Y_CHS) + j) * w_e + XB[(long long)(nx - 1) * ny + j];
@@ -242,10 +270,11 @@ __device__ __forceinline__ void adj_gather(const inst_view<double> &v, const bde
             if constexpr (KIND == 2) {
                 double db = W(SL_S2MZ, p + 1, q + 1) * F(p + 1, q + 1) - W(SL_S2MZ, p + 1, q - 1) * F(p + 1, q - 1) -
                             W(SL_S2MZ, p - 1, q + 1) * F(p - 1, q + 1) + W(SL_S2MZ, p - 1, q - 1) * F(p - 1, q - 1);
-                if (d.scheme == LSS_ADI_MODIFIED_CRAIG_SNEYD)
+                if (d.scheme != LSS_ADI_CRAIG_SNEYD)
                     db += W(SL_X1, p + 1, q) * F(p + 1, q) + W(SL_X2, p, q) * F(p, q) + W(SL_X3, p - 1, q) * F(p - 1, q) +
                           W(SL_X4, p, q + 1) * F(p, q + 1) + W(SL_X5, p, q - 1) * F(p, q - 1);
-                Y2B[o] = db;
+                // HV: rows 1..nx-2 already hold the last v stage's adjoint of its input Y2
+                if (d.scheme == LSS_ADI_HUNDSDORFER_VERWER && p >= 1 && p <= nx - 2) Y2B[o] += db; else Y2B[o] = db;
                 val -= db;
             } else {
                 val += W(SL_WW, p + 1, q) * F(p + 1, q) + W(SL_WE, p - 1, q) * F(p - 1, q) +
@@ -294,13 +323,18 @@ __device__ __forceinline__ void adj_step(const inst_view<double> &v, const bdesc
                                          double *LS, double *HS, adj_acc &acc, double tau)
 {
     const int l0 = threadIdx.x;
-    adj_b2(v, VB, UB, l0, BS);
+    const bool hv = d.scheme == LSS_ADI_HUNDSDORFER_VERWER;
+    adj_b2(v, VB, UB, hv, l0, BS);
     __syncthreads();
     if (d.scheme == LSS_ADI_DOUGLAS_RACHFORD) {
         adj_v<true>(v, U, Vo, VB, UB, Y1B, TMP, LV, acc, l0, BS);
         __syncthreads();
     } else {
-        adj_v<true>(v, U, Vo, VB, UB, Y3B, TMP, LV, acc, l0, BS);
+        // last v stage: in = U (CS/MCS) or Y2 (HV)
+        if (hv)
+            adj_v<true>(v, Y2, Vo, VB, Y2B, Y3B, TMP, LV, acc, l0, BS);
+        else
+            adj_v<true>(v, U, Vo, VB, UB, Y3B, TMP, LV, acc, l0, BS);
         __syncthreads();
         adj_s<2>(v, d, U, Y1, Y2, Y3, Y3B, FB, TMP, LS, HS, UB, Y1B, acc, tau, l0, BS);
         __syncthreads();

@@ -823,7 +823,7 @@ __global__ void k_wadj_b2(const __grid_constant__ bparams<double> p, double *VB,
 {
     const bdesc d = p.desc[0];
     const inst_view<double> v = make_view(p, d);
-    adj_b2(v, VB, UB, gtid(), gstride());
+    adj_b2(v, VB, UB, d.scheme == LSS_ADI_HUNDSDORFER_VERWER, gtid(), gstride());
 }
 
 template <bool FIRST>
@@ -962,7 +962,7 @@ template <typename T> struct batch_typed {
     int grid_blocks = 0;
     long long launches = 0;
     // forward + adjoint
-    bool adjoint_ok = false;      // FP64 DR/CS/MCS, Heston and SABR with r = 0
+    bool adjoint_ok = false;      // FP64, Heston and SABR with r = 0
     std::string adjoint_why;
     int ck_override = 0;          // checkpoint interval (0 = ceil(sqrt(steps)))
     int grid_adj = 0;                 // CTAs the workspace has slices for
@@ -1202,7 +1202,7 @@ template <typename T> int batch_typed<T>::create(const lss_adi_problem *ps, int 
     adjoint_why = adjoint_ok ? "" : "the adjoint is FP64 only";
     for (int k = 0; k < n && adjoint_ok; ++k) {
         if (time_dependent(ps[k])) { adjoint_ok = false; adjoint_why = "no adjoint for SABR with r != 0"; }
-        if (ps[k].scheme == LSS_ADI_HUNDSDORFER_VERWER) { adjoint_ok = false; adjoint_why = "no adjoint for Hundsdorfer-Verwer yet"; }
+
     }
 
     // factorise on the device from the base tables
@@ -1610,7 +1610,10 @@ template <typename T> int batch_typed<T>::enqueue_wide_adjoint(cudaStream_t s)
                     k_wadj_v<true><<<grid, threads, 0, s>>>(p, um, Vo, vb, ub, Y1B, TMP, LV, ACC);
                     nl += 2;
                 } else {
-                    k_wadj_v<true><<<grid, threads, 0, s>>>(p, um, Vo, vb, ub, Y3B, TMP, LV, ACC);
+                    if (d.scheme == LSS_ADI_HUNDSDORFER_VERWER)
+                        k_wadj_v<true><<<grid, threads, 0, s>>>(p, Y2, Vo, vb, Y2B, Y3B, TMP, LV, ACC);
+                    else
+                        k_wadj_v<true><<<grid, threads, 0, s>>>(p, um, Vo, vb, ub, Y3B, TMP, LV, ACC);
                     k_wadj_s<2><<<grid, threads, 0, s>>>(p, um, Y1, Y2, Y3, Y3B, FB, TMP, LS, HS, ub, Y1B, ACC, tau);
                     k_wadj_gather<2><<<grid, threads, 0, s>>>(p, um, FB, LS, HS, LV, ub, Y2B, ACC, tau);
                     k_wadj_v<false><<<grid, threads, 0, s>>>(p, um, Y2, Y2B, ub, Y1B, TMP, LV, ACC);
@@ -1779,8 +1782,6 @@ adjoint_solver::~adjoint_solver() = default;
 
 int adjoint_solver::init(const lss_adi_problem &p)
 {
-    if (p.scheme == LSS_ADI_HUNDSDORFER_VERWER)
-        return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_adjoint: no adjoint for Hundsdorfer-Verwer yet");
     if (p.scheme == LSS_ADI_EXPLICIT_EULER)
         return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_adjoint: no adjoint for the explicit Euler scheme");
     if (time_dependent(p))

@@ -72,10 +72,15 @@ CASES = {
     "sabr_dr": dict(SABR, scheme="dr", nx=48, ny=26, nt=31),
     "sabr_cs": dict(SABR, scheme="cs", nx=44, ny=24, nt=25, rho=0.3),
     "sabr_mcs_z08": dict(SABR, scheme="mcs", zeta=0.8, theta_scheme="theta80", nx=40, ny=22, nt=21),
+    # Hundsdorfer-Verwer: the second S stage acts on Y1 along the line, the last v stage on Y2
+    "hv_60x30": dict(BASE, scheme="hv", nx=60, ny=30, nt=31),
+    "hv_z07_theta80": dict(BASE, scheme="hv", zeta=0.7, theta_scheme="theta80", nx=50, ny=28, nt=21, rho=-0.2),
+    "sabr_hv": dict(SABR, scheme="hv", nx=46, ny=24, nt=21),
     # large instances: the adjoint runs as one kernel per stage over the whole GPU
     "wide_heston_cs": dict(BASE, scheme="cs", nx=300, ny=64, nt=21, rho=-0.3),
     "wide_heston_mcs": dict(BASE, scheme="mcs", zeta=1.0 / 3.0, nx=264, ny=160, nt=9, rho=-0.2),
     "wide_sabr_dr": dict(SABR, scheme="dr", nx=280, ny=90, nt=17),
+    "wide_heston_hv": dict(BASE, scheme="hv", nx=300, ny=70, nt=13),
 }
 
 
@@ -91,7 +96,7 @@ def test_parameter_gradients_match_device_finite_differences(lss, key):
 
 
 @pytest.mark.parametrize("key", ["mcs_64x32", "dr_70x35", "mcs_z08_cn", "sabr_dr", "sabr_mcs_z08", "wide_heston_cs",
-                                 "wide_sabr_dr"])
+                                 "wide_sabr_dr", "hv_60x30", "sabr_hv", "wide_heston_hv"])
 def test_parameter_gradients_match_reference_bump_and_revalue(lss, oracle, key):
     p = lss.HestonProblem(**CASES[key])
     val, grads, _ = lss.ImplicitHestonSolver(p, precision="f64", arith="fast").adjoint(want_payoff_grad=False)
@@ -100,7 +105,8 @@ def test_parameter_gradients_match_reference_bump_and_revalue(lss, oracle, key):
         assert abs(grads[k] - fd) <= 1e-6 * max(abs(fd), 1e-3 * abs(val)), (name, grads[k], fd)
 
 
-@pytest.mark.parametrize("key", ["mcs_64x32", "cs_60x30", "dr_70x35", "sabr_cs", "wide_heston_mcs"])
+@pytest.mark.parametrize("key", ["mcs_64x32", "cs_60x30", "dr_70x35", "sabr_cs", "wide_heston_mcs", "hv_60x30",
+                                 "wide_heston_hv"])
 def test_payoff_gradient_is_the_linear_response(lss, key):
     p = lss.HestonProblem(**CASES[key])
     s = lss.ImplicitHestonSolver(p, precision="f64", arith="fast")
@@ -115,7 +121,7 @@ def test_payoff_gradient_is_the_linear_response(lss, key):
     assert abs((v1 - v0) - pred) <= 1e-9 * max(1.0, np.sum(np.abs(lam * delta)))
 
 
-@pytest.mark.parametrize("key", ["mcs_64x32", "wide_heston_cs"])
+@pytest.mark.parametrize("key", ["mcs_64x32", "wide_heston_cs", "hv_60x30"])
 def test_checkpoint_interval_does_not_change_results(lss, key):
     p = lss.HestonProblem(**CASES[key])
     s = lss.ImplicitHestonSolver(p, precision="f64", arith="fast")
