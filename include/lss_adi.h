@@ -176,8 +176,11 @@ int lss_adi_forward_graph(lss_adi_handle *h, const void *payoff, void *out_surfa
 
 /* Adjoint of the whole forward solve (no counterpart in the reference, which has no
  * sensitivities): returns out_value = V(eval_s, eval_v), dV/d(kappa, theta, sigma, rho, r)
- * in dv_dparams[5] (host doubles; Heston only) and dV/d(payoff grid) in dv_dpayoff (Nx*Ny,
- * may be NULL).  Checkpoints every `checkpoint_every` steps (0 = ~sqrt(steps)). */
+ * in dv_dparams[5] (host doubles; for SABR sigma is nu and kappa, theta give 0) and
+ * dV/d(payoff grid) in dv_dpayoff (Nx*Ny, may be NULL).  FP64, all four splittings, Heston
+ * and SABR with r = 0 (the r sensitivity includes the discount factors D(t)).  Instances
+ * larger than 256 x 160 points run the adjoint as one kernel per stage over the whole GPU.
+ * Checkpoints every `checkpoint_every` steps (0 = ~sqrt(steps)). */
 int lss_adi_adjoint(lss_adi_handle *h, const void *payoff, double *out_value, double *dv_dparams,
                     void *dv_dpayoff, int checkpoint_every, int flags, void *stream);
 
@@ -202,7 +205,8 @@ void lss_adi_destroy(lss_adi_handle *h);
 int lss_adi_batch_create(const lss_adi_problem *problems, int count, lss_adi_batch **b);
 
 /* mode 0 = forward values only, 1 = forward + adjoint (values, the 5 parameter
- * sensitivities and dV/d(initial condition) per instance; FP64 Heston with DR, CS or MCS).
+ * sensitivities and dV/d(initial condition) per instance; FP64, every splitting, Heston and
+ * SABR with r = 0).
  * The adjoint keeps a checkpoint every ceil(sqrt(steps)) steps and recomputes each segment
  * once.  Device-resident: inputs were uploaded by batch_create. */
 int lss_adi_batch_run(lss_adi_batch *b, int mode, void *stream);

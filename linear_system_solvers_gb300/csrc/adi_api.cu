@@ -172,8 +172,8 @@ int lss_adi_adjoint(lss_adi_handle *h, const void *payoff, double *out_value, do
 {
     clear_error();
     if (!h) return set_error(LSS_ADI_EINVAL, "lss_adi_adjoint: null handle");
-    if (!h->parametric || h->prob.model != LSS_ADI_HESTON || h->precision != LSS_ADI_FP64)
-        return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_adjoint: parametric FP64 Heston problems only");
+    if (!h->parametric || h->precision != LSS_ADI_FP64)
+        return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_adjoint: parametric FP64 problems only");
     if (checkpoint_every < 0) return set_error(LSS_ADI_EINVAL, "lss_adi_adjoint: checkpoint_every must be >= 0");
     if (!h->adj) {
         std::unique_ptr<adjoint_solver> a(new (std::nothrow) adjoint_solver());
