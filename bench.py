@@ -45,7 +45,7 @@ def parse():
     ap.add_argument("--max-time-steps", type=int, default=0,
                     help="cap every instance's time loop (a smaller workload for profiler captures; 0 = no cap)")
     ap.add_argument("--configs", default="", help="comma list of configurations to measure instead of the batched "
-                    "headline: c1, c2, c4, c5, c5sabr, mcsz (one JSON line each)")
+                    "headline: c1, c2, c4, c5, c5sabr, mcsz, euler (one JSON line each)")
     return ap.parse_args()
 
 
@@ -468,6 +468,30 @@ def run_configs(args):
         for fp in ("f64", "f32"):
             p = lss.HestonProblem(**dict(CONFIG1, scheme="hv", nx=4096, ny=2048, nt=1001, **NU_K100))
             case("config5 HV 4096x2048x1000", p, fp, 1, oracle_nt=11)
+    if "euler" in wanted:
+        # explicit Euler (explicit_solvers::general_heston_equation): 200 x 100, 8000 steps, T = 0.25
+        p = lss.HestonProblem(**dict(CONFIG1, scheme="euler", nx=200, ny=100, nt=8001, maturity=0.25))
+        op = oracle_problem(p)
+        t0 = time.perf_counter()
+        want = O.solve(op, "f64")
+        cpu_s = time.perf_counter() - t0
+        gps = p.nx * p.ny * (p.nt - 1)
+        for arith in ("reference", "fast"):
+            sv = lss.ImplicitHestonSolver(p, precision="f64", arith=arith)
+            secs, surf, val = _time_solver(sv, 3)
+            rec = {"config": "explicit Euler 200x100x8000", "arith": arith, "device_gps": gps / secs,
+                   "device_seconds": secs, "value": val, "path": "kernel per step, graph",
+                   "cpu_oracle_gps_1core": gps / cpu_s}
+            if arith == "reference":
+                rec["bitwise_equal_oracle"] = bool(np.array_equal(surf, want))
+            else:
+                rec["rel_err_vs_fp64_oracle"] = _rel_err(surf, want)
+            print(json.dumps(rec), flush=True)
+        if O.reference_available():
+            ref_p = oracle_problem(p, 201)
+            _, ref_s = O.run_reference(ref_p, "f64")
+            print(json.dumps({"config": "explicit Euler 200x100x8000", "path": "reference host Euler (compiled), "
+                              "first 200 steps", "cpu_reference_gps_1core": p.nx * p.ny * 200 / ref_s}), flush=True)
     if "mcsz" in wanted:
         # the batch of the headline with a genuine modified Craig-Sneyd weight (zeta = 1/3 != theta):
         # the full MCS stencil, forward and forward + adjoint
