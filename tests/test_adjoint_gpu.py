@@ -1,11 +1,13 @@
 """Adjoint (lss_adi_adjoint / batch mode 1) against finite differences and linearity.
 
 The reference has no sensitivities; its forward path is the check: dV/d(kappa, theta, sigma,
-rho, r) against Richardson-extrapolated central finite differences (relative bumps 1e-5 and
-5e-6, error O(h^4): the reference's genuine modified Craig-Sneyd scheme (zeta != theta) grows
-by orders of magnitude per step, so a plain central difference of it carries a relative
-truncation error near 1e-5) of (a) the device forward and (b) the CPU oracle (bit-exact with
-the reference's Thomas-LU path), and dV/d(payoff grid) against the exact linearity of the scheme in the terminal condition.
+rho, r) against Richardson-extrapolated central finite differences of (a) the device forward
+and (b) the CPU oracle (bit-exact with the reference's Thomas-LU path), and dV/d(payoff grid)
+against the exact linearity of the scheme in the terminal condition.  Bumps: relative 1e-5
+and 5e-6 (Heston), 1e-4 and 5e-5 (SABR); the extrapolation (error O(h^4)) is needed because
+the reference's genuine modified Craig-Sneyd scheme (zeta != theta) grows by orders of
+magnitude per step, so a plain central difference of it carries a relative truncation error
+near 1e-5.
 """
 import dataclasses
 
@@ -37,7 +39,9 @@ def bilinear_value(surface, x, y, s0, v0):
 
 
 def device_value(lss, p):
-    return lss.ImplicitHestonSolver(p, precision="f64", arith="fast").solve()[1]
+    # thread-per-line solves: the autotuned chunk counts of a large instance may differ between
+    # the bumped problems, which would put rounding noise into the differences
+    return lss.ImplicitHestonSolver(dataclasses.replace(p, line_per_thread=True), precision="f64", arith="fast").solve()[1]
 
 
 def oracle_value(oracle, lss, p):
@@ -48,7 +52,7 @@ def oracle_value(oracle, lss, p):
     return bilinear_value(surf, x, y, p.eval_s, p.eval_v)
 
 
-def fd_grad(fn, p, name, rel=1e-5):
+def fd_grad(fn, p, name, rel=None):
     base = getattr(p, name)
 
     def central(h):
@@ -56,7 +60,11 @@ def fd_grad(fn, p, name, rel=1e-5):
         dn = dataclasses.replace(p, **{name: base - h})
         return (fn(up) - fn(dn)) / (2 * h)
 
-    h = rel * (abs(base) if base != 0.0 else 1e-2)  # r = 0: absolute bump 1e-7
+    if rel is None:
+        # SABR sensitivities are ~1e-2 of the value: a larger bump keeps the rounding noise of the
+        # differences (value x 1e-14 / h) well below 1e-6 of them
+        rel = 1e-4 if p.model == "sabr" else 1e-5
+    h = rel * (abs(base) if base != 0.0 else 1e-2)  # r = 0: absolute bump rel x 1e-2
     return (4.0 * central(h / 2) - central(h)) / 3.0
 
 
