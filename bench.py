@@ -524,7 +524,8 @@ def run_configs(args):
                               eval_v=0.2)
         case("config5 SABR DR 2048x1024x800", p, "f64", 1, oracle_nt=11)
         # forward + adjoint: dV/d(nu, rho, r) and dV/d(payoff) in one backward pass; nu and rho
-        # checked against Richardson central differences (bumps 1e-5, 5e-6) of the device forward
+        # checked against Richardson central differences (relative bumps 1e-4, 5e-5: the
+        # sensitivities are ~1e-2 of the value) of the device forward, thread-per-line solves
         s = lss.ImplicitHestonSolver(p, precision="f64", arith="fast")
         s.adjoint(want_payoff_grad=False)
         torch.cuda.synchronize()
@@ -534,13 +535,14 @@ def run_configs(args):
         secs = time.perf_counter() - t0
 
         def fwd(q):
+            q = dataclasses.replace(q, line_per_thread=True)
             return lss.ImplicitHestonSolver(q, precision="f64", arith="fast").solve()[1]
 
         errs = {}
         for idx, name in ((2, "sigma"), (3, "rho")):
             base = getattr(p, name)
             cd = []
-            for rel in (1e-5, 5e-6):
+            for rel in (1e-4, 5e-5):
                 h = rel * abs(base)
                 cd.append((fwd(dataclasses.replace(p, **{name: base + h})) -
                            fwd(dataclasses.replace(p, **{name: base - h}))) / (2 * h))
@@ -549,7 +551,7 @@ def run_configs(args):
         print(json.dumps({"config": "config5 SABR DR 2048x1024x800 forward + adjoint", "device_gps_fwd_adj":
                           p.nx * p.ny * (p.nt - 1) / secs, "device_seconds": secs, "value": val,
                           "dV_dnu": grads[2], "dV_drho": grads[3], "dV_dr": grads[4],
-                          "rel_err_vs_device_fd": errs, "fd": "Richardson central, bumps 1e-5 / 5e-6, device forward"}),
+                          "rel_err_vs_device_fd": errs, "fd": "Richardson central, bumps 1e-4 / 5e-5, device forward"}),
               flush=True)
 
 
