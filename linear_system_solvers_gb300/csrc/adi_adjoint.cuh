@@ -48,6 +48,18 @@ __device__ __forceinline__ void adj_b2(const inst_view<double> &v, double *__res
     }
 }
 
+// Parameter sums of one v-line point: mu = ib * w, dm / dc / dn = (in - out) at t-1, t, t+1.
+__device__ __forceinline__ void adj_v_sum(const inst_view<double> &v, int t, double mu, double dm, double dc, double dn,
+                                          adj_acc &acc)
+{
+    const double q = mu * (dm - dn);
+    acc.vk += q * __ldg(v.Yv(Y_EK) + t);
+    acc.vt += q * __ldg(v.Yv(Y_ET) + t);
+    acc.vs1 += q * __ldg(v.Yv(Y_ES) + t);
+    acc.vs2 += mu * (2.0 * dc - dm - dn) * __ldg(v.Yv(Y_BS) + t);
+    acc.vb += mu * dc;
+}
+
 // V-line stage adjoint.  XB: adjoint of the stage output (rows i, incl. the lo copy at t=0);
 // in/out: the stage's `in` array and its output; INB (+)= adjoint of `in`; INHB (+)= adjoint
 // of `inh`; LV (+)= adjoint of the line's lo value.
@@ -85,12 +97,7 @@ __device__ __forceinline__ void adj_v(const inst_view<double> &v, const double *
             const double mu = ib * w;
             if (FIRST) INHB[row + t] = mu; else INHB[row + t] += mu;
             const double dm = in[row + t - 1] - out[row + t - 1];
-            const double q = mu * (dm - dn);
-            acc.vk += q * __ldg(v.Yv(Y_EK) + t);
-            acc.vt += q * __ldg(v.Yv(Y_ET) + t);
-            acc.vs1 += q * __ldg(v.Yv(Y_ES) + t);
-            acc.vs2 += mu * (2.0 * dc - dm - dn) * __ldg(v.Yv(Y_BS) + t);
-            acc.vb += mu * dc;
+            adj_v_sum(v, t, mu, dm, dc, dn, acc);
             dn = dc;
             dc = dm;
             la_next = la;
@@ -100,6 +107,96 @@ __device__ __forceinline__ void adj_v(const inst_view<double> &v, const double *
         const double lob = -la_next * w + XB[row];
         if (FIRST) LV[i] = lob; else LV[i] += lob;
     }
+}
+
+// d(residual)/d(coefficient) at one S-stage point o (row t of line j): M, Z, P, M~, W, P~, C.
+// KIND 1: the first stage on U with output Yo = Y1.  KIND 2: the second stage, whose extra
+// terms on Delta = Y2 - U carry the weight zt (zeta - theta for MCS, zeta for HV, 0 for CS).
+struct s_terms {
+    double M, Z, P, Mt, W, Pt, C;
+};
+template <int KIND>
+__device__ __forceinline__ s_terms adj_s_terms(const bdesc &d, long long o, int ny, const double *__restrict__ U,
+                                               const double *__restrict__ Y1, const double *__restrict__ Y2,
+                                               const double *__restrict__ Yo, double th, double zt, bool hv)
+{
+    s_terms r;
+    const double Uw = U[o - ny], Uc = U[o], Ue = U[o + ny], Us = U[o - 1], Un = U[o + 1];
+    if constexpr (KIND == 1) {
+        const double omt = 1.0 - th;
+        r.M = omt * Uw + th * Yo[o - ny];
+        r.Z = -(omt * Uc + th * Yo[o]);
+        r.P = omt * Ue + th * Yo[o + ny];
+        r.Mt = Us;
+        r.W = -Uc;
+        r.Pt = Un;
+        r.C = d.a_gamma * ((U[o - ny - 1] - U[o - ny + 1]) + (U[o + ny + 1] - U[o + ny - 1]));
+    } else {
+        if (hv) {
+            const double Dw = Y2[o - ny] - Uw, Dc = Y2[o] - Uc, De = Y2[o + ny] - Ue;
+            r.M = th * (Yo[o - ny] - Y1[o - ny] - Dw) + zt * Dw;
+            r.Z = -th * (Yo[o] - Y1[o] - Dc) - zt * Dc;
+            r.P = th * (Yo[o + ny] - Y1[o + ny] - De) + zt * De;
+            r.W = -zt * Dc;
+            r.Mt = zt * (Y2[o - 1] - Us);
+            r.Pt = zt * (Y2[o + 1] - Un);
+        } else if (zt != 0.0) {
+            const double Dw = Y2[o - ny] - Uw, Dc = Y2[o] - Uc, De = Y2[o + ny] - Ue;
+            r.M = th * (Yo[o - ny] - Uw) + zt * Dw;
+            r.Z = -th * (Yo[o] - Uc) - zt * Dc;
+            r.P = th * (Yo[o + ny] - Ue) - zt * De; // the reference's sign of the P term
+            r.W = -zt * Dc;
+            r.Mt = zt * (Y2[o - 1] - Us);
+            r.Pt = zt * (Y2[o + 1] - Un);
+        } else {
+            // Craig-Sneyd: no extra term, only M, Z, P, C depend on this stage's residual
+            r.M = th * (Yo[o - ny] - Uw);
+            r.Z = -th * (Yo[o] - Uc);
+            r.P = th * (Yo[o + ny] - Ue);
+            r.W = 0.0;
+            r.Mt = 0.0;
+            r.Pt = 0.0;
+        }
+        const double mix = ((Y2[o - ny - 1] - U[o - ny - 1]) - (Y2[o - ny + 1] - U[o - ny + 1])) +
+                           ((Y2[o + ny + 1] - U[o + ny + 1]) - (Y2[o + ny - 1] - U[o + ny - 1]));
+        r.C = d.a_zeta * d.a_gamma * mix;
+    }
+    return r;
+}
+
+// Line sums of mu * d(residual)/d(parameter) pieces of an S line (the S-direction factors of the
+// coefficient derivatives applied per point; the v-direction ones once per line, adj_s_line).
+struct s_sums {
+    double A, B, Q, D, E, Aa, Dd;
+};
+__device__ __forceinline__ void adj_s_sum(const inst_view<double> &v, s_sums &p, const s_terms &s, double mu, int t,
+                                          bool vterms, bool sabr)
+{
+    p.A += mu * __ldg(v.X(X_HX) + t) * (s.P - s.M);
+    p.B += mu * (s.Z + s.W);
+    if (vterms) {
+        p.Q += mu * (s.Pt - s.Mt);
+        p.D += mu * (s.Mt + s.Pt + 2.0 * s.W);
+    }
+    p.E += mu * __ldg(v.X(X_HC) + t) * s.C;
+    if (sabr) {
+        p.Aa += mu * __ldg(v.X(X_HA) + t) * (s.M + s.P + 2.0 * s.Z);
+        p.Dd += mu * __ldg(v.X(X_HDD) + t) * (s.P - s.M);
+    }
+}
+__device__ __forceinline__ void adj_s_line(const inst_view<double> &v, const bdesc &d, int j, const s_sums &p,
+                                           double tau, bool sabr, adj_acc &acc)
+{
+    const double ek = __ldg(v.Yv(Y_EK) + j), et = __ldg(v.Yv(Y_ET) + j), es = __ldg(v.Yv(Y_ES) + j);
+    const double bs = __ldg(v.Yv(Y_BS) + j), hy = __ldg(v.Yv(Y_HY) + j);
+    acc.s[0] += d.a_delta * p.A + d.a_halfk * p.B;
+    if (sabr) // D(t) terms of a^, d^ and c^
+        acc.s[0] += tau * d.a_omb *
+                    (__ldg(v.Yv(Y_HV2) + j) * (2.0 * d.a_delta * p.Dd - 2.0 * d.a_alphat * p.Aa) - d.a_rho * d.a_sigma * hy * p.E);
+    acc.s[1] += d.a_ni * ek * p.Q;
+    acc.s[2] += d.a_ni * et * p.Q;
+    acc.s[3] += d.a_ni * es * p.Q + d.a_betat * bs * p.D + d.a_rho * hy * p.E;
+    acc.s[4] += d.a_sigma * hy * p.E;
 }
 
 // S-line stage adjoint.  KIND 1: S1 (explicit operator on U, output Y1).  KIND 2: second S
@@ -132,7 +229,7 @@ __device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d
         }
         double w = 0.0, la_next = 0.0, w_e = 0.0;
         double acc_t1 = 0.0, acc_t = 0.0;
-        double pA = 0.0, pB = 0.0, pQ = 0.0, pD = 0.0, pE = 0.0, pAa = 0.0, pDd = 0.0;
+        s_sums ps = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
 #pragma unroll 2
         for (int t = e; t >= 1; --t) {
             const long long o = (long long)t * ny + j;
@@ -142,19 +239,7 @@ __device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d
             const double la = __ldg(v.S(SL_LA) + o);
             const double ib = __ldg(v.S(SL_IB) + o);
             const double mu = ib * w;
-            const double hx = __ldg(v.X(X_HX) + t);
-            const double Uw = U[o - ny], Uc = U[o], Ue = U[o + ny], Us = U[o - 1], Un = U[o + 1];
-            double sM, sZ, sP, sMt, sW, sPt, sC;
-            if constexpr (KIND == 1) {
-                const double omt = 1.0 - th;
-                sM = omt * Uw + th * Yo[o - ny];
-                sZ = -(omt * Uc + th * Yo[o]);
-                sP = omt * Ue + th * Yo[o + ny];
-                sMt = Us;
-                sW = -Uc;
-                sPt = Un;
-                sC = d.a_gamma * ((U[o - ny - 1] - U[o - ny + 1]) + (U[o + ny + 1] - U[o + ny - 1]));
-            } else {
+            if constexpr (KIND == 2) {
                 // along-line terms of the second S stage: la A(t-1) + sc A(t) + se A(t+1) (+ ib Y1(t)),
                 // A = U for CS/MCS, A = Y1 for HV (its rows are written once here: no accumulation)
                 const double sc = __ldg(v.S(SL_S2SC) + o), se = __ldg(v.S(SL_S2SE) + o);
@@ -163,51 +248,13 @@ __device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d
                 acc_t = la * w;
                 if (hv) {
                     Y1B[o + ny] = fin;
-                    const double Dw = Y2[o - ny] - Uw, Dc = Y2[o] - Uc, De = Y2[o + ny] - Ue;
-                    const double Ds = Y2[o - 1] - Us, Dn = Y2[o + 1] - Un;
-                    sM = th * (Yo[o - ny] - Y1[o - ny] - Dw) + zt * Dw;
-                    sZ = -th * (Yo[o] - Y1[o] - Dc) - zt * Dc;
-                    sP = th * (Yo[o + ny] - Y1[o + ny] - De) + zt * De;
-                    sW = -zt * Dc;
-                    sMt = zt * Ds;
-                    sPt = zt * Dn;
-                } else if (zt != 0.0) {
-                    UB[o + ny] += fin;
-                    Y1B[o] = mu;
-                    const double Dw = Y2[o - ny] - Uw, Dc = Y2[o] - Uc, De = Y2[o + ny] - Ue;
-                    const double Ds = Y2[o - 1] - Us, Dn = Y2[o + 1] - Un;
-                    sM = th * (Yo[o - ny] - Uw) + zt * Dw;
-                    sZ = -th * (Yo[o] - Uc) - zt * Dc;
-                    sP = th * (Yo[o + ny] - Ue) - zt * De;
-                    sW = -zt * Dc;
-                    sMt = zt * Ds;
-                    sPt = zt * Dn;
                 } else {
-                    // Craig-Sneyd: no extra term, only M, Z, P, C depend on this stage's residual
                     UB[o + ny] += fin;
                     Y1B[o] = mu;
-                    sM = th * (Yo[o - ny] - Uw);
-                    sZ = -th * (Yo[o] - Uc);
-                    sP = th * (Yo[o + ny] - Ue);
-                    sW = 0.0;
-                    sMt = 0.0;
-                    sPt = 0.0;
                 }
-                const double mix = ((Y2[o - ny - 1] - U[o - ny - 1]) - (Y2[o - ny + 1] - U[o - ny + 1])) +
-                                   ((Y2[o + ny + 1] - U[o + ny + 1]) - (Y2[o + ny - 1] - U[o + ny - 1]));
-                sC = d.a_zeta * d.a_gamma * mix;
             }
-            pA += mu * hx * (sP - sM);
-            pB += mu * (sZ + sW);
-            if (KIND == 1 || zt != 0.0) {
-                pQ += mu * (sPt - sMt);
-                pD += mu * (sMt + sPt + 2.0 * sW);
-            }
-            pE += mu * __ldg(v.X(X_HC) + t) * sC;
-            if (sabr) {
-                pAa += mu * __ldg(v.X(X_HA) + t) * (sM + sP + 2.0 * sZ);
-                pDd += mu * __ldg(v.X(X_HDD) + t) * (sP - sM);
-            }
+            const s_terms st = adj_s_terms<KIND>(d, o, ny, U, Y1, Y2, Yo, th, zt, hv);
+            adj_s_sum(v, ps, st, mu, t, KIND == 1 || zt != 0.0, sabr);
             la_next = la;
         }
         if constexpr (KIND == 2) {
@@ -221,22 +268,93 @@ __device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d
         }
         LS[j] = -la_next * w + XB[j];
         HS[j] = -__ldg(v.Yv(Y_CHS) + j) * w_e + XB[(long long)(nx - 1) * ny + j];
-        const double ek = __ldg(v.Yv(Y_EK) + j), et = __ldg(v.Yv(Y_ET) + j), es = __ldg(v.Yv(Y_ES) + j);
-        const double bs = __ldg(v.Yv(Y_BS) + j), hy = __ldg(v.Yv(Y_HY) + j);
-        acc.s[0] += d.a_delta * pA + d.a_halfk * pB;
-        if (sabr) // D(t) terms of a^, d^ and c^
-            acc.s[0] += tau * d.a_omb *
-                        (__ldg(v.Yv(Y_HV2) + j) * (2.0 * d.a_delta * pDd - 2.0 * d.a_alphat * pAa) - d.a_rho * d.a_sigma * hy * pE);
-        acc.s[1] += d.a_ni * ek * pQ;
-        acc.s[2] += d.a_ni * et * pQ;
-        acc.s[3] += d.a_ni * es * pQ + d.a_betat * bs * pD + d.a_rho * hy * pE;
-        acc.s[4] += d.a_sigma * hy * pE;
+        adj_s_line(v, d, j, ps, tau, sabr, acc);
     }
 }
 
-// Gather pass over columns q: cross-line right-hand-side adjoints of an S stage into UB
-// (and Y2B for KIND 2), the lo/hi adjoints of the S lines, and for KIND 1 the adjoint of
-// the explicit v = v_lo boundary column (B1^T) with its parameter sensitivities.
+// Gather: cross-line right-hand-side adjoints of an S stage into UB (and Y2B for KIND 2), the
+// lo/hi adjoints of the S lines (lsum / hsum of column q, added on rows 0 / nx-1), and for
+// KIND 1 the adjoint of the explicit v = v_lo boundary column (B1^T) with its parameter
+// sensitivities.  One grid point (p, q) per call.
+template <int KIND>
+__device__ __forceinline__ void adj_gather_point(const inst_view<double> &v, const bdesc &d, const double *__restrict__ U,
+                                                 const double *__restrict__ FB, const double *__restrict__ LV,
+                                                 double *__restrict__ UB, double *__restrict__ Y2B, adj_acc &acc,
+                                                 double tau, int p, int q, double lsum, double hsum)
+{
+    const int nx = v.nx, ny = v.ny;
+    auto F = [&](int a, int b) -> double {
+        return (a >= 1 && a <= nx - 2 && b >= 1 && b <= ny - 2) ? FB[(long long)a * ny + b] : 0.0;
+    };
+    auto W = [&](int slot, int a, int b) -> double {
+        return (a >= 1 && a <= nx - 2 && b >= 1 && b <= ny - 2) ? __ldg(v.S(slot) + (long long)a * ny + b) : 0.0;
+    };
+    // lo-value adjoint of the explicit boundary column: bbar0(i) = sum over v lines i' with imap[i'] = i
+    auto B0 = [&](int i) -> double {
+        if (i < 1 || i > nx - 2) return 0.0;
+        double sum = 0.0;
+        if (__ldg(v.imap() + i) == i) sum += LV[i];
+        if (i + 1 <= nx - 2 && __ldg(v.imap() + i + 1) == i) sum += LV[i + 1];
+        return sum;
+    };
+    const long long o = (long long)p * ny + q;
+    double val = 0.0;
+    if constexpr (KIND == 2) {
+        double db = W(SL_S2MZ, p + 1, q + 1) * F(p + 1, q + 1) - W(SL_S2MZ, p + 1, q - 1) * F(p + 1, q - 1) -
+                    W(SL_S2MZ, p - 1, q + 1) * F(p - 1, q + 1) + W(SL_S2MZ, p - 1, q - 1) * F(p - 1, q - 1);
+        if (d.scheme != LSS_ADI_CRAIG_SNEYD)
+            db += W(SL_X1, p + 1, q) * F(p + 1, q) + W(SL_X2, p, q) * F(p, q) + W(SL_X3, p - 1, q) * F(p - 1, q) +
+                  W(SL_X4, p, q + 1) * F(p, q + 1) + W(SL_X5, p, q - 1) * F(p, q - 1);
+        // HV: rows 1..nx-2 already hold the last v stage's adjoint of its input Y2
+        if (d.scheme == LSS_ADI_HUNDSDORFER_VERWER && p >= 1 && p <= nx - 2) Y2B[o] += db; else Y2B[o] = db;
+        val -= db;
+    } else {
+        val += W(SL_WW, p + 1, q) * F(p + 1, q) + W(SL_WE, p - 1, q) * F(p - 1, q) + W(SL_WS, p, q + 1) * F(p, q + 1) +
+               W(SL_WN, p, q - 1) * F(p, q - 1) + W(SL_WC, p, q) * F(p, q) + W(SL_WG, p + 1, q + 1) * F(p + 1, q + 1) -
+               W(SL_WG, p + 1, q - 1) * F(p + 1, q - 1) - W(SL_WG, p - 1, q + 1) * F(p - 1, q + 1) +
+               W(SL_WG, p - 1, q - 1) * F(p - 1, q - 1);
+        if (q <= 2) {
+            if (q == 0) {
+                val += (p + 1 <= nx - 2 ? __ldg(v.X(XB_M) + p + 1) * B0(p + 1) : 0.0) + __ldg(v.X(XB_C) + p) * B0(p) +
+                       (p >= 1 ? __ldg(v.X(XB_P) + p - 1) * B0(p - 1) : 0.0);
+                if (p >= 1 && p <= nx - 2) {
+                    const double bb = B0(p);
+                    if (bb != 0.0) {
+                        const double u0 = U[o], u1 = U[o + 1], u2 = U[o + 2];
+                        const double um = U[o - ny], up = U[o + ny];
+                        const double ee = d.a_ni * bb * (4.0 * u1 - 3.0 * u0 - u2);
+                        double hd = __ldg(v.X(X_HX) + p);
+                        if (d.model == LSS_ADI_SABR) hd += 2.0 * d.a_omb * tau * __ldg(v.Yv(Y_HV2)) * __ldg(v.X(X_HDD) + p);
+                        acc.s[0] += bb * (d.a_delta * hd * (up - um) - d.a_k * u0);
+                        acc.s[1] += ee * __ldg(v.Yv(Y_EK));
+                        acc.s[2] += ee * __ldg(v.Yv(Y_ET));
+                        acc.s[3] += ee * __ldg(v.Yv(Y_ES));
+                    }
+                }
+            } else if (q == 1) {
+                val += __ldg(v.X(XB_1) + p) * B0(p);
+            } else {
+                val += __ldg(v.X(XB_2) + p) * B0(p);
+            }
+        }
+    }
+    if (p == 0) val += lsum;
+    if (p == nx - 1) val += hsum;
+    UB[o] += val;
+}
+
+// lo / hi adjoints of the S lines whose Dirichlet values come from column q (index_of remap)
+__device__ __forceinline__ void adj_line_ends(const inst_view<double> &v, const double *__restrict__ LS,
+                                              const double *__restrict__ HS, int q, double &lsum, double &hsum)
+{
+    const int ny = v.ny;
+    lsum = 0.0;
+    hsum = 0.0;
+    if (q >= 1 && q <= ny - 2 && __ldg(v.jmap() + q) == q) { lsum += LS[q]; hsum += HS[q]; }
+    if (q + 1 <= ny - 2 && __ldg(v.jmap() + q + 1) == q) { lsum += LS[q + 1]; hsum += HS[q + 1]; }
+}
+
+// Gather pass over columns q (thread per column).
 template <int KIND>
 __device__ __forceinline__ void adj_gather(const inst_view<double> &v, const bdesc &d, const double *__restrict__ U,
                                            const double *__restrict__ FB, const double *__restrict__ LS,
@@ -245,72 +363,11 @@ __device__ __forceinline__ void adj_gather(const inst_view<double> &v, const bde
                                            int l0, int ls)
 {
     const int nx = v.nx, ny = v.ny;
-    auto F = [&](int p, int q) -> double {
-        return (p >= 1 && p <= nx - 2 && q >= 1 && q <= ny - 2) ? FB[(long long)p * ny + q] : 0.0;
-    };
-    auto W = [&](int slot, int p, int q) -> double {
-        return (p >= 1 && p <= nx - 2 && q >= 1 && q <= ny - 2) ? __ldg(v.S(slot) + (long long)p * ny + q) : 0.0;
-    };
-    // lo-value adjoint of the explicit boundary column: bbar0(i) = sum over v lines i' with imap[i'] = i
-    auto B0 = [&](int i) -> double {
-        if (i < 1 || i > nx - 2) return 0.0;
-        double s = 0.0;
-        if (__ldg(v.imap() + i) == i) s += LV[i];
-        if (i + 1 <= nx - 2 && __ldg(v.imap() + i + 1) == i) s += LV[i + 1];
-        return s;
-    };
     for (int q = l0; q < ny; q += ls) {
-        double lsum = 0.0, hsum = 0.0;
-        if (q >= 1 && q <= ny - 2 && __ldg(v.jmap() + q) == q) { lsum += LS[q]; hsum += HS[q]; }
-        if (q + 1 <= ny - 2 && __ldg(v.jmap() + q + 1) == q) { lsum += LS[q + 1]; hsum += HS[q + 1]; }
+        double lsum, hsum;
+        adj_line_ends(v, LS, HS, q, lsum, hsum);
 #pragma unroll 2
-        for (int p = 0; p < nx; ++p) {
-            const long long o = (long long)p * ny + q;
-            double val = 0.0;
-            if constexpr (KIND == 2) {
-                double db = W(SL_S2MZ, p + 1, q + 1) * F(p + 1, q + 1) - W(SL_S2MZ, p + 1, q - 1) * F(p + 1, q - 1) -
-                            W(SL_S2MZ, p - 1, q + 1) * F(p - 1, q + 1) + W(SL_S2MZ, p - 1, q - 1) * F(p - 1, q - 1);
-                if (d.scheme != LSS_ADI_CRAIG_SNEYD)
-                    db += W(SL_X1, p + 1, q) * F(p + 1, q) + W(SL_X2, p, q) * F(p, q) + W(SL_X3, p - 1, q) * F(p - 1, q) +
-                          W(SL_X4, p, q + 1) * F(p, q + 1) + W(SL_X5, p, q - 1) * F(p, q - 1);
-                // HV: rows 1..nx-2 already hold the last v stage's adjoint of its input Y2
-                if (d.scheme == LSS_ADI_HUNDSDORFER_VERWER && p >= 1 && p <= nx - 2) Y2B[o] += db; else Y2B[o] = db;
-                val -= db;
-            } else {
-                val += W(SL_WW, p + 1, q) * F(p + 1, q) + W(SL_WE, p - 1, q) * F(p - 1, q) +
-                       W(SL_WS, p, q + 1) * F(p, q + 1) + W(SL_WN, p, q - 1) * F(p, q - 1) + W(SL_WC, p, q) * F(p, q) +
-                       W(SL_WG, p + 1, q + 1) * F(p + 1, q + 1) - W(SL_WG, p + 1, q - 1) * F(p + 1, q - 1) -
-                       W(SL_WG, p - 1, q + 1) * F(p - 1, q + 1) + W(SL_WG, p - 1, q - 1) * F(p - 1, q - 1);
-                if (q <= 2) {
-                    if (q == 0) {
-                        val += (p + 1 <= nx - 2 ? __ldg(v.X(XB_M) + p + 1) * B0(p + 1) : 0.0) +
-                               __ldg(v.X(XB_C) + p) * B0(p) + (p >= 1 ? __ldg(v.X(XB_P) + p - 1) * B0(p - 1) : 0.0);
-                        if (p >= 1 && p <= nx - 2) {
-                            const double bb = B0(p);
-                            if (bb != 0.0) {
-                                const double u0 = U[o], u1 = U[o + 1], u2 = U[o + 2];
-                                const double um = U[o - ny], up = U[o + ny];
-                                const double ee = d.a_ni * bb * (4.0 * u1 - 3.0 * u0 - u2);
-                                double hd = __ldg(v.X(X_HX) + p);
-                                if (d.model == LSS_ADI_SABR)
-                                    hd += 2.0 * d.a_omb * tau * __ldg(v.Yv(Y_HV2)) * __ldg(v.X(X_HDD) + p);
-                                acc.s[0] += bb * (d.a_delta * hd * (up - um) - d.a_k * u0);
-                                acc.s[1] += ee * __ldg(v.Yv(Y_EK));
-                                acc.s[2] += ee * __ldg(v.Yv(Y_ET));
-                                acc.s[3] += ee * __ldg(v.Yv(Y_ES));
-                            }
-                        }
-                    } else if (q == 1) {
-                        val += __ldg(v.X(XB_1) + p) * B0(p);
-                    } else {
-                        val += __ldg(v.X(XB_2) + p) * B0(p);
-                    }
-                }
-            }
-            if (p == 0) val += lsum;
-            if (p == nx - 1) val += hsum;
-            UB[o] += val;
-        }
+        for (int p = 0; p < nx; ++p) adj_gather_point<KIND>(v, d, U, FB, LV, UB, Y2B, acc, tau, p, q, lsum, hsum);
     }
 }
 

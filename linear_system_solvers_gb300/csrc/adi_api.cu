@@ -180,6 +180,12 @@ int lss_adi_adjoint(lss_adi_handle *h, const void *payoff, double *out_value, do
         if (!a) return set_error(LSS_ADI_ENOMEM, "host allocation failed");
         int rc = a->init(h->prob);
         if (rc) return rc;
+        if (h->wide) { // the forward's chunk counts, so both passes solve alike
+            int ps = 1, pv = 1;
+            h->wide->current_chunks(ps, pv);
+            rc = a->set_chunks(ps, pv, stream);
+            if (rc) return rc;
+        }
         h->adj = std::move(a);
     }
     return h->adj->run(payoff, out_value, dv_dparams, dv_dpayoff, checkpoint_every, flags, stream);
@@ -205,7 +211,16 @@ int lss_adi_line_chunks(lss_adi_handle *h, int s_chunks, int v_chunks, int *out_
     clear_error();
     if (!h) return set_error(LSS_ADI_EINVAL, "lss_adi_line_chunks: null handle");
     if (!h->wide) return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_line_chunks: not a partitioned (fast single-instance) handle");
-    return h->wide->chunks(s_chunks, v_chunks, out_s, out_v, stream);
+    int ps = 1, pv = 1;
+    int rc = h->wide->chunks(s_chunks, v_chunks, &ps, &pv, stream);
+    if (rc) return rc;
+    if (h->adj) {
+        rc = h->adj->set_chunks(ps, pv, stream);
+        if (rc) return rc;
+    }
+    if (out_s) *out_s = ps;
+    if (out_v) *out_v = pv;
+    return LSS_ADI_OK;
 }
 
 void lss_adi_destroy(lss_adi_handle *h) { delete h; }

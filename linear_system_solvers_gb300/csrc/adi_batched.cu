@@ -828,42 +828,239 @@ __global__ void k_wadj_b2(const __grid_constant__ bparams<double> p, double *VB,
 
 template <bool FIRST>
 __global__ void k_wadj_v(const __grid_constant__ bparams<double> p, const double *in, const double *out, const double *XB,
-                         double *INB, double *INHB, double *TMP, double *LV, double *acc_a)
+                         double *INB, double *INHB, double *TMP, double *LV, double *acc_a, long long nacc)
 {
     const bdesc d = p.desc[0];
     const inst_view<double> v = make_view(p, d);
-    const long long nthr = gstride(), t = gtid();
+    const long long t = gtid();
     adj_acc acc;
-    acc_load(acc, acc_a, nthr, t);
+    acc_load(acc, acc_a, nacc, t);
     adj_v<FIRST>(v, in, out, XB, INB, INHB, TMP, LV, acc, gtid(), gstride());
-    acc_store(acc, acc_a, nthr, t);
+    acc_store(acc, acc_a, nacc, t);
 }
 
 template <int KIND>
 __global__ void k_wadj_s(const __grid_constant__ bparams<double> p, const double *U, const double *Y1, const double *Y2,
                          const double *Yo, const double *XB, double *FB, double *TMP, double *LS, double *HS, double *UB,
-                         double *Y1B, double *acc_a, double tau)
+                         double *Y1B, double *acc_a, long long nacc, double tau)
 {
     const bdesc d = p.desc[0];
     const inst_view<double> v = make_view(p, d);
-    const long long nthr = gstride(), t = gtid();
+    const long long t = gtid();
     adj_acc acc;
-    acc_load(acc, acc_a, nthr, t);
+    acc_load(acc, acc_a, nacc, t);
     adj_s<KIND>(v, d, U, Y1, Y2, Yo, XB, FB, TMP, LS, HS, UB, Y1B, acc, tau, gtid(), gstride());
-    acc_store(acc, acc_a, nthr, t);
+    acc_store(acc, acc_a, nacc, t);
+}
+
+// Partitioned adjoint line solves (the wide adjoint's counterpart of k_wide_s_chunk /
+// k_wide_v_chunk): the transposed factorised solve
+//   z_t = xbar_t - g_{t-1} z_{t-1}  (t = 1..e),   w_t = z_t - la_{t+1} w_{t+1}  (t = e..1)
+// is cut into chunks with the chunk products hz_t = prod_{s=t0..t} (-g_{s-1}) and
+// hw_t = prod_{s=t..t1} (-la_{s+1}); after the final w of the whole line is in TMP, each chunk
+// applies the point-local terms (right-hand-side adjoints, parameter sums).
+template <typename T>
+__global__ void k_wadj_spikes(const T *__restrict__ la, const T *__restrict__ g, T *__restrict__ hz,
+                              T *__restrict__ hw, int lines, int stride, int e, int P)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= (lines - 2) * P) return;
+    const int l = 1 + q / P, c = q % P;
+    int t0, t1;
+    chunk_range(e, P, c, t0, t1);
+    T pr = T(1);
+    for (int t = t0; t <= t1; ++t) {
+        pr *= (t > 1) ? -g[(long long)(t - 1) * stride + l] : T(0);
+        hz[(long long)t * stride + l] = pr;
+    }
+    pr = T(1);
+    for (int t = t1; t >= t0; --t) {
+        pr *= (t < e) ? -la[(long long)(t + 1) * stride + l] : T(0);
+        hw[(long long)t * stride + l] = pr;
+    }
+}
+
+// z and w of one chunk of a line: element t of the line at base[t * st] in TMP, tables at
+// tab + t * ts; carries through the block's shared arrays (rows: chunks, columns: lines).
+__device__ __forceinline__ void adj_chunk_solve(double *__restrict__ TMP, long long base, long long st,
+                                                const double *__restrict__ XB, const double *__restrict__ G,
+                                                const double *__restrict__ LA, const double *__restrict__ hz,
+                                                const double *__restrict__ hw, long long tab, long long ts, int e,
+                                                int t0, int t1, int c, int P, int lane, bool act, double (*sa)[33],
+                                                double (*sb)[33])
+{
+    double z = 0.0;
+    if (act) {
+        for (int t = t0; t <= t1; ++t) {
+            const double gprev = (t > 1) ? __ldg(G + tab + (long long)(t - 1) * ts) : 0.0;
+            z = XB[base + t * st] - gprev * z;
+            TMP[base + t * st] = z;
+        }
+        sb[c][lane] = z;
+        sa[c][lane] = hz[tab + (long long)t1 * ts];
+    }
+    __syncthreads();
+    double w = 0.0;
+    if (act) {
+        double zin = 0.0;
+        if (c > 0) {
+            zin = sb[0][lane];
+            for (int q = 1; q < c; ++q) zin = sb[q][lane] + sa[q][lane] * zin;
+        }
+        double la_next = 0.0;
+        for (int t = t1; t >= t0; --t) {
+            const double zt = (c > 0) ? TMP[base + t * st] + hz[tab + (long long)t * ts] * zin : TMP[base + t * st];
+            w = zt - la_next * w;
+            TMP[base + t * st] = w;
+            la_next = __ldg(LA + tab + (long long)t * ts);
+        }
+    }
+    __syncthreads();
+    if (act) {
+        sb[c][lane] = w;
+        sa[c][lane] = hw[tab + (long long)t0 * ts];
+    }
+    __syncthreads();
+    if (act && c < P - 1) {
+        double win = sb[P - 1][lane];
+        for (int q = P - 2; q > c; --q) win = sb[q][lane] + sa[q][lane] * win;
+        for (int t = t0; t <= t1; ++t) TMP[base + t * st] += hw[tab + (long long)t * ts] * win;
+    }
+    __syncthreads();
+}
+
+template <bool FIRST>
+__global__ void __launch_bounds__(1024) k_wadj_v_chunk(const __grid_constant__ bparams<double> p, const double *in,
+                                                        const double *out, const double *XB, double *INB, double *INHB,
+                                                        double *TMP, double *LV, double *acc_a, long long nacc,
+                                                        const double *__restrict__ hz, const double *__restrict__ hw)
+{
+    __shared__ double sa[32][33], sb[32][33];
+    const bdesc d = p.desc[0];
+    const inst_view<double> v = make_view(p, d);
+    const int nx = d.nx, ny = d.ny, e = ny - 2, P = blockDim.y, c = threadIdx.y, lane = threadIdx.x;
+    const int i = 1 + blockIdx.x * 32 + lane;
+    const bool act = i <= nx - 2;
+    const long long row = (long long)i * ny, tid = ((long long)blockIdx.x * P + c) * 32 + lane;
+    int t0, t1;
+    chunk_range(e, P, c, t0, t1);
+    adj_chunk_solve(TMP, row, 1, XB, v.Vt(VL_G), v.Vt(VL_LA), hz, hw, i, nx, e, t0, t1, c, P, lane, act, sa, sb);
+    if (!act) return;
+    adj_acc acc;
+    acc_load(acc, acc_a, nacc, tid);
+    const double *LA = v.Vt(VL_LA), *VC = v.Vt(VL_VC), *VN = v.Vt(VL_VN), *IB = v.Vt(VL_IB);
+    for (int t = t1; t >= t0; --t) {
+        const long long ot = (long long)t * nx + i;
+        const double w0 = TMP[row + t];
+        const double w1 = (t + 1 <= e) ? TMP[row + t + 1] : 0.0, w2 = (t + 2 <= e) ? TMP[row + t + 2] : 0.0;
+        const double la2 = (t + 2 <= e) ? __ldg(LA + ot + 2LL * nx) : 0.0, vc1 = (t + 1 <= e) ? __ldg(VC + ot + nx) : 0.0;
+        const double fin = la2 * w2 + vc1 * w1 + __ldg(VN + ot) * w0; // adjoint of in(t+1)
+        if (FIRST) INB[row + t + 1] = fin; else INB[row + t + 1] += fin;
+        const double mu = __ldg(IB + ot) * w0;
+        if (FIRST) INHB[row + t] = mu; else INHB[row + t] += mu;
+        adj_v_sum(v, t, mu, in[row + t - 1] - out[row + t - 1], in[row + t] - out[row + t],
+                  in[row + t + 1] - out[row + t + 1], acc);
+    }
+    if (c == 0) {
+        const double w1 = TMP[row + 1], w2 = (2 <= e) ? TMP[row + 2] : 0.0;
+        const double la1 = __ldg(LA + nx + i), la2 = (2 <= e) ? __ldg(LA + 2LL * nx + i) : 0.0;
+        const double a1 = la2 * w2 + __ldg(VC + nx + i) * w1, a0 = la1 * w1;
+        if (FIRST) { INB[row + 1] = a1; INB[row] = a0; }
+        else { INB[row + 1] += a1; INB[row] += a0; }
+        const double lob = -la1 * w1 + XB[row];
+        if (FIRST) LV[i] = lob; else LV[i] += lob;
+    }
+    acc_store(acc, acc_a, nacc, tid);
 }
 
 template <int KIND>
-__global__ void k_wadj_gather(const __grid_constant__ bparams<double> p, const double *U, const double *FB, const double *LS,
-                              const double *HS, const double *LV, double *UB, double *Y2B, double *acc_a, double tau)
+__global__ void __launch_bounds__(1024) k_wadj_s_chunk(const __grid_constant__ bparams<double> p, const double *U,
+                                                        const double *Y1, const double *Y2, const double *Yo,
+                                                        const double *XB, double *FB, double *TMP, double *LS, double *HS,
+                                                        double *UB, double *Y1B, double *acc_a, long long nacc, double tau,
+                                                        const double *__restrict__ hz, const double *__restrict__ hw)
+{
+    __shared__ double sa[32][33], sb[32][33];
+    const bdesc d = p.desc[0];
+    const inst_view<double> v = make_view(p, d);
+    const int nx = d.nx, ny = d.ny, e = nx - 2, P = blockDim.y, c = threadIdx.y, lane = threadIdx.x;
+    const int j = 1 + blockIdx.x * 32 + lane;
+    const bool act = j <= ny - 2;
+    const long long tid = ((long long)blockIdx.x * P + c) * 32 + lane;
+    int t0, t1;
+    chunk_range(e, P, c, t0, t1);
+    adj_chunk_solve(TMP, j, ny, XB, v.S(SL_G), v.S(SL_LA), hz, hw, j, ny, e, t0, t1, c, P, lane, act, sa, sb);
+    if (!act) return;
+    const bool sabr = d.model == LSS_ADI_SABR, hv = d.scheme == LSS_ADI_HUNDSDORFER_VERWER;
+    const double th = d.a_theta;
+    const double zt = (d.scheme == LSS_ADI_MODIFIED_CRAIG_SNEYD) ? (d.a_zeta - th) : hv ? d.a_zeta : 0.0;
+    adj_acc acc;
+    acc_load(acc, acc_a, nacc, tid);
+    const double *LA = v.S(SL_LA), *IB = v.S(SL_IB);
+    s_sums ps = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int t = t1; t >= t0; --t) {
+        const long long o = (long long)t * ny + j;
+        const double w0 = TMP[o];
+        FB[o] = w0;
+        const double mu = __ldg(IB + o) * w0;
+        if constexpr (KIND == 2) {
+            const double w1 = (t + 1 <= e) ? TMP[o + ny] : 0.0, w2 = (t + 2 <= e) ? TMP[o + 2LL * ny] : 0.0;
+            const double la2 = (t + 2 <= e) ? __ldg(LA + o + 2LL * ny) : 0.0;
+            const double sc1 = (t + 1 <= e) ? __ldg(v.S(SL_S2SC) + o + ny) : 0.0;
+            const double fin = la2 * w2 + sc1 * w1 + __ldg(v.S(SL_S2SE) + o) * w0;
+            if (hv) {
+                Y1B[o + ny] = fin;
+            } else {
+                UB[o + ny] += fin;
+                Y1B[o] = mu;
+            }
+        }
+        const s_terms st = adj_s_terms<KIND>(d, o, ny, U, Y1, Y2, Yo, th, zt, hv);
+        adj_s_sum(v, ps, st, mu, t, KIND == 1 || zt != 0.0, sabr);
+    }
+    if (c == 0) {
+        const double w1 = TMP[(long long)ny + j], la1 = __ldg(LA + ny + j);
+        LS[j] = -la1 * w1 + XB[j];
+        if constexpr (KIND == 2) {
+            const double w2 = (2 <= e) ? TMP[2LL * ny + j] : 0.0, la2 = (2 <= e) ? __ldg(LA + 2LL * ny + j) : 0.0;
+            const double a1 = la2 * w2 + __ldg(v.S(SL_S2SC) + ny + j) * w1, a0 = la1 * w1;
+            if (hv) {
+                Y1B[(long long)ny + j] = a1;
+                Y1B[j] = a0;
+            } else {
+                UB[(long long)ny + j] += a1;
+                UB[j] += a0;
+            }
+        }
+    }
+    if (c == P - 1) HS[j] = -__ldg(v.Yv(Y_CHS) + j) * TMP[(long long)e * ny + j] + XB[(long long)(nx - 1) * ny + j];
+    adj_s_line(v, d, j, ps, tau, sabr, acc);
+    acc_store(acc, acc_a, nacc, tid);
+}
+
+// Gather with one thread per grid point; the B1 parameter sums of column 0 go to acc slot p.
+template <int KIND>
+__global__ void k_wadj_gather2d(const __grid_constant__ bparams<double> p, const double *U, const double *FB,
+                                const double *LS, const double *HS, const double *LV, double *UB, double *Y2B,
+                                double *acc_a, long long nacc, double tau)
 {
     const bdesc d = p.desc[0];
     const inst_view<double> v = make_view(p, d);
-    const long long nthr = gstride(), t = gtid();
+    const long long n = (long long)d.nx * d.ny;
+    const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= n) return;
+    const int pr = static_cast<int>(o / d.ny), q = static_cast<int>(o % d.ny);
+    double lsum = 0.0, hsum = 0.0;
+    if (pr == 0 || pr == d.nx - 1) adj_line_ends(v, LS, HS, q, lsum, hsum);
     adj_acc acc;
-    acc_load(acc, acc_a, nthr, t);
-    adj_gather<KIND>(v, d, U, FB, LS, HS, LV, UB, Y2B, acc, tau, gtid(), gstride());
-    acc_store(acc, acc_a, nthr, t);
+    if (q == 0) {
+        acc_load(acc, acc_a, nacc, pr);
+    } else {
+        for (int k = 0; k < 5; ++k) acc.s[k] = 0.0;
+        acc.vk = acc.vt = acc.vs1 = acc.vs2 = acc.vb = 0.0;
+    }
+    adj_gather_point<KIND>(v, d, U, FB, LV, UB, Y2B, acc, tau, pr, q, lsum, hsum);
+    if (q == 0) acc_store(acc, acc_a, nacc, pr);
 }
 
 // final surface out, adjoint arrays cleared, finiteness of the final surface
@@ -1029,6 +1226,8 @@ template <typename T> struct batch_typed {
     // wide forward + adjoint (count == 1, FP64)
     dbuf<double> d_wws;
     long long wws_need = 0;
+    dbuf<T> d_aspk;                 // adjoint chunk products: S hz, S hw, v hz, v hw (n each)
+    int aspk_ps = 0, aspk_pv = 0;
     int enqueue_wide_adjoint(cudaStream_t s);
     int enqueue(int mode, cudaStream_t s);
     int run(int mode, cudaStream_t s, bool use_graph);
@@ -1561,7 +1760,24 @@ template <typename T> int batch_typed<T>::enqueue_wide_adjoint(cudaStream_t s)
         const int nseg = (d.steps + c - 1) / c;
         const int threads = 128, grid = grid_for(std::max(nx, ny), threads);
         const long long nthr = static_cast<long long>(grid) * threads;
-        const long long need = (nseg + 4LL * (c + 1) + 9) * n + nx + 2LL * ny + 10 * nthr;
+        // partitioned adjoint solves with the forward's chunk counts
+        const int ps = wide_ps, pv = wide_pv, gS = grid_for(ny - 2, 32), gV = grid_for(nx - 2, 32);
+        const long long nacc = std::max({nthr, 32LL * gS * ps, 32LL * gV * pv, static_cast<long long>(nx)});
+        if ((ps > 1 || pv > 1) && (aspk_ps != ps || aspk_pv != pv)) {
+            if (!d_aspk.p) LSS_CUDA_TRY(d_aspk.alloc(4 * n), "wide adjoint: allocating chunk products");
+            const bparams<double> q = params();
+            if (ps > 1)
+                k_wadj_spikes<double><<<grid_for((ny - 2) * ps, 128), 128, 0, s>>>(q.S[SL_LA], q.S[SL_G], d_aspk.p,
+                                                                                   d_aspk.p + n, ny, ny, nx - 2, ps);
+            if (pv > 1)
+                k_wadj_spikes<double><<<grid_for((nx - 2) * pv, 128), 128, 0, s>>>(q.Vt[VL_LA], q.Vt[VL_G], d_aspk.p + 2 * n,
+                                                                                   d_aspk.p + 3 * n, nx, nx, ny - 2, pv);
+            LSS_CUDA_TRY(cudaGetLastError(), "wide adjoint: chunk products");
+            aspk_ps = ps;
+            aspk_pv = pv;
+        }
+        const double *hzS = d_aspk.p, *hwS = d_aspk.p + n, *hzV = d_aspk.p + 2 * n, *hwV = d_aspk.p + 3 * n;
+        const long long need = (nseg + 4LL * (c + 1) + 9) * n + nx + 2LL * ny + 10 * nacc;
         if (!d_wws.p || wws_need != need) {
             LSS_CUDA_TRY(d_wws.alloc(need), "wide adjoint: allocating workspace");
             wws_need = need;
@@ -1575,7 +1791,7 @@ template <typename T> int batch_typed<T>::enqueue_wide_adjoint(cudaStream_t s)
         const bparams<double> p = params();
         // stage arrays start at zero (rows 0 and nx-1 of Y2 are never written by the sweeps)
         LSS_CUDA_TRY(cudaMemsetAsync(SEG, 0, (c + 1) * 4LL * n * sizeof(double), s), "wide adjoint: clearing");
-        LSS_CUDA_TRY(cudaMemsetAsync(ACC, 0, 10 * nthr * sizeof(double), s), "wide adjoint: clearing");
+        LSS_CUDA_TRY(cudaMemsetAsync(ACC, 0, 10 * nacc * sizeof(double), s), "wide adjoint: clearing");
         LSS_CUDA_TRY(cudaMemsetAsync(d_status.p, 0, sizeof(int), s), "wide adjoint: clearing");
         LSS_CUDA_TRY(cudaMemcpyAsync(CK, d_payoff.p, n * sizeof(double), cudaMemcpyDeviceToDevice, s), "wide adjoint: initial state");
         long long nl = 0;
@@ -1605,27 +1821,58 @@ template <typename T> int batch_typed<T>::enqueue_wide_adjoint(cudaStream_t s)
                 const double *um = (m == 0) ? u0 : slot(m, 0);
                 const double *Y1 = slot(m, 1), *Y2 = slot(m, 2), *Y3 = slot(m, 3), *Vo = slot(m + 1, 0);
                 const double tau = d.a_tau0 + d.a_dtau * (n0 + m);
+                // v stages: (in, out, output adjoint, adjoint of in, adjoint of inh), first or accumulating
+                auto adj_v_stage = [&](bool first, const double *in, const double *out, const double *XB, double *INB,
+                                       double *INHB) {
+                    if (pv > 1) {
+                        if (first)
+                            k_wadj_v_chunk<true><<<gV, dim3(32, pv), 0, s>>>(p, in, out, XB, INB, INHB, TMP, LV, ACC, nacc, hzV, hwV);
+                        else
+                            k_wadj_v_chunk<false><<<gV, dim3(32, pv), 0, s>>>(p, in, out, XB, INB, INHB, TMP, LV, ACC, nacc, hzV, hwV);
+                    } else {
+                        if (first)
+                            k_wadj_v<true><<<grid, threads, 0, s>>>(p, in, out, XB, INB, INHB, TMP, LV, ACC, nacc);
+                        else
+                            k_wadj_v<false><<<grid, threads, 0, s>>>(p, in, out, XB, INB, INHB, TMP, LV, ACC, nacc);
+                    }
+                };
+                auto adj_s_stage = [&](int kind, const double *Yo, const double *XB) {
+                    if (ps > 1) {
+                        if (kind == 2)
+                            k_wadj_s_chunk<2><<<gS, dim3(32, ps), 0, s>>>(p, um, Y1, Y2, Yo, XB, FB, TMP, LS, HS, ub, Y1B, ACC,
+                                                                          nacc, tau, hzS, hwS);
+                        else
+                            k_wadj_s_chunk<1><<<gS, dim3(32, ps), 0, s>>>(p, um, Y1, Y2, Yo, XB, FB, TMP, LS, HS, ub, Y1B, ACC,
+                                                                          nacc, tau, hzS, hwS);
+                    } else {
+                        if (kind == 2)
+                            k_wadj_s<2><<<grid, threads, 0, s>>>(p, um, Y1, Y2, Yo, XB, FB, TMP, LS, HS, ub, Y1B, ACC, nacc, tau);
+                        else
+                            k_wadj_s<1><<<grid, threads, 0, s>>>(p, um, Y1, Y2, Yo, XB, FB, TMP, LS, HS, ub, Y1B, ACC, nacc, tau);
+                    }
+                };
+                const int gG = grid_for(n, 256);
                 k_wadj_b2<<<grid, threads, 0, s>>>(p, vb, ub);
                 if (d.scheme == LSS_ADI_DOUGLAS_RACHFORD) {
-                    k_wadj_v<true><<<grid, threads, 0, s>>>(p, um, Vo, vb, ub, Y1B, TMP, LV, ACC);
+                    adj_v_stage(true, um, Vo, vb, ub, Y1B);
                     nl += 2;
                 } else {
                     if (d.scheme == LSS_ADI_HUNDSDORFER_VERWER)
-                        k_wadj_v<true><<<grid, threads, 0, s>>>(p, Y2, Vo, vb, Y2B, Y3B, TMP, LV, ACC);
+                        adj_v_stage(true, Y2, Vo, vb, Y2B, Y3B);
                     else
-                        k_wadj_v<true><<<grid, threads, 0, s>>>(p, um, Vo, vb, ub, Y3B, TMP, LV, ACC);
-                    k_wadj_s<2><<<grid, threads, 0, s>>>(p, um, Y1, Y2, Y3, Y3B, FB, TMP, LS, HS, ub, Y1B, ACC, tau);
-                    k_wadj_gather<2><<<grid, threads, 0, s>>>(p, um, FB, LS, HS, LV, ub, Y2B, ACC, tau);
-                    k_wadj_v<false><<<grid, threads, 0, s>>>(p, um, Y2, Y2B, ub, Y1B, TMP, LV, ACC);
+                        adj_v_stage(true, um, Vo, vb, ub, Y3B);
+                    adj_s_stage(2, Y3, Y3B);
+                    k_wadj_gather2d<2><<<gG, 256, 0, s>>>(p, um, FB, LS, HS, LV, ub, Y2B, ACC, nacc, tau);
+                    adj_v_stage(false, um, Y2, Y2B, ub, Y1B);
                     nl += 5;
                 }
-                k_wadj_s<1><<<grid, threads, 0, s>>>(p, um, Y1, Y2, Y1, Y1B, FB, TMP, LS, HS, ub, Y1B, ACC, tau);
-                k_wadj_gather<1><<<grid, threads, 0, s>>>(p, um, FB, LS, HS, LV, ub, Y2B, ACC, tau);
+                adj_s_stage(1, Y1, Y1B);
+                k_wadj_gather2d<1><<<gG, 256, 0, s>>>(p, um, FB, LS, HS, LV, ub, Y2B, ACC, nacc, tau);
                 nl += 2;
                 std::swap(ub, vb);
             }
         }
-        k_wadj_reduce<<<1, 256, 0, s>>>(p, ACC, nthr);
+        k_wadj_reduce<<<1, 256, 0, s>>>(p, ACC, nacc);
         LSS_CUDA_TRY(cudaMemcpyAsync(p.V, vb, n * sizeof(double), cudaMemcpyDeviceToDevice, s), "wide adjoint: payoff gradient");
         LSS_CUDA_TRY(cudaGetLastError(), "wide adjoint: launching");
         launches = nl + 1;
@@ -1749,6 +1996,11 @@ template <typename T> struct wide_solver : wide_solver_base {
         if (out_v) *out_v = b.wide_pv;
         return LSS_ADI_OK;
     }
+    void current_chunks(int &s_chunks, int &v_chunks) const override
+    {
+        s_chunks = b.wide_ps;
+        v_chunks = b.wide_pv;
+    }
 };
 
 int make_wide_solver(const lss_adi_problem &p, std::unique_ptr<wide_solver_base> &out)
@@ -1800,6 +2052,12 @@ int adjoint_solver::init(const lss_adi_problem &p)
         LSS_CUDA_TRY(cudaDeviceSynchronize(), "lss_adi_adjoint: tuning");
     }
     return LSS_ADI_OK;
+}
+
+int adjoint_solver::set_chunks(int s_chunks, int v_chunks, void *stream)
+{
+    if (!impl || !impl->wide) return LSS_ADI_OK;
+    return impl->b.set_wide_chunks(s_chunks, v_chunks, static_cast<cudaStream_t>(stream));
 }
 
 int adjoint_solver::run(const void *payoff, double *out_value, double *dv_dparams, void *dv_dpayoff, int checkpoint_every,

@@ -185,3 +185,21 @@ def test_batch_gradients_finite_difference_sample(lss):
             assert abs(grads[k, q] - fd) <= 1e-6 * max(abs(fd), 1e-3 * abs(vals[k])), (k, name, grads[k, q], fd)
         checked += 1
     assert checked >= 4
+
+
+@pytest.mark.parametrize("key", ["wide_heston_mcs", "wide_heston_hv", "wide_sabr_dr"])
+def test_wide_adjoint_partitioned_solves_match_line_per_thread(lss, key):
+    """The wide adjoint's partitioned transposed solves (chunk products, composed carries)
+    against its thread-per-line solves, with the forward chunked alike: the same derivatives
+    up to rounding."""
+    p = lss.HestonProblem(**CASES[key])
+    ref = lss.ImplicitHestonSolver(dataclasses.replace(p, line_per_thread=True), precision="f64", arith="fast")
+    v0, g0, l0 = ref.adjoint()
+    for chunks in ((4, 2), (16, 8), (32, 4)):
+        s = lss.ImplicitHestonSolver(p, precision="f64", arith="fast")
+        assert s.line_chunks(*chunks) == chunks
+        v, g, lam = s.adjoint()
+        assert abs(v - v0) <= 1e-12 * max(1.0, abs(v0))
+        scale = max(np.abs(g0).max(), 1e-3 * abs(v0))
+        assert np.max(np.abs(g - g0)) <= 1e-10 * scale, (chunks, g, g0)
+        assert np.max(np.abs(lam - l0)) <= 1e-10 * np.abs(l0).max()
