@@ -64,7 +64,7 @@ def fd_grad(fn, p, name, rel=None):
         # SABR sensitivities are ~1e-2 of the value: a larger bump keeps the rounding noise of the
         # differences (value x 1e-14 / h) well below 1e-6 of them
         rel = 1e-4 if p.model == "sabr" else 1e-5
-    h = rel * (abs(base) if base != 0.0 else 1e-2)  # r = 0: absolute bump rel x 1e-2
+    h = rel * (abs(base) if base != 0.0 else 1.0)  # r = 0: absolute bump rel
     return (4.0 * central(h / 2) - central(h)) / 3.0
 
 
