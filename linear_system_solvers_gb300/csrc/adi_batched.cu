@@ -439,7 +439,10 @@ __device__ __forceinline__ void fwd_step(const inst_view<T> &v, int scheme, cons
     __syncthreads();
 }
 
-template <typename T, int BS> __global__ void __launch_bounds__(BS) k_batch_forward(const __grid_constant__ bparams<T> p)
+// Register budget: 64 per thread (1024 / BS resident threads' worth of CTAs per SM).  The time
+// loop waits on streamed table loads; twice the resident warps of the unconstrained build
+// (96 registers) outweigh the few spills (+18 % on the 4096-instance batch, measured).
+template <typename T, int BS> __global__ void __launch_bounds__(BS, 1024 / BS) k_batch_forward(const __grid_constant__ bparams<T> p)
 {
     __shared__ int s_idx;
     __shared__ int s_bad;
@@ -486,7 +489,10 @@ template <typename T, int BS> __global__ void __launch_bounds__(BS) k_batch_forw
 // values of every step, followed by the adjoint steps of the segment in reverse order.
 // Results: value, the 5 parameter sensitivities, the final surface (state U arena) and
 // dV/d(initial condition) (state V arena).
-template <int BS> __global__ void __launch_bounds__(BS, 512 / BS) k_batch_fwdadj(const __grid_constant__ bparams<double> p)
+// Register budget ~72 per thread (896 / BS CTAs per SM): more resident warps to cover the load
+// latency of the adjoint's workspace traffic beat the spills (+15 % over 128 registers,
+// measured; 64 and 80 registers were slower).
+template <int BS> __global__ void __launch_bounds__(BS, 896 / BS) k_batch_fwdadj(const __grid_constant__ bparams<double> p)
 {
     __shared__ int s_idx;
     __shared__ int s_bad;
