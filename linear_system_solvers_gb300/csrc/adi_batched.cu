@@ -1211,7 +1211,7 @@ template <typename T> struct batch_typed {
 
     int create(const lss_adi_problem *ps, int n);
     int prepare_adjoint(cudaStream_t s);
-    int ensure_ws(int bs);
+    int ensure_ws(int bs, bool shrink = false); // shrink: release slices the size `bs` does not use
     // threads per instance (CTA size) of the persistent kernels, per mode; chosen by autotune()
     int bs_mode[2] = {64, 64};
     template <int BS> int launch_forward(cudaStream_t s);
@@ -1477,7 +1477,7 @@ template <typename T> int batch_typed<T>::prepare_adjoint(cudaStream_t s)
 }
 
 // Adjoint workspace for every resident CTA of k_batch_fwdadj<bs> (one slice per CTA).
-template <typename T> int batch_typed<T>::ensure_ws(int bs)
+template <typename T> int batch_typed<T>::ensure_ws(int bs, bool shrink)
 {
     int per_sm = 0;
     switch (bs) {
@@ -1487,8 +1487,8 @@ template <typename T> int batch_typed<T>::ensure_ws(int bs)
     default: LSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_fwdadj<64>, 64, 0), "occupancy"); break;
     }
     const int want = std::max(1, std::min(sms * std::max(1, per_sm), count));
-    if (d_ws.p && ws_stride == ws_need && grid_adj >= want) return LSS_ADI_OK;
-    const int slices = (d_ws.p && ws_stride == ws_need) ? std::max(want, grid_adj) : want;
+    if (d_ws.p && ws_stride == ws_need && (shrink ? grid_adj == want : grid_adj >= want)) return LSS_ADI_OK;
+    const int slices = (d_ws.p && ws_stride == ws_need && !shrink) ? std::max(want, grid_adj) : want;
     ws_stride = ws_need;
     grid_adj = slices;
     LSS_CUDA_TRY(d_ws.alloc(static_cast<size_t>(ws_stride) * grid_adj), "batch: allocating adjoint workspace");
@@ -1598,6 +1598,10 @@ template <typename T> int batch_typed<T>::autotune(int mode, int *chosen, cudaSt
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         bs_mode[m] = best_bs;
+        if (mode == 1) { // the candidates' workspace (one-warp CTAs: the most slices) down to the chosen size's
+            int rc = ensure_ws(best_bs, true);
+            if (rc) return rc;
+        }
     }
     if (graph && graph_mode == mode) {
         cudaGraphExecDestroy(graph);
