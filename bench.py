@@ -29,6 +29,10 @@ sys.path.insert(0, ROOT)
 SEED = 20261203
 METRIC = "grid-point-steps/s, batched fwd+adjoint vs plain path, FP64 \u22641e-10 rel err"
 BYTES_PER_GPS_FWD = {"dr": 40, "cs": 96, "mcs": 96, "hv": 96}  # algorithmic bytes per grid-point-step (FP64)
+# DRAM bytes (read + write) per grid-point-step of the batched kernels from one ncu capture of
+# the 512-instance, 20-step case (profiles/k_batch_*_mcs512x20.md), scaled to a launch by the
+# grid-point-steps it processes: mode 0 = k_batch_forward, mode 1 = k_batch_fwdadj
+DRAM_BYTES_PER_GPS = {0: 303.0, 1: 1123.0}
 
 
 def parse():
@@ -349,7 +353,9 @@ def main():
                    "l2": f"inputs larger than L2 (line tables {total_n * 23 * 8 / 1e9:.1f} GB streamed every step)",
                    "parallelism": f"instance sharding x{world}" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "peak_source": peak_kind,
+                     "traffic": DRAM_BYTES_PER_GPS[mode] * gps, "traffic_unit": "bytes per launch",
+                     "traffic_source": "ncu dram__bytes_read+write of the 512-instance 20-step capture, per "
+                                       "grid-point-step, times this launch's grid-point-steps", "peak_source": peak_kind,
                      "algorithmic_bytes_per_grid_point_step": bpg,
                      "note": "FP64 pipe (1.196 TFLOP/s measured) binds before HBM on GB300"},
         "e2e": {"value": gps / e2e_s, "unit": "grid-point-steps/s", "h2d_bytes_per_step": int(total_n * 8),
@@ -361,7 +367,7 @@ def main():
     if cpu is not None:
         out["cpu_baseline"] = cpu
     if world == 1 and not args.no_plain:
-        out["plain_path"] = time_plain_path(lss, problems, stream, value)
+        out["plain_path"] = time_plain_path(lss, problems, stream, value, mode)
     print(json.dumps(out))
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -644,7 +650,7 @@ def run_config4(count=1024, sample=16):
           flush=True)
 
 
-def time_plain_path(lss, problems, stream, batched_value, m=64):
+def time_plain_path(lss, problems, stream, batched_value, mode, m=64):
     """The plain device path (one instance per launch sequence, kernel per sweep, FMA
     arithmetic) on a bounded sample of the same batch, for the batched/plain ratio."""
     import torch
@@ -666,9 +672,26 @@ def time_plain_path(lss, problems, stream, batched_value, m=64):
         torch.cuda.synchronize()
     secs = e0.elapsed_time(e1) * 1e-3
     plain = gps / secs
-    return {"value": plain, "unit": "grid-point-steps/s", "sample_instances": len(sample),
-            "how": "lss_adi_forward_graph per instance (kernel per sweep, graph replay), host copies per instance",
-            "batched_over_plain": batched_value / plain}
+    out = {"value": plain, "unit": "grid-point-steps/s", "sample_instances": len(sample),
+           "how": "lss_adi_forward_graph per instance (forward only; kernel per stage over the whole GPU, "
+                  "graph replay), host copies per instance",
+           "batched_over_plain": batched_value / plain}
+    if mode == 1:
+        # like for like: forward + adjoint through lss_adi_adjoint, one instance per call
+        sub = cpu_sample(problems, 16)
+        adj = [lss.ImplicitHestonSolver(p, precision="f64", arith="fast") for p in sub]
+        gps_a = sum(p.nx * p.ny * (p.nt - 1) for p in sub)
+        adj[0].adjoint(stream=sptr)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for s in adj:
+            s.adjoint(stream=sptr)
+        torch.cuda.synchronize()
+        plain_a = gps_a / (time.perf_counter() - t0)
+        out = {"value": plain_a, "unit": "grid-point-steps/s", "sample_instances": len(sub),
+               "how": "lss_adi_adjoint per instance (forward + adjoint, the same work as the batched run)",
+               "batched_over_plain": batched_value / plain_a, "forward_only": out}
+    return out
 
 
 def build_payoffs(problems, buf):
