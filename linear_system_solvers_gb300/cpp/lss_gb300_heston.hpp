@@ -11,9 +11,12 @@
 //                    heat_implicit_solver_config          pde_solvers/lss_*config*.hpp
 //   lss_pde_solvers::two_dimensional::implicit_solvers::general_heston_equation
 //                                             .../lss_2d_general_heston_equation.hpp:83-307
+//   lss_pde_solvers::two_dimensional::explicit_solvers::general_heston_equation
+//                                             .../lss_2d_general_heston_equation.hpp:317-510
 //   lss_pde_solvers::general_heston_equation_builder   builders/lss_2d_general_heston_equation_builder.hpp:57-128
-// solve() runs the device policy (tridiagonal_method_enum::GB300ThomasLUSolver on
-// memory_space_enum::Device) through the C-ABI of include/lss_adi.h: the user's coefficient
+// solve() runs the device policies (tridiagonal_method_enum::GB300ThomasLUSolver or
+// GB300DoubleSweepSolver on memory_space_enum::Device; the explicit Euler scheme) through the
+// C-ABI of include/lss_adi.h: the user's coefficient
 // functions are transformed to the computational grid and sampled exactly as the reference
 // does (lss_heat_data_transform.hpp:174-214, lss_2d_general_heston_equation_coefficients.hpp:89-98),
 // then handed to lss_adi_create_tabulated.  Host policies are not provided here (they stay in
@@ -53,11 +56,19 @@ namespace lss_enumerations {
 enum class by_enum { Row, Column };
 enum class factorization_enum { QRMethod, LUMethod, CholeskyMethod, None };
 enum class splitting_method_enum { DouglasRachford, CraigSneyd, ModifiedCraigSneyd, HundsdorferVerwer };
-enum class tridiagonal_method_enum { CUDASolver, DoubleSweepSolver, SORSolver, ThomasLUSolver, GB300ThomasLUSolver };
+enum class tridiagonal_method_enum {
+    CUDASolver,
+    DoubleSweepSolver,
+    SORSolver,
+    ThomasLUSolver,
+    GB300ThomasLUSolver,     // device policies of this library: Thomas LU ...
+    GB300DoubleSweepSolver   // ... and the double sweep (bit-identical to the host policies)
+};
 enum class grid_enum { Uniform, Nonuniform };
 enum class traverse_direction_enum { Forward, Backward };
 enum class memory_space_enum { Host, Device };
 enum class implicit_pde_schemes_enum { Euler, Theta_30, CrankNicolson, Theta_80 };
+enum class explicit_pde_schemes_enum { Euler, ADEBarakatClark, ADESaulyev };
 } // namespace lss_enumerations
 
 namespace lss_containers {
@@ -220,6 +231,25 @@ class heat_implicit_solver_config {
 };
 using heat_implicit_solver_config_ptr = std::shared_ptr<heat_implicit_solver_config>;
 
+// heat_explicit_solver_config (pde_solvers/lss_heat_solver_config.hpp:56-78)
+class heat_explicit_solver_config {
+    lss_enumerations::memory_space_enum mem_;
+    lss_enumerations::traverse_direction_enum dir_;
+    lss_enumerations::explicit_pde_schemes_enum sch_;
+
+  public:
+    heat_explicit_solver_config(lss_enumerations::memory_space_enum memory_space,
+                                lss_enumerations::traverse_direction_enum traverse_direction,
+                                lss_enumerations::explicit_pde_schemes_enum explicit_pde_scheme)
+        : mem_{memory_space}, dir_{traverse_direction}, sch_{explicit_pde_scheme}
+    {
+    }
+    lss_enumerations::memory_space_enum memory_space() const { return mem_; }
+    lss_enumerations::traverse_direction_enum traverse_direction() const { return dir_; }
+    lss_enumerations::explicit_pde_schemes_enum explicit_pde_scheme() const { return sch_; }
+};
+using heat_explicit_solver_config_ptr = std::shared_ptr<heat_explicit_solver_config>;
+
 namespace default_heat_solver_configs {
 // the device counterparts of the reference's host_bwd_tlusolver_*_solver_config_ptr
 inline heat_implicit_solver_config_ptr const dev_bwd_gb300_cn_solver_config_ptr =
@@ -232,9 +262,138 @@ inline heat_implicit_solver_config_ptr const dev_bwd_gb300_o8_solver_config_ptr 
         lss_enumerations::memory_space_enum::Device, lss_enumerations::traverse_direction_enum::Backward,
         lss_enumerations::tridiagonal_method_enum::GB300ThomasLUSolver, lss_enumerations::factorization_enum::None,
         lss_enumerations::implicit_pde_schemes_enum::Theta_80);
+// the reference's dev_expl_{fwd,bwd}_euler_solver_config_ptr (lss_heat_solver_config.hpp:244-252)
+inline heat_explicit_solver_config_ptr const dev_expl_fwd_euler_solver_config_ptr =
+    std::make_shared<heat_explicit_solver_config>(lss_enumerations::memory_space_enum::Device,
+                                                  lss_enumerations::traverse_direction_enum::Forward,
+                                                  lss_enumerations::explicit_pde_schemes_enum::Euler);
+inline heat_explicit_solver_config_ptr const dev_expl_bwd_euler_solver_config_ptr =
+    std::make_shared<heat_explicit_solver_config>(lss_enumerations::memory_space_enum::Device,
+                                                  lss_enumerations::traverse_direction_enum::Backward,
+                                                  lss_enumerations::explicit_pde_schemes_enum::Euler);
 } // namespace default_heat_solver_configs
 
 namespace two_dimensional {
+namespace detail {
+// The user's coefficient functions transformed to the computational grid and sampled exactly as
+// the reference does (lss_heat_data_transform.hpp:174-214, coefficients.hpp:89-98), the
+// boundaries and the terminal condition on the grid, then the device time loop through
+// lss_adi_create_tabulated / lss_adi_forward.  Coefficients and boundaries must not depend on t.
+template <typename T>
+void tabulated_solve(heat_data_config_2d_ptr<T> const &data, pde_discretization_config_2d_ptr<T> const &disc,
+                     lss_boundary::boundary_2d_ptr<T> const &ver, lss_boundary::boundary_2d_pair<T> const &hor,
+                     lss_grids::grid_config_hints_2d_ptr<T> const &hints, bool fwd, int scheme, int theta_scheme,
+                     double zeta, int arith, int options,
+                     lss_containers::container_2d<lss_enumerations::by_enum::Row, T> &solution)
+{
+    const auto sizes = disc->number_of_space_points();
+    const std::size_t nx = sizes.first, ny = sizes.second;
+    if (!(solution.rows() == nx && solution.columns() == ny))
+        throw std::invalid_argument("The input solution container must have the correct size");
+    const auto sp = disc->space_range();
+    const T one = T(1.0), two = T(2.0), half = T(0.5), quarter = T(0.25);
+    // sinh grid map (discretization/lss_grid_transform_config.hpp:118-149)
+    const T low1 = sp.first.lower(), high1 = sp.first.upper(), low2 = sp.second.lower(), high2 = sp.second.upper();
+    const T point = hints->accumulation_point();
+    T alpha = high1 - low1, beta = high2 - low2;
+    if (hints->grid() == lss_enumerations::grid_enum::Nonuniform) {
+        alpha = (point - low1) / hints->alpha_scale();
+        beta = (high2 - low2) / hints->beta_scale();
+    }
+    const T c0 = std::asinh((high1 - point) / alpha), c1 = std::asinh((low1 - point) / alpha);
+    const T dd = std::asinh((high2 - low2) / beta), cdiff = c0 - c1;
+    auto X = [&](T z) { return point + alpha * std::sinh(c0 * z + c1 * (one - z)); };
+    auto Y = [&](T e) { return low2 + beta * std::sinh(dd * e); };
+    auto Ad = [&](T z) { return alpha * cdiff * std::cosh(c0 * z + c1 * (one - z)); };
+    auto Bd = [&](T e) { return beta * dd * std::cosh(dd * e); };
+    auto Cd = [&](T z) { return alpha * cdiff * cdiff * std::sinh(c0 * z + c1 * (one - z)); };
+    auto Dd = [&](T e) { return beta * dd * dd * std::sinh(dd * e); };
+    // scheme scalars (implicit_coefficients/...coefficients.hpp:59-73)
+    const T k = disc->time_step();
+    const T h1 = one / static_cast<T>(nx - 1), h2 = one / static_cast<T>(ny - 1);
+    const T al = k / (h1 * h1), be = k / (h2 * h2), de = half * k / h1, ni = half * k / h2, rho = k;
+    (void)quarter;
+    const auto &cf = *data->coefficients;
+    const T t_first = fwd ? (disc->time_range().lower() + k) : (disc->time_range().upper() - k);
+    const T t_last = fwd ? disc->time_range().upper() : disc->time_range().lower() + k;
+    const std::size_t n = nx * ny;
+    auto fill = [&](T t, std::vector<T> &coef, std::vector<T> &v0) {
+        coef.assign(7 * n, T(0));
+        v0.assign(3 * nx, T(0));
+        for (std::size_t i = 0; i < nx; ++i) {
+            const T z = h1 * static_cast<T>(i);
+            for (std::size_t j = 0; j < ny; ++j) {
+                const T e = h2 * static_cast<T>(j);
+                const T x = X(z), y = Y(e);
+                const T av = Ad(z), bv = Bd(e);
+                const T A = cf.a(t, x, y), B = cf.b(t, x, y);
+                const T ah = A / (av * av), bh = B / (bv * bv), ch = cf.c(t, x, y) / (av * bv);
+                const T dh = cf.d(t, x, y) / av - (A * Cd(z)) / (av * av * av);
+                const T eh = cf.e(t, x, y) / bv - (B * Dd(e)) / (bv * bv * bv);
+                const T fh = cf.f(t, x, y);
+                const std::size_t o = i * ny + j;
+                coef[o] = al * ah - de * dh;
+                coef[n + o] = al * ah + de * dh;
+                coef[2 * n + o] = two * al * ah - half * rho * fh;
+                coef[3 * n + o] = be * bh - ni * eh;
+                coef[4 * n + o] = be * bh + ni * eh;
+                coef[5 * n + o] = two * be * bh - half * rho * fh;
+                coef[6 * n + o] = ch;
+                if (j == 0) {
+                    v0[i] = dh;
+                    v0[nx + i] = eh;
+                    v0[2 * nx + i] = fh;
+                }
+            }
+        }
+    };
+    std::vector<T> coef, v0, coef_last, v0_last;
+    fill(t_first, coef, v0);
+    fill(t_last, coef_last, v0_last);
+    if (coef != coef_last || v0 != v0_last)
+        throw std::invalid_argument("the device policy needs time-invariant coefficients");
+    // boundaries on the computational grid (lss_heston_boundary_transform.hpp:47-65)
+    std::vector<T> slo(ny), neu(ny), vhi(nx), pay(n);
+    const T A1 = Ad(one);
+    for (std::size_t j = 0; j < ny; ++j) {
+        const T y = Y(h2 * static_cast<T>(j));
+        slo[j] = hor.first->value(t_first, y);
+        neu[j] = hor.second->value(t_first, y) * A1;
+        if (slo[j] != hor.first->value(t_last, y) || hor.second->value(t_first, y) != hor.second->value(t_last, y))
+            throw std::invalid_argument("the device policy needs time-invariant boundary values");
+    }
+    for (std::size_t i = 0; i < nx; ++i) {
+        const T x = X(h1 * static_cast<T>(i));
+        vhi[i] = ver->value(t_first, x);
+        for (std::size_t j = 0; j < ny; ++j) pay[i * ny + j] = data->initial->initial_condition(x, Y(h2 * static_cast<T>(j)));
+    }
+    lss_adi_tables t{};
+    t.nx = static_cast<int>(nx);
+    t.ny = static_cast<int>(ny);
+    t.nt = static_cast<int>(disc->number_of_time_points());
+    t.t_lo = static_cast<double>(disc->time_range().lower());
+    t.t_hi = static_cast<double>(disc->time_range().upper());
+    t.scheme = scheme;
+    t.theta_scheme = theta_scheme;
+    t.forward = fwd ? 1 : 0;
+    t.precision = std::is_same<T, double>::value ? LSS_ADI_FP64 : LSS_ADI_FP32;
+    t.arith = arith;
+    t.zeta = zeta;
+    t.coef = coef.data();
+    t.coef_v0 = v0.data();
+    t.s_lo_dirichlet = slo.data();
+    t.s_hi_neumann = neu.data();
+    t.v_hi_dirichlet = vhi.data();
+    t.payoff = pay.data();
+    t.options = options;
+    lss_adi_handle *h = nullptr;
+    if (lss_adi_create_tabulated(&t, &h) != LSS_ADI_OK) throw std::runtime_error(lss_adi_last_error());
+    const int rc = lss_adi_forward(h, nullptr, solution.data(), nullptr, 0, nullptr);
+    lss_adi_destroy(h);
+    if (rc != LSS_ADI_OK) throw std::runtime_error(lss_adi_last_error());
+}
+} // namespace detail
+
 namespace implicit_solvers {
 
 /*
@@ -285,94 +444,15 @@ template <typename T> class general_heston_equation {
         verify(cfg_ != nullptr, "solver_config must not be null");
         verify(hints_ != nullptr, "grid_config_hints must not be null");
         if (cfg_->memory_space() != lss_enumerations::memory_space_enum::Device ||
-            cfg_->tridiagonal_method() != lss_enumerations::tridiagonal_method_enum::GB300ThomasLUSolver)
-            throw std::invalid_argument("this front end runs the Device/GB300ThomasLUSolver policy only; "
-                                        "host policies stay in the reference library");
+            (cfg_->tridiagonal_method() != lss_enumerations::tridiagonal_method_enum::GB300ThomasLUSolver &&
+             cfg_->tridiagonal_method() != lss_enumerations::tridiagonal_method_enum::GB300DoubleSweepSolver))
+            throw std::invalid_argument("this front end runs the Device/GB300ThomasLUSolver and "
+                                        "Device/GB300DoubleSweepSolver policies only; host policies stay in the "
+                                        "reference library");
     }
 
     void solve(lss_containers::container_2d<lss_enumerations::by_enum::Row, T> &solution)
     {
-        const auto sizes = disc_->number_of_space_points();
-        const std::size_t nx = sizes.first, ny = sizes.second;
-        verify(solution.rows() == nx && solution.columns() == ny, "The input solution container must have the correct size");
-        const auto sp = disc_->space_range();
-        const T one = T(1.0), two = T(2.0), half = T(0.5), quarter = T(0.25);
-        // sinh grid map (discretization/lss_grid_transform_config.hpp:118-149)
-        const T low1 = sp.first.lower(), high1 = sp.first.upper(), low2 = sp.second.lower(), high2 = sp.second.upper();
-        const T point = hints_->accumulation_point();
-        T alpha = high1 - low1, beta = high2 - low2;
-        if (hints_->grid() == lss_enumerations::grid_enum::Nonuniform) {
-            alpha = (point - low1) / hints_->alpha_scale();
-            beta = (high2 - low2) / hints_->beta_scale();
-        }
-        const T c0 = std::asinh((high1 - point) / alpha), c1 = std::asinh((low1 - point) / alpha);
-        const T dd = std::asinh((high2 - low2) / beta), cdiff = c0 - c1;
-        auto X = [&](T z) { return point + alpha * std::sinh(c0 * z + c1 * (one - z)); };
-        auto Y = [&](T e) { return low2 + beta * std::sinh(dd * e); };
-        auto Ad = [&](T z) { return alpha * cdiff * std::cosh(c0 * z + c1 * (one - z)); };
-        auto Bd = [&](T e) { return beta * dd * std::cosh(dd * e); };
-        auto Cd = [&](T z) { return alpha * cdiff * cdiff * std::sinh(c0 * z + c1 * (one - z)); };
-        auto Dd = [&](T e) { return beta * dd * dd * std::sinh(dd * e); };
-        // scheme scalars (implicit_coefficients/...coefficients.hpp:59-73)
-        const T k = disc_->time_step();
-        const T h1 = one / static_cast<T>(nx - 1), h2 = one / static_cast<T>(ny - 1);
-        const T al = k / (h1 * h1), be = k / (h2 * h2), de = half * k / h1, ni = half * k / h2, rho = k;
-        (void)quarter;
-        const auto &cf = *data_->coefficients;
-        const bool fwd = cfg_->traverse_direction() == lss_enumerations::traverse_direction_enum::Forward;
-        const T t_first = fwd ? (disc_->time_range().lower() + k) : (disc_->time_range().upper() - k);
-        const T t_last = fwd ? disc_->time_range().upper() : disc_->time_range().lower() + k;
-        const std::size_t n = nx * ny;
-        auto fill = [&](T t, std::vector<T> &coef, std::vector<T> &v0) {
-            coef.assign(7 * n, T(0));
-            v0.assign(3 * nx, T(0));
-            for (std::size_t i = 0; i < nx; ++i) {
-                const T z = h1 * static_cast<T>(i);
-                for (std::size_t j = 0; j < ny; ++j) {
-                    const T e = h2 * static_cast<T>(j);
-                    const T x = X(z), y = Y(e);
-                    const T av = Ad(z), bv = Bd(e);
-                    const T A = cf.a(t, x, y), B = cf.b(t, x, y);
-                    const T ah = A / (av * av), bh = B / (bv * bv), ch = cf.c(t, x, y) / (av * bv);
-                    const T dh = cf.d(t, x, y) / av - (A * Cd(z)) / (av * av * av);
-                    const T eh = cf.e(t, x, y) / bv - (B * Dd(e)) / (bv * bv * bv);
-                    const T fh = cf.f(t, x, y);
-                    const std::size_t o = i * ny + j;
-                    coef[o] = al * ah - de * dh;
-                    coef[n + o] = al * ah + de * dh;
-                    coef[2 * n + o] = two * al * ah - half * rho * fh;
-                    coef[3 * n + o] = be * bh - ni * eh;
-                    coef[4 * n + o] = be * bh + ni * eh;
-                    coef[5 * n + o] = two * be * bh - half * rho * fh;
-                    coef[6 * n + o] = ch;
-                    if (j == 0) {
-                        v0[i] = dh;
-                        v0[nx + i] = eh;
-                        v0[2 * nx + i] = fh;
-                    }
-                }
-            }
-        };
-        std::vector<T> coef, v0, coef_last, v0_last;
-        fill(t_first, coef, v0);
-        fill(t_last, coef_last, v0_last);
-        if (coef != coef_last || v0 != v0_last)
-            throw std::invalid_argument("the device policy needs time-invariant coefficients");
-        // boundaries on the computational grid (lss_heston_boundary_transform.hpp:47-65)
-        std::vector<T> slo(ny), neu(ny), vhi(nx), pay(n);
-        const T A1 = Ad(one);
-        for (std::size_t j = 0; j < ny; ++j) {
-            const T y = Y(h2 * static_cast<T>(j));
-            slo[j] = hor_.first->value(t_first, y);
-            neu[j] = hor_.second->value(t_first, y) * A1;
-            if (slo[j] != hor_.first->value(t_last, y) || hor_.second->value(t_first, y) != hor_.second->value(t_last, y))
-                throw std::invalid_argument("the device policy needs time-invariant boundary values");
-        }
-        for (std::size_t i = 0; i < nx; ++i) {
-            const T x = X(h1 * static_cast<T>(i));
-            vhi[i] = ver_->value(t_first, x);
-            for (std::size_t j = 0; j < ny; ++j) pay[i * ny + j] = data_->initial->initial_condition(x, Y(h2 * static_cast<T>(j)));
-        }
         int scheme = 0;
         switch (split_->splitting_method()) {
         case lss_enumerations::splitting_method_enum::DouglasRachford: scheme = LSS_ADI_DOUGLAS_RACHFORD; break;
@@ -380,33 +460,72 @@ template <typename T> class general_heston_equation {
         case lss_enumerations::splitting_method_enum::ModifiedCraigSneyd: scheme = LSS_ADI_MODIFIED_CRAIG_SNEYD; break;
         default: scheme = LSS_ADI_HUNDSDORFER_VERWER; break;
         }
-        lss_adi_tables t{};
-        t.nx = static_cast<int>(nx);
-        t.ny = static_cast<int>(ny);
-        t.nt = static_cast<int>(disc_->number_of_time_points());
-        t.t_lo = static_cast<double>(disc_->time_range().lower());
-        t.t_hi = static_cast<double>(disc_->time_range().upper());
-        t.scheme = scheme;
-        t.theta_scheme = static_cast<int>(cfg_->implicit_pde_scheme());
-        t.forward = fwd ? 1 : 0;
-        t.precision = std::is_same<T, double>::value ? LSS_ADI_FP64 : LSS_ADI_FP32;
-        t.arith = arith_;
-        t.zeta = static_cast<double>(split_->weighting_value());
-        t.coef = coef.data();
-        t.coef_v0 = v0.data();
-        t.s_lo_dirichlet = slo.data();
-        t.s_hi_neumann = neu.data();
-        t.v_hi_dirichlet = vhi.data();
-        t.payoff = pay.data();
-        lss_adi_handle *h = nullptr;
-        if (lss_adi_create_tabulated(&t, &h) != LSS_ADI_OK) throw std::runtime_error(lss_adi_last_error());
-        const int rc = lss_adi_forward(h, nullptr, solution.data(), nullptr, 0, nullptr);
-        lss_adi_destroy(h);
-        if (rc != LSS_ADI_OK) throw std::runtime_error(lss_adi_last_error());
+        const bool fwd = cfg_->traverse_direction() == lss_enumerations::traverse_direction_enum::Forward;
+        const int options =
+            cfg_->tridiagonal_method() == lss_enumerations::tridiagonal_method_enum::GB300DoubleSweepSolver
+                ? LSS_ADI_OPT_DOUBLE_SWEEP
+                : 0;
+        detail::tabulated_solve<T>(data_, disc_, ver_, hor_, hints_, fwd, scheme, static_cast<int>(cfg_->implicit_pde_scheme()),
+                                   static_cast<double>(split_->weighting_value()), arith_, options, solution);
+    }
+};
+} // namespace implicit_solvers
+
+namespace explicit_solvers {
+
+/*
+ * explicit_solvers::general_heston_equation (lss_2d_general_heston_equation.hpp:317-510) with
+ * the device explicit Euler scheme: the whole time loop runs on the GPU with the coefficients
+ * resident there.  arith: LSS_ADI_ARITH_REFERENCE (bit-identical to the reference's host
+ * Euler scheme) or LSS_ADI_ARITH_FAST.  Stability is the caller's, as in the reference.
+ */
+template <typename T> class general_heston_equation {
+    heat_data_config_2d_ptr<T> data_;
+    pde_discretization_config_2d_ptr<T> disc_;
+    lss_boundary::boundary_2d_ptr<T> ver_;
+    lss_boundary::boundary_2d_pair<T> hor_;
+    lss_grids::grid_config_hints_2d_ptr<T> hints_;
+    heat_explicit_solver_config_ptr cfg_;
+    int arith_;
+
+  public:
+    general_heston_equation(heat_data_config_2d_ptr<T> const &heat_data_config,
+                            pde_discretization_config_2d_ptr<T> const &discretization_config,
+                            lss_boundary::boundary_2d_ptr<T> const &vertical_upper_boundary_ptr,
+                            lss_boundary::boundary_2d_pair<T> const &horizontal_boundary_pair,
+                            lss_grids::grid_config_hints_2d_ptr<T> const &grid_config_hints,
+                            heat_explicit_solver_config_ptr const &solver_config =
+                                default_heat_solver_configs::dev_expl_fwd_euler_solver_config_ptr,
+                            int arith = LSS_ADI_ARITH_REFERENCE)
+        : data_{heat_data_config}, disc_{discretization_config}, ver_{vertical_upper_boundary_ptr},
+          hor_{horizontal_boundary_pair}, hints_{grid_config_hints}, cfg_{solver_config}, arith_{arith}
+    {
+        // the checks of the reference's initialize (lss_2d_general_heston_equation.hpp:375-402)
+        if (!data_) throw std::invalid_argument("heat_data_config must not be null");
+        if (!disc_) throw std::invalid_argument("discretization_config must not be null");
+        if (!std::dynamic_pointer_cast<lss_boundary::dirichlet_boundary_2d<T>>(ver_))
+            throw std::invalid_argument("vertical_upper_boundary_ptr must be of dirichlet type only");
+        if (!std::dynamic_pointer_cast<lss_boundary::dirichlet_boundary_2d<T>>(hor_.first))
+            throw std::invalid_argument("horizontal_boundary_pair.first must be of dirichlet type only");
+        if (!std::dynamic_pointer_cast<lss_boundary::neumann_boundary_2d<T>>(hor_.second))
+            throw std::invalid_argument("horizontal_boundary_pair.second must be of neumann type only");
+        if (!cfg_) throw std::invalid_argument("solver_config must not be null");
+        if (!hints_) throw std::invalid_argument("grid_config_hints must not be null");
+        if (cfg_->memory_space() != lss_enumerations::memory_space_enum::Device ||
+            cfg_->explicit_pde_scheme() != lss_enumerations::explicit_pde_schemes_enum::Euler)
+            throw std::invalid_argument("this front end runs the Device explicit Euler scheme only "
+                                        "(the reference supports no other on the device either)");
+    }
+
+    void solve(lss_containers::container_2d<lss_enumerations::by_enum::Row, T> &solution)
+    {
+        const bool fwd = cfg_->traverse_direction() == lss_enumerations::traverse_direction_enum::Forward;
+        detail::tabulated_solve<T>(data_, disc_, ver_, hor_, hints_, fwd, LSS_ADI_EXPLICIT_EULER, LSS_ADI_CRANK_NICOLSON,
+                                   0.5, arith_, 0, solution);
     }
 };
 
-} // namespace implicit_solvers
+} // namespace explicit_solvers
 } // namespace two_dimensional
 
 template <typename T> class general_heston_equation_builder {

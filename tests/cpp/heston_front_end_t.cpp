@@ -5,7 +5,9 @@
 //
 // usage: heston_front_end_t <f32|f64> <dr|cs|mcs|hv> nx ny nt kappa theta sigma rho rate
 //        strike maturity s_lo s_hi v_lo v_hi zeta theta_scheme nonuniform acc alpha_s beta_s
-//        arith(0 fast|1 reference) builder(0|1) out.bin
+//        arith(0 fast|1 reference) builder(0|1) method(tlu|ds|euler) out.bin
+// method: tridiagonal_method_enum::GB300ThomasLUSolver / GB300DoubleSweepSolver, or the
+// explicit_solvers::general_heston_equation with the device explicit Euler scheme.
 #include <cstdio>
 #include <cstdlib>
 #include <string>
@@ -43,6 +45,7 @@ template <typename T> static int run(int argc, char **argv)
     const int theta_scheme = std::atoi(argv[k++]), nonuniform = std::atoi(argv[k++]);
     const double acc = std::atof(argv[k++]), alpha_s = std::atof(argv[k++]), beta_s = std::atof(argv[k++]);
     const int arith = std::atoi(argv[k++]), use_builder = std::atoi(argv[k++]);
+    const std::string method = argv[k++];
     const std::string out = argv[k++];
     (void)argc;
 
@@ -79,12 +82,19 @@ template <typename T> static int run(int argc, char **argv)
         nonuniform ? grid_enum::Nonuniform : grid_enum::Uniform);
     auto const solver_cfg = std::make_shared<heat_implicit_solver_config>(
         lss_enumerations::memory_space_enum::Device, lss_enumerations::traverse_direction_enum::Backward,
-        lss_enumerations::tridiagonal_method_enum::GB300ThomasLUSolver, lss_enumerations::factorization_enum::None,
-        static_cast<lss_enumerations::implicit_pde_schemes_enum>(theta_scheme));
+        method == "ds" ? lss_enumerations::tridiagonal_method_enum::GB300DoubleSweepSolver
+                       : lss_enumerations::tridiagonal_method_enum::GB300ThomasLUSolver,
+        lss_enumerations::factorization_enum::None, static_cast<lss_enumerations::implicit_pde_schemes_enum>(theta_scheme));
 
     container_2d<by_enum::Row, T> solution(Sd, Vd, T{});
     try {
-        if (use_builder) {
+        if (method == "euler") {
+            lss_pde_solvers::two_dimensional::explicit_solvers::general_heston_equation<T> pdesolver(
+                heat_data_ptr, discretization_ptr, vertical_upper_boundary_ptr, horizontal_boundary_pair,
+                grid_config_hints_ptr, lss_pde_solvers::default_heat_solver_configs::dev_expl_bwd_euler_solver_config_ptr,
+                arith);
+            pdesolver.solve(solution);
+        } else if (use_builder) {
             auto pdesolver = lss_pde_solvers::general_heston_equation_builder<T>()
                                  .heat_data_config(heat_data_ptr)
                                  .discretization_config(discretization_ptr)
@@ -114,8 +124,8 @@ template <typename T> static int run(int argc, char **argv)
 
 int main(int argc, char **argv)
 {
-    if (argc != 26) {
-        std::fprintf(stderr, "heston_front_end_t: expected 25 arguments, got %d\n", argc - 1);
+    if (argc != 27) {
+        std::fprintf(stderr, "heston_front_end_t: expected 26 arguments, got %d\n", argc - 1);
         return 2;
     }
     return std::string(argv[1]) == "f32" ? run<float>(argc, argv) : run<double>(argc, argv);

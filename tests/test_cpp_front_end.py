@@ -29,10 +29,10 @@ def test_front_end_compiles_against_the_c_abi(front_end_binary):
     assert os.access(front_end_binary, os.X_OK)
     # wrong argument count is reported, not crashed on
     res = subprocess.run([front_end_binary], capture_output=True, text=True)
-    assert res.returncode == 2 and "expected 25 arguments" in res.stderr
+    assert res.returncode == 2 and "expected 26 arguments" in res.stderr
 
 
-def run_front_end(binary, kw, fp, arith, builder):
+def run_front_end(binary, kw, fp, arith, builder, method="tlu"):
     thetas = {"euler": 0, "theta30": 1, "cn": 2, "theta80": 3}
     with tempfile.TemporaryDirectory() as td:
         out = os.path.join(td, "v.bin")
@@ -42,7 +42,7 @@ def run_front_end(binary, kw, fp, arith, builder):
         args += [repr(float(kw.get("zeta", 0.5))), str(thetas[kw.get("theta_scheme", "cn")]),
                  str(int(kw.get("nonuniform", False))), repr(float(kw.get("acc_point", 0.0))),
                  repr(float(kw.get("alpha_scale", 3.0))), repr(float(kw.get("beta_scale", 50.0))), str(arith),
-                 str(builder), out]
+                 str(builder), method, out]
         res = subprocess.run(args, capture_output=True, text=True)
         assert res.returncode == 0, res.stderr
         dt = np.float32 if fp == "f32" else np.float64
@@ -69,3 +69,23 @@ def test_front_end_config1_fast(front_end_binary, oracle):
     got = run_front_end(front_end_binary, dict(CONFIG1), "f64", arith=0, builder=0)
     want = oracle.solve(oracle.Problem(**CONFIG1), "f64")
     assert rel_err(got, want) < 1e-10
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("scheme,fp", [("dr", "f64"), ("mcs", "f32"), ("hv", "f64")])
+def test_front_end_double_sweep_policy_bitwise(front_end_binary, oracle, scheme, fp):
+    # tridiagonal_method_enum::GB300DoubleSweepSolver against the reference's DoubleSweepSolver
+    kw = dict(CONFIG1, scheme=scheme, nx=50, ny=26, nt=31, **(NU if scheme != "dr" else {}))
+    got = run_front_end(front_end_binary, kw, fp, arith=1, builder=0, method="ds")
+    want = oracle.solve(oracle.Problem(**kw, solver="ds"), fp)
+    assert np.array_equal(got, want, equal_nan=True)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fp", ["f64", "f32"])
+def test_front_end_explicit_euler_bitwise(front_end_binary, oracle, fp):
+    # explicit_solvers::general_heston_equation with the device explicit Euler scheme
+    kw = dict(CONFIG1, scheme="euler", rho=-0.5, nx=30, ny=20, nt=401, maturity=0.25)
+    got = run_front_end(front_end_binary, kw, fp, arith=1, builder=0, method="euler")
+    want = oracle.solve(oracle.Problem(**kw), fp)
+    assert np.array_equal(got, want, equal_nan=True)
