@@ -272,6 +272,42 @@ __device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d
     }
 }
 
+// B1^T at grid point (p, q <= 2): the adjoint of the explicit v = v_lo boundary column, whose
+// values are the lo ends of the v lines (bbar0(i) = sum of LV over lines i' with imap[i'] = i),
+// with its parameter sensitivities (D, E, F of the v = v_lo line) at q = 0.
+__device__ __forceinline__ double adj_b1_terms(const inst_view<double> &v, const bdesc &d, const double *__restrict__ U,
+                                               const double *__restrict__ LV, adj_acc &acc, double tau, int p, int q)
+{
+    const int nx = v.nx, ny = v.ny;
+    auto B0 = [&](int i) -> double {
+        if (i < 1 || i > nx - 2) return 0.0;
+        double sum = 0.0;
+        if (__ldg(v.imap() + i) == i) sum += LV[i];
+        if (i + 1 <= nx - 2 && __ldg(v.imap() + i + 1) == i) sum += LV[i + 1];
+        return sum;
+    };
+    const long long o = (long long)p * ny + q;
+    if (q == 1) return __ldg(v.X(XB_1) + p) * B0(p);
+    if (q == 2) return __ldg(v.X(XB_2) + p) * B0(p);
+    const double val = (p + 1 <= nx - 2 ? __ldg(v.X(XB_M) + p + 1) * B0(p + 1) : 0.0) + __ldg(v.X(XB_C) + p) * B0(p) +
+                       (p >= 1 ? __ldg(v.X(XB_P) + p - 1) * B0(p - 1) : 0.0);
+    if (p >= 1 && p <= nx - 2) {
+        const double bb = B0(p);
+        if (bb != 0.0) {
+            const double u0 = U[o], u1 = U[o + 1], u2 = U[o + 2];
+            const double um = U[o - ny], up = U[o + ny];
+            const double ee = d.a_ni * bb * (4.0 * u1 - 3.0 * u0 - u2);
+            double hd = __ldg(v.X(X_HX) + p);
+            if (d.model == LSS_ADI_SABR) hd += 2.0 * d.a_omb * tau * __ldg(v.Yv(Y_HV2)) * __ldg(v.X(X_HDD) + p);
+            acc.s[0] += bb * (d.a_delta * hd * (up - um) - d.a_k * u0);
+            acc.s[1] += ee * __ldg(v.Yv(Y_EK));
+            acc.s[2] += ee * __ldg(v.Yv(Y_ET));
+            acc.s[3] += ee * __ldg(v.Yv(Y_ES));
+        }
+    }
+    return val;
+}
+
 // Gather: cross-line right-hand-side adjoints of an S stage into UB (and Y2B for KIND 2), the
 // lo/hi adjoints of the S lines (lsum / hsum of column q, added on rows 0 / nx-1), and for
 // KIND 1 the adjoint of the explicit v = v_lo boundary column (B1^T) with its parameter
@@ -289,14 +325,6 @@ __device__ __forceinline__ void adj_gather_point(const inst_view<double> &v, con
     auto W = [&](int slot, int a, int b) -> double {
         return (a >= 1 && a <= nx - 2 && b >= 1 && b <= ny - 2) ? __ldg(v.S(slot) + (long long)a * ny + b) : 0.0;
     };
-    // lo-value adjoint of the explicit boundary column: bbar0(i) = sum over v lines i' with imap[i'] = i
-    auto B0 = [&](int i) -> double {
-        if (i < 1 || i > nx - 2) return 0.0;
-        double sum = 0.0;
-        if (__ldg(v.imap() + i) == i) sum += LV[i];
-        if (i + 1 <= nx - 2 && __ldg(v.imap() + i + 1) == i) sum += LV[i + 1];
-        return sum;
-    };
     const long long o = (long long)p * ny + q;
     double val = 0.0;
     if constexpr (KIND == 2) {
@@ -313,30 +341,7 @@ __device__ __forceinline__ void adj_gather_point(const inst_view<double> &v, con
                W(SL_WN, p, q - 1) * F(p, q - 1) + W(SL_WC, p, q) * F(p, q) + W(SL_WG, p + 1, q + 1) * F(p + 1, q + 1) -
                W(SL_WG, p + 1, q - 1) * F(p + 1, q - 1) - W(SL_WG, p - 1, q + 1) * F(p - 1, q + 1) +
                W(SL_WG, p - 1, q - 1) * F(p - 1, q - 1);
-        if (q <= 2) {
-            if (q == 0) {
-                val += (p + 1 <= nx - 2 ? __ldg(v.X(XB_M) + p + 1) * B0(p + 1) : 0.0) + __ldg(v.X(XB_C) + p) * B0(p) +
-                       (p >= 1 ? __ldg(v.X(XB_P) + p - 1) * B0(p - 1) : 0.0);
-                if (p >= 1 && p <= nx - 2) {
-                    const double bb = B0(p);
-                    if (bb != 0.0) {
-                        const double u0 = U[o], u1 = U[o + 1], u2 = U[o + 2];
-                        const double um = U[o - ny], up = U[o + ny];
-                        const double ee = d.a_ni * bb * (4.0 * u1 - 3.0 * u0 - u2);
-                        double hd = __ldg(v.X(X_HX) + p);
-                        if (d.model == LSS_ADI_SABR) hd += 2.0 * d.a_omb * tau * __ldg(v.Yv(Y_HV2)) * __ldg(v.X(X_HDD) + p);
-                        acc.s[0] += bb * (d.a_delta * hd * (up - um) - d.a_k * u0);
-                        acc.s[1] += ee * __ldg(v.Yv(Y_EK));
-                        acc.s[2] += ee * __ldg(v.Yv(Y_ET));
-                        acc.s[3] += ee * __ldg(v.Yv(Y_ES));
-                    }
-                }
-            } else if (q == 1) {
-                val += __ldg(v.X(XB_1) + p) * B0(p);
-            } else {
-                val += __ldg(v.X(XB_2) + p) * B0(p);
-            }
-        }
+        if (q <= 2) val += adj_b1_terms(v, d, U, LV, acc, tau, p, q);
     }
     if (p == 0) val += lsum;
     if (p == nx - 1) val += hsum;
@@ -354,7 +359,15 @@ __device__ __forceinline__ void adj_line_ends(const inst_view<double> &v, const 
     if (q + 1 <= ny - 2 && __ldg(v.jmap() + q + 1) == q) { lsum += LS[q + 1]; hsum += HS[q + 1]; }
 }
 
-// Gather pass over columns q (thread per column).
+// Gather pass over columns q (thread per column), walking down the column with a window of three
+// rows.  The transposed stencil at (p, q) is  down(p+1) + up(p-1) + mid(p)  where each row r
+// contributes, from FB and the weight tables at columns q-1, q, q+1 of that row,
+//   KIND 1:  down = WW F + g+ - g-,  up = WE F - g+ + g-,  mid = WS(q+1) F(q+1) + WN(q-1) F(q-1) + WC F
+//            with g+- = WG(q+-1) F(q+-1)   (mixed term of the explicit operator);
+//   KIND 2:  the same with S2MZ for WG and, for MCS/HV, X1 / X3 / X2, X4, X5 for WW / WE / WC, WS, WN.
+// FB and the tables are zero on the boundary rows and columns of an instance (never written), so
+// only the rows and columns outside the instance need guards.  Each row's table and FB values are
+// loaded once instead of once per neighbour.
 template <int KIND>
 __device__ __forceinline__ void adj_gather(const inst_view<double> &v, const bdesc &d, const double *__restrict__ U,
                                            const double *__restrict__ FB, const double *__restrict__ LS,
@@ -363,11 +376,59 @@ __device__ __forceinline__ void adj_gather(const inst_view<double> &v, const bde
                                            int l0, int ls)
 {
     const int nx = v.nx, ny = v.ny;
+    const bool xterms = KIND == 2 && d.scheme != LSS_ADI_CRAIG_SNEYD;
+    const bool hv = d.scheme == LSS_ADI_HUNDSDORFER_VERWER;
+    const double *WG = v.S(KIND == 1 ? SL_WG : SL_S2MZ);
+    const double *WD = v.S(KIND == 1 ? SL_WW : SL_X1), *WU = v.S(KIND == 1 ? SL_WE : SL_X3);
+    const double *WM = v.S(KIND == 1 ? SL_WC : SL_X2), *WR = v.S(KIND == 1 ? SL_WS : SL_X4);
+    const double *WL = v.S(KIND == 1 ? SL_WN : SL_X5);
     for (int q = l0; q < ny; q += ls) {
         double lsum, hsum;
         adj_line_ends(v, LS, HS, q, lsum, hsum);
+        const bool ql = q >= 1, qr = q + 1 <= ny - 1;
+        auto row = [&](int r, double &dn, double &up, double &mid) {
+            if (r < 0 || r > nx - 1) {
+                dn = up = mid = 0.0;
+                return;
+            }
+            const long long o = (long long)r * ny + q;
+            const double f0 = FB[o], fm = ql ? FB[o - 1] : 0.0, fp = qr ? FB[o + 1] : 0.0;
+            const double gp = qr ? __ldg(WG + o + 1) * fp : 0.0, gm = ql ? __ldg(WG + o - 1) * fm : 0.0;
+            if (KIND == 1 || xterms) {
+                dn = __ldg(WD + o) * f0 + gp - gm;
+                up = __ldg(WU + o) * f0 - gp + gm;
+                mid = (qr ? __ldg(WR + o + 1) * fp : 0.0) + (ql ? __ldg(WL + o - 1) * fm : 0.0) + __ldg(WM + o) * f0;
+            } else {
+                dn = gp - gm;
+                up = gm - gp;
+                mid = 0.0;
+            }
+        };
+        double up_m = 0.0;          // up of row p-1 (no row above row 0)
+        double dn_c, up_c, mid_c;   // row p (its down term is used one row earlier)
+        double dn_p, up_p, mid_p;   // row p+1
+        row(0, dn_c, up_c, mid_c);
 #pragma unroll 2
-        for (int p = 0; p < nx; ++p) adj_gather_point<KIND>(v, d, U, FB, LV, UB, Y2B, acc, tau, p, q, lsum, hsum);
+        for (int p = 0; p < nx; ++p) {
+            row(p + 1, dn_p, up_p, mid_p);
+            const long long o = (long long)p * ny + q;
+            double val;
+            if constexpr (KIND == 2) {
+                const double db = dn_p + up_m + mid_c;
+                // HV: rows 1..nx-2 already hold the last v stage's adjoint of its input Y2
+                if (hv && p >= 1 && p <= nx - 2) Y2B[o] += db; else Y2B[o] = db;
+                val = -db;
+            } else {
+                val = dn_p + up_m + mid_c;
+                if (q <= 2) val += adj_b1_terms(v, d, U, LV, acc, tau, p, q);
+            }
+            if (p == 0) val += lsum;
+            if (p == nx - 1) val += hsum;
+            UB[o] += val;
+            up_m = up_c;
+            up_c = up_p;
+            mid_c = mid_p;
+        }
     }
 }
 
