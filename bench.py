@@ -268,7 +268,7 @@ def main():
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    from linear_system_solvers_gb300.sharding import max_over_ranks, rank_seed
+    from linear_system_solvers_gb300.sharding import max_over_ranks, rank_seed, sum_over_ranks
 
     problems = problems_all if rank == 0 else cap_time_steps(draw_batch(args.count, seed=rank_seed(SEED, rank)),
                                                              args.max_time_steps)
@@ -331,10 +331,11 @@ def main():
     e2e_ok = bool(np.allclose(vals_h, values, rtol=1e-12, atol=1e-12))
 
     t_max, e2e_s = max_over_ranks([ms, e2e_s], device="cuda")
+    (gps_all,) = sum_over_ranks([float(gps)], device="cuda")  # every rank's own batch (weak scaling)
     if rank != 0:
         torch.distributed.destroy_process_group()
         return
-    value = gps * world / (t_max * 1e-3)
+    value = gps_all / (t_max * 1e-3)
     bpg = BYTES_PER_GPS_FWD["mcs"] * (1 if mode == 0 else 10.0 / 3.0)
     peak, peak_kind = measured_peaks()
     achieved = gps * bpg / (ms * 1e-3) / 1e9
@@ -358,7 +359,7 @@ def main():
                                        "grid-point-step, times this launch's grid-point-steps", "peak_source": peak_kind,
                      "algorithmic_bytes_per_grid_point_step": bpg,
                      "note": "FP64 pipe (1.196 TFLOP/s measured) binds before HBM on GB300"},
-        "e2e": {"value": gps / e2e_s, "unit": "grid-point-steps/s", "h2d_bytes_per_step": int(total_n * 8),
+        "e2e": {"value": gps_all / e2e_s, "unit": "grid-point-steps/s", "h2d_bytes_per_step": int(total_n * 8),
                 "d2h_bytes_per_step": int(len(problems) * 8 * (6 if mode == 1 else 1)), "matches_device_values": e2e_ok},
         "gpu_launches": launches,
         "clocks": clk.summary(),

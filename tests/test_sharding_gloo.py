@@ -1,5 +1,5 @@
-"""Multi-rank logic on CPU (gloo, world_size 2): instance sharding and the max-over-ranks
-timing reduction used by bench.py under torchrun."""
+"""Multi-rank logic on CPU (gloo, world_size 2): instance sharding, the max-over-ranks timing
+reduction and the sum of the ranks' work used by bench.py under torchrun."""
 import os
 import socket
 
@@ -21,12 +21,13 @@ def _worker(rank, world, port, out):
     os.environ["MASTER_PORT"] = str(port)
     dist.init_process_group("gloo", rank=rank, world_size=world)
     from linear_system_solvers_gb300.batch import draw_batch
-    from linear_system_solvers_gb300.sharding import max_over_ranks, rank_seed, shard_lpt
+    from linear_system_solvers_gb300.sharding import max_over_ranks, rank_seed, shard_lpt, sum_over_ranks
 
     mine = draw_batch(8, seed=rank_seed(20261203, rank))
     times = max_over_ranks([1.0 + rank, 10.0 - rank])
+    work = sum_over_ranks([float(100 + rank)])
     shards = shard_lpt(draw_batch(64), world)
-    out.put((rank, mine[0].kappa, times, shards[rank]))
+    out.put((rank, mine[0].kappa, times + work, shards[rank]))
     dist.destroy_process_group()
 
 
@@ -45,7 +46,7 @@ def test_two_rank_gloo_sharding_and_max():
         assert p.exitcode == 0
     (r0, k0, t0, s0), (r1, k1, t1, s1) = res
     assert k0 != k1                      # own batch per rank (weak scaling)
-    assert t0 == t1 == [2.0, 10.0]       # max over ranks of each timing
+    assert t0 == t1 == [2.0, 10.0, 201.0]  # max over ranks of each timing; sum of the work
     assert not set(s0) & set(s1) and len(s0) + len(s1) == 64
 
 
