@@ -32,7 +32,7 @@ BYTES_PER_GPS_FWD = {"dr": 40, "cs": 96, "mcs": 96, "hv": 96}  # algorithmic byt
 # DRAM bytes (read + write) per grid-point-step of the batched kernels from one ncu capture of
 # the 512-instance, 20-step case (--count 512 --max-time-steps 20), scaled to a launch by the
 # grid-point-steps it processes: mode 0 = k_batch_forward, mode 1 = k_batch_fwdadj
-DRAM_BYTES_PER_GPS = {0: 303.0, 1: 1123.0}
+DRAM_BYTES_PER_GPS = {0: 303.0, 1: 1134.0}
 
 
 def parse():
