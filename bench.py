@@ -33,6 +33,11 @@ BYTES_PER_GPS_FWD = {"dr": 40, "cs": 96, "mcs": 96, "hv": 96}  # algorithmic byt
 # the 512-instance, 20-step case (--count 512 --max-time-steps 20), scaled to a launch by the
 # grid-point-steps it processes: mode 0 = k_batch_forward, mode 1 = k_batch_fwdadj
 DRAM_BYTES_PER_GPS = {0: 303.0, 1: 1134.0}
+# FP64 instructions (DFMA + DADD + DMUL, thread level) per grid-point-step from the same capture
+# (smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum), and the FP64 pipe's rate:
+# 1.196 TFLOP/s of DFMA measured on this GPU model = 5.98e11 FP64 instructions/s
+FP64_INSTR_PER_GPS = {0: 34.7, 1: 184.4}
+FP64_INSTR_PEAK = 5.98e11
 
 
 def parse():
@@ -359,6 +364,10 @@ def main():
                                        "grid-point-step, times this launch's grid-point-steps", "peak_source": peak_kind,
                      "algorithmic_bytes_per_grid_point_step": bpg,
                      "note": "FP64 pipe (1.196 TFLOP/s measured) binds before HBM on GB300"},
+        "fp64_pipe": {"instructions_per_grid_point_step": FP64_INSTR_PER_GPS[mode],
+                      "achieved": gps * FP64_INSTR_PER_GPS[mode] / (ms * 1e-3), "peak": FP64_INSTR_PEAK,
+                      "unit": "FP64 instructions/s", "frac": gps * FP64_INSTR_PER_GPS[mode] / (ms * 1e-3) / FP64_INSTR_PEAK,
+                      "note": "the binding resource of this path; instruction counts from ncu, peak from a DFMA probe"},
         "e2e": {"value": gps_all / e2e_s, "unit": "grid-point-steps/s", "h2d_bytes_per_step": int(total_n * 8),
                 "d2h_bytes_per_step": int(len(problems) * 8 * (6 if mode == 1 else 1)), "matches_device_values": e2e_ok},
         "gpu_launches": launches,
