@@ -1572,7 +1572,12 @@ template <typename T> int batch_typed<T>::autotune(int mode, int *chosen, cudaSt
         for (int c : cand) {
             bs_mode[m] = c;
             if (mode == 1) {
+                // a size whose workspace (one slice per resident CTA) does not fit is skipped
                 int rc = ensure_ws(c);
+                if (rc == LSS_ADI_ENOMEM) {
+                    clear_error();
+                    continue;
+                }
                 if (rc) {
                     cudaEventDestroy(e0);
                     cudaEventDestroy(e1);
