@@ -54,7 +54,7 @@ def parse():
     ap.add_argument("--max-time-steps", type=int, default=0,
                     help="cap every instance's time loop (a smaller workload for profiler captures; 0 = no cap)")
     ap.add_argument("--configs", default="", help="comma list of configurations to measure instead of the batched "
-                    "headline: c1, c2, c4, c5, c5sabr, mcsz, euler (one JSON line each)")
+                    "headline: c1, c2, c4, c5, c5sabr, mcsz, euler, batch32 (one JSON line each)")
     return ap.parse_args()
 
 
@@ -508,6 +508,28 @@ def run_configs(args):
             _, ref_s = O.run_reference(ref_p, "f64")
             print(json.dumps({"config": "explicit Euler 200x100x8000", "path": "reference host Euler (compiled), "
                               "first 200 steps", "cpu_reference_gps_1core": p.nx * p.ny * 200 / ref_s}), flush=True)
+    if "batch32" in wanted:
+        # the headline batch in FP32, forward (the adjoint is FP64 only)
+        from linear_system_solvers_gb300.batch import draw_batch, grid_point_steps
+
+        probs = draw_batch(4096, seed=SEED)
+        b = lss.BatchSolver(probs, precision="f32")
+        threads = b.autotune(mode=0)
+        b.run(0, graph=True)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(3):
+            b.run(0, graph=True)
+        e1.record()
+        torch.cuda.synchronize()
+        secs = e0.elapsed_time(e1) / 3e3
+        gps = grid_point_steps(probs)
+        print(json.dumps({"config": "batched MCS FP32 forward, 4096 uneven instances (seed 20261203)",
+                          "device_gps": gps / secs, "device_seconds": secs, "threads_per_instance": threads,
+                          "hbm_gbs_at_48_B": gps * 48 / secs / 1e9,
+                          "nonfinite_instances": int(np.count_nonzero(b.results()[2]))}), flush=True)
     if "mcsz" in wanted:
         # the batch of the headline with a genuine modified Craig-Sneyd weight (zeta = 1/3 != theta):
         # the full MCS stencil, forward and forward + adjoint
