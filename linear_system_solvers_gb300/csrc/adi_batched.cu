@@ -652,7 +652,7 @@ template <typename T> __global__ void k_wide_b2(const __grid_constant__ bparams<
 }
 // Partitioned line solves of the wide path.  A large single instance has only Nx or Ny
 // lines per sweep -- a few warps per SM, far below what the FP64 pipe needs -- so each line
-// is cut into P chunks solved concurrently (block: 32 lines x P chunks).  Both recurrences
+// is cut into P chunks solved concurrently (CTA: L = 8, 16 or 32 lines x P chunks).  Both recurrences
 // of the factorised solve are first order and linear:
 //   y_t = f_t - la_t y_{t-1}:  y_t = yhat_t + hf_t y_in,  hf_t = prod_{s=t0..t} (-la_s)
 //   x_t = y_t - g_t x_{t+1}:   x_t = xhat_t + hb_t x_in,  hb_t = prod_{s=t..t1} (-g_s)
@@ -699,7 +699,7 @@ __global__ void __launch_bounds__(1024) k_wide_s_chunk(const __grid_constant__ b
     const bdesc d = p.desc[0];
     const inst_view<T> v = make_view(p, d);
     const int nx = d.nx, ny = d.ny, e = nx - 2, P = blockDim.y, c = threadIdx.y, lane = threadIdx.x;
-    const int j = 1 + blockIdx.x * 32 + lane;
+    const int j = 1 + blockIdx.x * blockDim.x + lane;
     const bool act = j <= ny - 2;
     int t0, t1;
     chunk_range(e, P, c, t0, t1);
@@ -755,7 +755,7 @@ __global__ void __launch_bounds__(1024) k_wide_v_chunk(const __grid_constant__ b
     const bdesc d = p.desc[0];
     const inst_view<T> v = make_view(p, d);
     const int nx = d.nx, ny = d.ny, e = ny - 2, P = blockDim.y, c = threadIdx.y, lane = threadIdx.x;
-    const int i = 1 + blockIdx.x * 32 + lane;
+    const int i = 1 + blockIdx.x * blockDim.x + lane;
     const bool act = i <= nx - 2;
     const long long row = (long long)i * ny;
     int t0, t1;
@@ -945,9 +945,9 @@ __global__ void __launch_bounds__(1024) k_wadj_v_chunk(const __grid_constant__ b
     const bdesc d = p.desc[0];
     const inst_view<double> v = make_view(p, d);
     const int nx = d.nx, ny = d.ny, e = ny - 2, P = blockDim.y, c = threadIdx.y, lane = threadIdx.x;
-    const int i = 1 + blockIdx.x * 32 + lane;
+    const int i = 1 + blockIdx.x * blockDim.x + lane;
     const bool act = i <= nx - 2;
-    const long long row = (long long)i * ny, tid = ((long long)blockIdx.x * P + c) * 32 + lane;
+    const long long row = (long long)i * ny, tid = ((long long)blockIdx.x * P + c) * blockDim.x + lane;
     int t0, t1;
     chunk_range(e, P, c, t0, t1);
     adj_chunk_solve(TMP, row, 1, XB, v.Vt(VL_G), v.Vt(VL_LA), hz, hw, i, nx, e, t0, t1, c, P, lane, act, sa, sb);
@@ -990,9 +990,9 @@ __global__ void __launch_bounds__(1024) k_wadj_s_chunk(const __grid_constant__ b
     const bdesc d = p.desc[0];
     const inst_view<double> v = make_view(p, d);
     const int nx = d.nx, ny = d.ny, e = nx - 2, P = blockDim.y, c = threadIdx.y, lane = threadIdx.x;
-    const int j = 1 + blockIdx.x * 32 + lane;
+    const int j = 1 + blockIdx.x * blockDim.x + lane;
     const bool act = j <= ny - 2;
-    const long long tid = ((long long)blockIdx.x * P + c) * 32 + lane;
+    const long long tid = ((long long)blockIdx.x * P + c) * blockDim.x + lane;
     int t0, t1;
     chunk_range(e, P, c, t0, t1);
     adj_chunk_solve(TMP, j, ny, XB, v.S(SL_G), v.S(SL_LA), hz, hw, j, ny, e, t0, t1, c, P, lane, act, sa, sb);
@@ -1221,6 +1221,7 @@ template <typename T> struct batch_typed {
     dbuf<T> d_b0;
     cudaGraphExec_t wide_graph = nullptr;
     int wide_ps = 1, wide_pv = 1;   // chunks per S line / per v line (1: thread per line)
+    int wide_ls = 32, wide_lv = 32; // lines per CTA of the partitioned kernels (CTA: lines x chunks)
     dbuf<T> d_spk;                  // chunk products: S hf, S hb, v hf, v hb (n each)
     int set_wide_chunks(int ps, int pv, cudaStream_t s);
     int autotune_wide(cudaStream_t s);
@@ -1628,7 +1629,8 @@ void batch_typed<T>::launch_wide_s(cudaStream_t s, const bparams<T> &p, const T 
         k_wide_s<T, KIND><<<grid_for(d.ny - 2, 32), 32, 0, s>>>(p, U, Y1, Y2, Y);
     } else {
         const long long n = total_n;
-        k_wide_s_chunk<T, KIND><<<grid_for(d.ny - 2, 32), dim3(32, wide_ps), 0, s>>>(p, U, Y1, Y2, Y, d_spk.p, d_spk.p + n);
+        k_wide_s_chunk<T, KIND><<<grid_for(d.ny - 2, wide_ls), dim3(wide_ls, wide_ps), 0, s>>>(p, U, Y1, Y2, Y, d_spk.p,
+                                                                                              d_spk.p + n);
     }
 }
 
@@ -1640,7 +1642,7 @@ void batch_typed<T>::launch_wide_v(cudaStream_t s, const bparams<T> &p, const T 
         k_wide_v<T><<<grid_for(d.nx - 2, 32), 32, 0, s>>>(p, in, inh, b0, out);
     } else {
         const long long n = total_n;
-        k_wide_v_chunk<T><<<grid_for(d.nx - 2, 32), dim3(32, wide_pv), 0, s>>>(p, in, inh, b0, out, d_spk.p + 2 * n,
+        k_wide_v_chunk<T><<<grid_for(d.nx - 2, wide_lv), dim3(wide_lv, wide_pv), 0, s>>>(p, in, inh, b0, out, d_spk.p + 2 * n,
                                                                                d_spk.p + 3 * n);
     }
 }
@@ -1662,6 +1664,15 @@ template <typename T> int batch_typed<T>::set_wide_chunks(int ps, int pv, cudaSt
     LSS_CUDA_TRY(cudaGetLastError(), "wide: chunk products");
     wide_ps = ps;
     wide_pv = pv;
+    // the fewest lines per CTA (32, 16 or 8: a warp still reads whole 64-256 B row segments) that
+    // give every SM a CTA: with 1-2 k lines, 32 lines per CTA would leave most SMs idle
+    auto lines_per_cta = [&](int lines) {
+        for (int l : {32, 16})
+            if (grid_for(lines, l) >= sms) return l;
+        return 8;
+    };
+    wide_ls = lines_per_cta(d.ny - 2);
+    wide_lv = lines_per_cta(d.nx - 2);
     if (wide_graph) cudaGraphExecDestroy(wide_graph);
     wide_graph = nullptr;
     return LSS_ADI_OK;
@@ -1776,8 +1787,9 @@ template <typename T> int batch_typed<T>::enqueue_wide_adjoint(cudaStream_t s)
         const int threads = 128, grid = grid_for(std::max(nx, ny), threads);
         const long long nthr = static_cast<long long>(grid) * threads;
         // partitioned adjoint solves with the forward's chunk counts
-        const int ps = wide_ps, pv = wide_pv, gS = grid_for(ny - 2, 32), gV = grid_for(nx - 2, 32);
-        const long long nacc = std::max({nthr, 32LL * gS * ps, 32LL * gV * pv, static_cast<long long>(nx)});
+        const int ps = wide_ps, pv = wide_pv, ls = wide_ls, lv = wide_lv;
+        const int gS = grid_for(ny - 2, ls), gV = grid_for(nx - 2, lv);
+        const long long nacc = std::max({nthr, 1LL * ls * gS * ps, 1LL * lv * gV * pv, static_cast<long long>(nx)});
         if ((ps > 1 || pv > 1) && (aspk_ps != ps || aspk_pv != pv)) {
             if (!d_aspk.p) LSS_CUDA_TRY(d_aspk.alloc(4 * n), "wide adjoint: allocating chunk products");
             const bparams<double> q = params();
@@ -1841,9 +1853,9 @@ template <typename T> int batch_typed<T>::enqueue_wide_adjoint(cudaStream_t s)
                                        double *INHB) {
                     if (pv > 1) {
                         if (first)
-                            k_wadj_v_chunk<true><<<gV, dim3(32, pv), 0, s>>>(p, in, out, XB, INB, INHB, TMP, LV, ACC, nacc, hzV, hwV);
+                            k_wadj_v_chunk<true><<<gV, dim3(lv, pv), 0, s>>>(p, in, out, XB, INB, INHB, TMP, LV, ACC, nacc, hzV, hwV);
                         else
-                            k_wadj_v_chunk<false><<<gV, dim3(32, pv), 0, s>>>(p, in, out, XB, INB, INHB, TMP, LV, ACC, nacc, hzV, hwV);
+                            k_wadj_v_chunk<false><<<gV, dim3(lv, pv), 0, s>>>(p, in, out, XB, INB, INHB, TMP, LV, ACC, nacc, hzV, hwV);
                     } else {
                         if (first)
                             k_wadj_v<true><<<grid, threads, 0, s>>>(p, in, out, XB, INB, INHB, TMP, LV, ACC, nacc);
@@ -1854,10 +1866,10 @@ template <typename T> int batch_typed<T>::enqueue_wide_adjoint(cudaStream_t s)
                 auto adj_s_stage = [&](int kind, const double *Yo, const double *XB) {
                     if (ps > 1) {
                         if (kind == 2)
-                            k_wadj_s_chunk<2><<<gS, dim3(32, ps), 0, s>>>(p, um, Y1, Y2, Yo, XB, FB, TMP, LS, HS, ub, Y1B, ACC,
+                            k_wadj_s_chunk<2><<<gS, dim3(ls, ps), 0, s>>>(p, um, Y1, Y2, Yo, XB, FB, TMP, LS, HS, ub, Y1B, ACC,
                                                                           nacc, tau, hzS, hwS);
                         else
-                            k_wadj_s_chunk<1><<<gS, dim3(32, ps), 0, s>>>(p, um, Y1, Y2, Yo, XB, FB, TMP, LS, HS, ub, Y1B, ACC,
+                            k_wadj_s_chunk<1><<<gS, dim3(ls, ps), 0, s>>>(p, um, Y1, Y2, Yo, XB, FB, TMP, LS, HS, ub, Y1B, ACC,
                                                                           nacc, tau, hzS, hwS);
                     } else {
                         if (kind == 2)
