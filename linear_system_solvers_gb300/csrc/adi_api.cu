@@ -181,9 +181,9 @@ int lss_adi_adjoint(lss_adi_handle *h, const void *payoff, double *out_value, do
         int rc = a->init(h->prob);
         if (rc) return rc;
         if (h->wide) { // the forward's chunk counts, so both passes solve alike
-            int ps = 1, pv = 1;
-            h->wide->current_chunks(ps, pv);
-            rc = a->set_chunks(ps, pv, stream);
+            int ps = 1, pv = 1, ls = 0, lv = 0;
+            h->wide->current_chunks(ps, pv, ls, lv);
+            rc = a->set_chunks(ps, pv, ls, lv, stream);
             if (rc) return rc;
         }
         h->adj = std::move(a);
@@ -211,11 +211,12 @@ int lss_adi_line_chunks(lss_adi_handle *h, int s_chunks, int v_chunks, int *out_
     clear_error();
     if (!h) return set_error(LSS_ADI_EINVAL, "lss_adi_line_chunks: null handle");
     if (!h->wide) return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_line_chunks: not a partitioned (fast single-instance) handle");
-    int ps = 1, pv = 1;
+    int ps = 1, pv = 1, ls = 0, lv = 0;
     int rc = h->wide->chunks(s_chunks, v_chunks, &ps, &pv, stream);
     if (rc) return rc;
     if (h->adj) {
-        rc = h->adj->set_chunks(ps, pv, stream);
+        h->wide->current_chunks(ps, pv, ls, lv);
+        rc = h->adj->set_chunks(ps, pv, ls, lv, stream);
         if (rc) return rc;
     }
     if (out_s) *out_s = ps;

@@ -1223,7 +1223,7 @@ template <typename T> struct batch_typed {
     int wide_ps = 1, wide_pv = 1;   // chunks per S line / per v line (1: thread per line)
     int wide_ls = 32, wide_lv = 32; // lines per CTA of the partitioned kernels (CTA: lines x chunks)
     dbuf<T> d_spk;                  // chunk products: S hf, S hb, v hf, v hb (n each)
-    int set_wide_chunks(int ps, int pv, cudaStream_t s);
+    int set_wide_chunks(int ps, int pv, cudaStream_t s, int ls = 0, int lv = 0); // ls, lv 0: by SM count
     int autotune_wide(cudaStream_t s);
     template <int KIND> void launch_wide_s(cudaStream_t s, const bparams<T> &p, const T *U, const T *Y1, const T *Y2, T *Y);
     void launch_wide_v(cudaStream_t s, const bparams<T> &p, const T *in, const T *inh, const T *b0, T *out);
@@ -1647,7 +1647,7 @@ void batch_typed<T>::launch_wide_v(cudaStream_t s, const bparams<T> &p, const T 
     }
 }
 
-template <typename T> int batch_typed<T>::set_wide_chunks(int ps, int pv, cudaStream_t s)
+template <typename T> int batch_typed<T>::set_wide_chunks(int ps, int pv, cudaStream_t s, int ls, int lv)
 {
     const bdesc &d = desc[0];
     const long long n = total_n;
@@ -1671,15 +1671,15 @@ template <typename T> int batch_typed<T>::set_wide_chunks(int ps, int pv, cudaSt
             if (grid_for(lines, l) >= sms) return l;
         return 8;
     };
-    wide_ls = lines_per_cta(d.ny - 2);
-    wide_lv = lines_per_cta(d.nx - 2);
+    wide_ls = (ls == 8 || ls == 16 || ls == 32) ? ls : lines_per_cta(d.ny - 2);
+    wide_lv = (lv == 8 || lv == 16 || lv == 32) ? lv : lines_per_cta(d.nx - 2);
     if (wide_graph) cudaGraphExecDestroy(wide_graph);
     wide_graph = nullptr;
     return LSS_ADI_OK;
 }
 
-// Chunk counts of the two sweeps, each timed on its own (first S stage, first v stage) over
-// P = 1, 2, 4, ..., 32 with at least 4 rows per chunk.
+// Chunk counts and lines per CTA of the two sweeps, each timed on its own (first S stage,
+// first v stage) over P = 1, 2, 4, ..., 32 (at least 4 rows per chunk) and L = 8, 16, 32.
 template <typename T> int batch_typed<T>::autotune_wide(cudaStream_t s)
 {
     const bdesc &d = desc[0];
@@ -1689,40 +1689,45 @@ template <typename T> int batch_typed<T>::autotune_wide(cudaStream_t s)
     LSS_CUDA_TRY(cudaEventCreate(&e0), "wide: tuning events");
     LSS_CUDA_TRY(cudaEventCreate(&e1), "wide: tuning events");
     float best_s = 1e30f, best_v = 1e30f;
-    int ps = 1, pv = 1;
+    int ps = 1, pv = 1, ls = 32, lv = 32;
     int rc = LSS_ADI_OK;
+    auto timed = [&](auto &&launch) {
+        launch();
+        cudaEventRecord(e0, s);
+        for (int r = 0; r < 3; ++r) launch();
+        cudaEventRecord(e1, s);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        return ms;
+    };
     for (int P = 1; P <= 32 && rc == LSS_ADI_OK; P *= 2) {
         const bool okS = (P == 1 || d.nx - 2 >= 4 * P), okV = (P == 1 || d.ny - 2 >= 4 * P);
         if (!okS && !okV) break;
-        rc = set_wide_chunks(okS ? P : 1, okV ? P : 1, s);
-        if (rc) break;
-        float ms = 0.f;
-        if (okS) {
-            launch_wide_s<1>(s, p, p.U, nullptr, nullptr, p.Y1);
-            cudaEventRecord(e0, s);
-            for (int r = 0; r < 3; ++r) launch_wide_s<1>(s, p, p.U, nullptr, nullptr, p.Y1);
-            cudaEventRecord(e1, s);
-            cudaEventSynchronize(e1);
-            cudaEventElapsedTime(&ms, e0, e1);
-            if (ms < best_s) { best_s = ms; ps = P; }
+        for (int L : {8, 16, 32}) {
+            if (P == 1 && L != 32) continue; // thread per line: L unused
+            rc = set_wide_chunks(okS ? P : 1, okV ? P : 1, s, L, L);
+            if (rc) break;
+            if (okS) {
+                const float ms = timed([&] { launch_wide_s<1>(s, p, p.U, nullptr, nullptr, p.Y1); });
+                if (ms < best_s) { best_s = ms; ps = P; ls = L; }
+            }
+            if (okV) {
+                k_wide_b1<T><<<grid_for(d.nx, 128), 128, 0, s>>>(p, p.U, d_b0.p);
+                const float ms = timed([&] { launch_wide_v(s, p, p.U, p.Y1, d_b0.p, p.Y2); });
+                if (ms < best_v) { best_v = ms; pv = P; lv = L; }
+            }
+            const cudaError_t err = cudaGetLastError();
+            if (err != cudaSuccess) {
+                rc = set_error(LSS_ADI_ECUDA, std::string("wide: tuning: ") + cudaGetErrorString(err));
+                break;
+            }
         }
-        if (okV) {
-            k_wide_b1<T><<<grid_for(d.nx, 128), 128, 0, s>>>(p, p.U, d_b0.p);
-            launch_wide_v(s, p, p.U, p.Y1, d_b0.p, p.Y2);
-            cudaEventRecord(e0, s);
-            for (int r = 0; r < 3; ++r) launch_wide_v(s, p, p.U, p.Y1, d_b0.p, p.Y2);
-            cudaEventRecord(e1, s);
-            cudaEventSynchronize(e1);
-            cudaEventElapsedTime(&ms, e0, e1);
-            if (ms < best_v) { best_v = ms; pv = P; }
-        }
-        const cudaError_t err = cudaGetLastError();
-        if (err != cudaSuccess) rc = set_error(LSS_ADI_ECUDA, std::string("wide: tuning: ") + cudaGetErrorString(err));
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc) return rc;
-    return set_wide_chunks(ps, pv, s);
+    return set_wide_chunks(ps, pv, s, ls, lv);
 }
 
 // One time step U -> V of the wide path (stage outputs in Y1, Y2, Y3).
@@ -2016,17 +2021,22 @@ template <typename T> struct wide_solver : wide_solver_base {
             rc = b.autotune_wide(s);
             if (rc) return rc;
         }
-        rc = b.set_wide_chunks(s_chunks ? s_chunks : b.wide_ps, v_chunks ? v_chunks : b.wide_pv, s);
-        if (rc) return rc;
+        if (s_chunks || v_chunks) { // a direction left at 0 keeps its tuned chunks and lines per CTA
+            rc = b.set_wide_chunks(s_chunks ? s_chunks : b.wide_ps, v_chunks ? v_chunks : b.wide_pv, s,
+                                   s_chunks ? 0 : b.wide_ls, v_chunks ? 0 : b.wide_lv);
+            if (rc) return rc;
+        }
         LSS_CUDA_TRY(cudaStreamSynchronize(s), "lss_adi_line_chunks");
         if (out_s) *out_s = b.wide_ps;
         if (out_v) *out_v = b.wide_pv;
         return LSS_ADI_OK;
     }
-    void current_chunks(int &s_chunks, int &v_chunks) const override
+    void current_chunks(int &s_chunks, int &v_chunks, int &s_lines, int &v_lines) const override
     {
         s_chunks = b.wide_ps;
         v_chunks = b.wide_pv;
+        s_lines = b.wide_ls;
+        v_lines = b.wide_lv;
     }
 };
 
@@ -2081,10 +2091,10 @@ int adjoint_solver::init(const lss_adi_problem &p)
     return LSS_ADI_OK;
 }
 
-int adjoint_solver::set_chunks(int s_chunks, int v_chunks, void *stream)
+int adjoint_solver::set_chunks(int s_chunks, int v_chunks, int s_lines, int v_lines, void *stream)
 {
     if (!impl || !impl->wide) return LSS_ADI_OK;
-    return impl->b.set_wide_chunks(s_chunks, v_chunks, static_cast<cudaStream_t>(stream));
+    return impl->b.set_wide_chunks(s_chunks, v_chunks, static_cast<cudaStream_t>(stream), s_lines, v_lines);
 }
 
 int adjoint_solver::run(const void *payoff, double *out_value, double *dv_dparams, void *dv_dpayoff, int checkpoint_every,

@@ -21,8 +21,9 @@ struct adjoint_solver {
     int init(const lss_adi_problem &p);
     int run(const void *payoff, double *out_value, double *dv_dparams, void *dv_dpayoff, int checkpoint_every, int flags,
             void *stream);
-    // chunk counts of the partitioned solves of a large instance (no effect on one-CTA instances)
-    int set_chunks(int s_chunks, int v_chunks, void *stream);
+    // chunk counts and lines per CTA of the partitioned solves of a large instance (0 lines: by
+    // SM count; no effect on one-CTA instances)
+    int set_chunks(int s_chunks, int v_chunks, int s_lines, int v_lines, void *stream);
 };
 
 // Single instance on the factorised ("fast") arithmetic: one kernel per stage over the whole
@@ -33,7 +34,7 @@ struct wide_solver_base {
                         bool use_graph) = 0;
     virtual int grid(void *x, void *y) const = 0;
     virtual int chunks(int s_chunks, int v_chunks, int *out_s, int *out_v, void *stream) = 0;
-    virtual void current_chunks(int &s_chunks, int &v_chunks) const = 0;
+    virtual void current_chunks(int &s_chunks, int &v_chunks, int &s_lines, int &v_lines) const = 0;
 };
 int make_wide_solver(const lss_adi_problem &p, std::unique_ptr<wide_solver_base> &out);
 
