@@ -1127,22 +1127,20 @@ __global__ void __launch_bounds__(256) k_wadj_reduce(const __grid_constant__ bpa
 }
 
 // value, finiteness flag and final-array flag of the single instance
+// value at the evaluation point and finiteness of the final surface, grid-wide (the status word
+// is cleared before the time loop; any block that sees a non-finite point sets it)
 template <typename T> __global__ void k_wide_finish(const __grid_constant__ bparams<T> p, const T *U)
 {
-    __shared__ int bad;
     const bdesc d = p.desc[0];
-    if (threadIdx.x == 0) bad = 0;
-    __syncthreads();
     const long long n = (long long)d.nx * d.ny;
     int b = 0;
-    for (long long q = threadIdx.x; q < n; q += blockDim.x) b |= !isfinite(static_cast<double>(U[q]));
-    if (b) atomicOr(&bad, 1);
-    __syncthreads();
-    if (threadIdx.x == 0) {
+    for (long long q = gtid(); q < n; q += gstride()) b |= !isfinite(static_cast<double>(U[q]));
+    b = __syncthreads_or(b);
+    if (b && threadIdx.x == 0) atomicOr(p.status, 1);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
         const long long o = (long long)d.i0 * d.ny + d.j0;
         p.values[0] = d.w00 * static_cast<double>(U[o]) + d.w10 * static_cast<double>(U[o + d.ny]) +
                       d.w01 * static_cast<double>(U[o + 1]) + d.w11 * static_cast<double>(U[o + d.ny + 1]);
-        p.status[0] = bad;
         p.final_in_v[0] = d.steps & 1;
     }
 }
@@ -1757,13 +1755,14 @@ template <typename T> int batch_typed<T>::enqueue_wide(cudaStream_t s)
     bparams<T> p = params();
     T *U = p.U, *V = p.V, *Y1 = p.Y1, *Y2 = p.Y2, *Y3 = p.Y3;
     LSS_CUDA_TRY(cudaMemcpyAsync(U, d_payoff.p, total_n * sizeof(T), cudaMemcpyDeviceToDevice, s), "wide: initial state");
+    LSS_CUDA_TRY(cudaMemsetAsync(d_status.p, 0, sizeof(int), s), "wide: clearing the status");
     long long nl = 0;
     for (int step = 0; step < d.steps; ++step) {
         enqueue_wide_step(s, p, U, Y1, Y2, Y3, V);
         nl += d.scheme == LSS_ADI_DOUGLAS_RACHFORD ? 4 : 6;
         std::swap(U, V);
     }
-    k_wide_finish<T><<<1, 256, 0, s>>>(p, U);
+    k_wide_finish<T><<<grid_for(total_n, 256), 256, 0, s>>>(p, U);
     LSS_CUDA_TRY(cudaGetLastError(), "wide: launching the time loop");
     launches = nl + 1;
     return LSS_ADI_OK;
