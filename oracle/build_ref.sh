@@ -1,21 +1,22 @@
 #!/usr/bin/env bash
-# build_ref.sh -- compile the reference's own host ADI path into oracle/_ref/ref_driver.
+# build_ref.sh -- compile the reference's own host ADI path into oracle/_ref/ref_driver and its
+# 1-D implicit heat path into oracle/_ref/ref_driver_1d.
 #
 # TEST INFRASTRUCTURE ONLY.  Reads the reference sources where they lie (default
 # /root/reference, override with LSS_REFERENCE_DIR), copies the headers it needs into
 # oracle/_ref/src (git-ignored, never committed), applies four mechanical portability
 # patches (MSVC-only std::exception(const char*) ctor; two shadowed template-template
-# parameter names; one decltype on a non-class), and compiles oracle/ref_driver.cu
-# against them.  Host code only runs; nvcc is used because the reference headers pull in
+# parameter names; one decltype on a non-class), and compiles oracle/ref_driver.cu and
+# oracle/ref_driver_1d.cu against them.  Host code only runs; nvcc is used because the reference headers pull in
 # thrust device headers.  -ffp-contract=off keeps the reference's two-rounding a*b+c.
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 REF="${LSS_REFERENCE_DIR:-/root/reference}"
 OUT="$HERE/_ref"
 mkdir -p "$OUT"
-if [ -x "$OUT/ref_driver" ] && "$OUT/ref_driver" >/dev/null 2>&1; [ $? -eq 2 ] && \
-   [ "$OUT/ref_driver" -nt "$HERE/ref_driver.cu" ] && [ "$OUT/ref_driver" -nt "$0" ]; then
-    echo "build_ref.sh: $OUT/ref_driver is up to date"
+fresh() { [ -x "$OUT/$1" ] && [ "$OUT/$1" -nt "$HERE/$1.cu" ] && [ "$OUT/$1" -nt "$0" ]; }
+if fresh ref_driver && fresh ref_driver_1d; then
+    echo "build_ref.sh: $OUT/ref_driver and $OUT/ref_driver_1d are up to date"
     exit 0
 fi
 if [ -d "$REF/pde_solvers" ]; then
@@ -44,7 +45,14 @@ touch .patched
 fi
 CUS=$(find . -name '*.cu' ! -name main.cu | sort)
 ARCH="${LSS_REF_ARCH:-sm_100}"
-nvcc -std=c++17 -O2 -arch="$ARCH" -Xcompiler -ffp-contract=off \
-    -include cmath -include stdexcept -I"$OUT/src" \
-    "$HERE/ref_driver.cu" $CUS -o "$OUT/ref_driver" -lcusolver -lcusparse -lcublas
-echo "build_ref.sh: built $OUT/ref_driver"
+for d in ref_driver ref_driver_1d; do
+    fresh "$d" && continue
+    nvcc -std=c++17 -O2 -arch="$ARCH" -Xcompiler -ffp-contract=off \
+        -include cmath -include stdexcept -I"$OUT/src" \
+        "$HERE/$d.cu" $CUS -o "$OUT/$d" -lcusolver -lcusparse -lcublas &
+done
+wait
+for d in ref_driver ref_driver_1d; do
+    [ -x "$OUT/$d" ] || { echo "build_ref.sh: building $d failed" >&2; exit 1; }
+done
+echo "build_ref.sh: built $OUT/ref_driver and $OUT/ref_driver_1d"

@@ -19,6 +19,7 @@
 #define SINH sinh
 #define COSH cosh
 #include "lss_oracle_impl.h"
+#include "lss_oracle_1d_impl.h"
 #undef REAL
 #undef SFX
 #undef ASINH
@@ -31,6 +32,7 @@
 #define SINH sinhf
 #define COSH coshf
 #include "lss_oracle_impl.h"
+#include "lss_oracle_1d_impl.h"
 #undef REAL
 #undef SFX
 #undef ASINH

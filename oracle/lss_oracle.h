@@ -76,6 +76,52 @@ int lsso_index_maps_f32(const lsso_problem *p, int *imap, int *jmap);
  * order M, P, Z, Mt, Pt, W, C, D, E, F  -> out has 10*Nx*Ny entries. */
 int lsso_coefficients_f64(const lsso_problem *p, double t, double *out);
 
+/* ---- 1-D implicit heat equation u_t = a u_xx + b u_x + c u + F (lss_oracle_1d_impl.h) ----
+ * The reference's implicit_solvers::general_heat_equation
+ * (pde_solvers/one_dimensional/heat_type/lss_1d_general_heat_equation.hpp:140-250) with its
+ * host Thomas-LU / double-sweep policies; theta = 1 (Euler) or 0.5 (Crank-Nicolson), the two
+ * schemes its implicit kernel accepts (lss_1d_general_heat_equation_implicit_kernel.hpp:930-945). */
+enum { LSSO_H1_BLACK_SCHOLES = 0, LSSO_H1_CONSTANT = 1 };
+enum { LSSO_BC_DIRICHLET = 0, LSSO_BC_NEUMANN = 1, LSSO_BC_ROBIN = 2 };
+
+typedef struct lsso_heat1d_problem {
+    int model;                  /* LSSO_H1_BLACK_SCHOLES | LSSO_H1_CONSTANT */
+    /* Black-Scholes (unit_tests/pde_solvers/one_dimensional/lss_black_scholes_equation_t.hpp:854-880):
+     * a = 0.5 sigma^2 x^2, b = rate x, c = -rate; terminal max(0, x - K) (put: max(0, K - x));
+     * Dirichlet data call V(x_lo) = 0, V(x_hi) = x_hi - K e^{-rate (t_hi - t)}
+     * (put: V(x_lo) = K e^{-rate (t_hi - t)}, V(x_hi) = 0). */
+    double sigma, rate, strike;
+    int put;
+    /* constant coefficients (pure heat / advection tests): a = diff, b = conv, c = react;
+     * initial condition init0 + init1 x; boundary kinds LSSO_BC_* with constant data
+     * (Robin: linear_value * u + value); heat source F = src0 + src1 x when has_source. */
+    double diff, conv, react;
+    double init0, init1;
+    int lo_kind, hi_kind;
+    double lo_value, lo_linear, hi_value, hi_linear;
+    int has_source;
+    double src0, src1;
+    double x_lo, x_hi, t_lo, t_hi;
+    int n, nt;                  /* space points >= 4, time points >= 2 */
+    int theta_scheme;           /* LSSO_EULER | LSSO_CN */
+    int nonuniform;             /* grid_config_hints_1d: Nonuniform */
+    double acc_point, alpha_scale;
+    int solver;                 /* LSSO_THOMAS_LU | LSSO_DOUBLE_SWEEP */
+    int forward;                /* 1 = forward from t_lo (host_fwd_* configs), 0 = backward from t_hi */
+} lsso_heat1d_problem;
+
+/* Solve; out = final n values; all (may be NULL) = nt rows of n by time index (the
+ * reference's solve(container_2d&) with run_with_stepping). */
+int lsso_heat1d_solve_f64(const lsso_heat1d_problem *p, double *out, double *all);
+int lsso_heat1d_solve_f32(const lsso_heat1d_problem *p, float *out, float *all);
+int lsso_heat1d_grid_f64(const lsso_heat1d_problem *p, double *x);
+int lsso_heat1d_grid_f32(const lsso_heat1d_problem *p, float *x);
+/* coef[3n] = A_, B_, D_; init[n]; bnd[4*(nt-1)] = per step lo value, lo linear, hi value,
+ * hi linear (transformed, at the step's time); src[nt*n] or NULL (row s: F at step s's time;
+ * row nt-1: F at the last step's next time). */
+int lsso_heat1d_tables_f64(const lsso_heat1d_problem *p, double *coef, double *init, double *bnd, double *src);
+int lsso_heat1d_tables_f32(const lsso_heat1d_problem *p, float *coef, float *init, float *bnd, float *src);
+
 #ifdef __cplusplus
 }
 #endif
