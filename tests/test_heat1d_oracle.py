@@ -69,7 +69,8 @@ def test_heat1d_oracle_tables_are_the_solver_inputs(oracle):
     np.testing.assert_array_equal(t["init"], np.maximum(0.0, x - p.strike))
     assert np.all(A + D >= 0.0) and np.all((A + D)[1:] > 0.0)
     # backward stepping: boundary data at t_hi - k, t_hi - 2k, ...: the discounted upper value
-    # V(x_hi) = x_hi - K e^{-r (T - t)} decreases towards t = 0
+    # V(x_hi) = x_hi - K e^{-r (T - t)} grows towards t = 0
     hi = t["bnd"][:, 2]
-    assert np.all(np.diff(hi) < 0)
+    assert np.all(np.diff(hi) > 0)
+    assert hi[0] == np.float64(p.x_hi - p.strike * np.exp(-p.rate * (p.t_hi - (p.t_hi - (p.t_hi - p.t_lo) / (p.nt - 1)))))
     assert np.all(t["bnd"][:, 0] == 0.0)
