@@ -1,4 +1,4 @@
-"""ctypes binding of the C-ABI in include/lss_adi.h (liblss_adi.so).
+"""ctypes binding of the C-ABI in include/lss_adi.h and include/lss_heat1d.h (liblss_adi.so).
 
 The library is the only compute path: if it cannot be loaded the import fails loudly;
 there is no CPU fallback.
@@ -54,7 +54,30 @@ class LssAdiTables(ctypes.Structure):
     ]
 
 
-# name -> (restype, argtypes); every symbol declared in include/lss_adi.h
+class LssHeat1DTables(ctypes.Structure):
+    """Mirror of ``lss_heat1d_tables``."""
+
+    _fields_ = [
+        ("n", c_int), ("nt", c_int), ("t_lo", c_double), ("t_hi", c_double), ("theta_scheme", c_int),
+        ("forward", c_int), ("lo_kind", c_int), ("hi_kind", c_int),
+        ("coef", c_void_p), ("initial", c_void_p), ("boundary", c_void_p), ("source", c_void_p),
+    ]
+
+
+class LssHeat1DBs(ctypes.Structure):
+    """Mirror of ``lss_heat1d_bs``."""
+
+    _fields_ = [
+        ("sigma", c_double), ("rate", c_double), ("strike", c_double), ("maturity", c_double), ("put", c_int),
+        ("s_lo", c_double), ("s_hi", c_double), ("n", c_int), ("nt", c_int), ("theta_scheme", c_int),
+        ("nonuniform", c_int), ("acc_point", c_double), ("alpha_scale", c_double), ("eval_s", c_double),
+    ]
+
+
+HEAT1D_DIRICHLET, HEAT1D_NEUMANN, HEAT1D_ROBIN = 0, 1, 2
+HEAT1D_OPT_ALL_STEPS, HEAT1D_OPT_DOUBLE_SWEEP = 1, 2
+
+# name -> (restype, argtypes); every symbol declared in include/lss_adi.h and include/lss_heat1d.h
 SIGNATURES = {
     "lss_adi_abi_version": (c_int, []),
     "lss_adi_last_error": (ctypes.c_char_p, []),
@@ -80,6 +103,16 @@ SIGNATURES = {
                                       c_void_p, c_void_p, c_void_p]),
     "lss_tridiag_thomas_lu_noalloc": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
                                               c_void_p, c_void_p, c_void_p, c_void_p]),
+    "lss_heat1d_batch_create": (c_int, [P(LssHeat1DTables), c_int, c_int, c_int, c_int, P(c_void_p)]),
+    "lss_heat1d_batch_create_bs": (c_int, [P(LssHeat1DBs), c_int, c_int, c_int, c_int, P(c_void_p)]),
+    "lss_heat1d_batch_run": (c_int, [c_void_p, c_void_p]),
+    "lss_heat1d_batch_run_host": (c_int, [c_void_p, c_void_p, P(c_double), P(c_int), c_void_p]),
+    "lss_heat1d_batch_results": (c_int, [c_void_p, P(c_double), P(c_int)]),
+    "lss_heat1d_batch_solution": (c_int, [c_void_p, c_int, c_void_p]),
+    "lss_heat1d_batch_grid": (c_int, [c_void_p, c_int, c_void_p]),
+    "lss_heat1d_batch_launch_count": (c_int, [c_void_p]),
+    "lss_heat1d_batch_point_steps": (c_double, [c_void_p]),
+    "lss_heat1d_batch_destroy": (None, [c_void_p]),
 }
 
 _lib = None

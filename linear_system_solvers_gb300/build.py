@@ -36,6 +36,7 @@ def sources() -> list[str]:
 def _deps() -> list[str]:
     files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
     files.append(os.path.join(INCLUDE, "lss_adi.h"))
+    files.append(os.path.join(INCLUDE, "lss_heat1d.h"))
     files.append(os.path.abspath(__file__))
     return files
 
