@@ -54,7 +54,7 @@ def parse():
     ap.add_argument("--max-time-steps", type=int, default=0,
                     help="cap every instance's time loop (a smaller workload for profiler captures; 0 = no cap)")
     ap.add_argument("--configs", default="", help="comma list of configurations to measure instead of the batched "
-                    "headline: c1, c2, c4, c5, c5sabr, mcsz, euler, batch32 (one JSON line each)")
+                    "headline: c1, c2, c4, c5, c5sabr, mcsz, euler, batch32, heat1d (one JSON line each)")
     return ap.parse_args()
 
 
@@ -555,6 +555,8 @@ def run_configs(args):
                               "mode": ["forward", "forward + adjoint"][mode], "device_gps": grid_point_steps(probs) / secs,
                               "device_seconds": secs, "threads_per_instance": threads,
                               "nonfinite_instances": int(np.count_nonzero(status))}), flush=True)
+    if "heat1d" in wanted:
+        run_heat1d()
     if "c5sabr" in wanted:
         p = lss.HestonProblem(model="sabr", sigma=0.4, rho=-0.3, sabr_beta=0.5, rate=0.0, strike=0.05, maturity=2.0,
                               s_lo=0.0, s_hi=0.2, v_lo=0.0, v_hi=1.0, nx=2048, ny=1024, nt=801, scheme="dr",
@@ -609,6 +611,100 @@ def _oracle_value(args):
     wy = min(1.0, max(0.0, (v0 - y[j]) / (y[j + 1] - y[j])))
     return float((1 - wx) * (1 - wy) * surf[i, j] + wx * (1 - wy) * surf[i + 1, j] + (1 - wx) * wy * surf[i, j + 1]
                  + wx * wy * surf[i + 1, j + 1])
+
+
+# 1-D implicit heat / Black-Scholes batch (lss_heat1d.h): bytes and FP64 operations per
+# point-step of the factorised kernel k_h1_fast (forward: WB, WD, M, U[t+1] loads, Y store;
+# backward: Y, G loads, U store; 4 + 1 FP64 operations)
+HEAT1D_BYTES_PER_PS = {"f64": 64.0, "f32": 32.0}
+HEAT1D_SEED = 20261205
+
+
+def run_heat1d(count=65536, sample=48):
+    """Batched 1-D Black-Scholes (draw_black_scholes: n 128-512, 99-999 steps, CN, sinh grid at K):
+    device throughput of both arithmetics and precisions, end to end through run_host, parity on
+    a sample against the oracle, CPU baselines (oracle and the compiled reference) on a sample."""
+    import numpy as np
+    import torch
+
+    import linear_system_solvers_gb300 as lss
+    from oracle import oracle as O
+
+    torch.cuda.set_device(0)
+    qs = lss.draw_black_scholes(count, seed=HEAT1D_SEED)
+    ps = float(sum(q.n * (q.nt - 1) for q in qs))
+    peak, peak_kind = measured_peaks()
+    rng = np.random.default_rng(1)
+    idx = sorted(rng.choice(count, size=sample, replace=False).tolist())
+
+    def oproblem(q):
+        return O.Heat1DProblem(model="bs", sigma=q.sigma, rate=q.rate, strike=q.strike, put=q.put, x_lo=q.s_lo,
+                               x_hi=q.s_hi, t_lo=0.0, t_hi=q.maturity, n=q.n, nt=q.nt, theta_scheme=q.theta_scheme,
+                               nonuniform=q.nonuniform, acc_point=q.acc_point, alpha_scale=q.alpha_scale,
+                               forward=False)
+
+    t0 = time.perf_counter()
+    wants = {i: O.solve_1d(oproblem(qs[i]), "f64") for i in idx}
+    cpu_s = time.perf_counter() - t0
+    cpu_ps = sum(qs[i].n * (qs[i].nt - 1) for i in idx)
+    for fp in ("f64", "f32"):
+        for arith in ("fast", "reference"):
+            t0 = time.perf_counter()
+            b = lss.black_scholes_batch(qs, fp, arith)
+            create_s = time.perf_counter() - t0
+            b.run()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            reps = 3
+            with ClockSampler(0) as clk:
+                e0.record()
+                for _ in range(reps):
+                    b.run()
+                e1.record()
+                torch.cuda.synchronize()
+            secs = e0.elapsed_time(e1) / 1e3 / reps
+            # end to end: new terminal conditions from pinned host memory, values back
+            init = np.concatenate([np.maximum(0.0, b.grid(i).astype(np.float64) - qs[i].strike) for i in range(count)])
+            init_t = torch.from_numpy(init.astype(np.float64 if fp == "f64" else np.float32)).pin_memory()
+            init_np = init_t.numpy()
+            b.run_host(init_np)
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                vals, st = b.run_host(init_np)
+            e2e_s = (time.perf_counter() - t0) / reps
+            errs = [_rel_err(b.solution(i), wants[i]) for i in idx]
+            rec = {"config": f"batched 1-D Black-Scholes, {count} uneven calls (seed {HEAT1D_SEED})",
+                   "precision": fp, "arith": arith, "device_point_steps_per_s": ps / secs, "device_seconds": secs,
+                   "e2e": {"value": ps / e2e_s, "unit": "point-steps/s", "h2d_bytes_per_step": int(init_np.nbytes),
+                           "d2h_bytes_per_step": int(count * (8 + 4))},
+                   "create_seconds": create_s, "gpu_launches_per_run": b.launch_count(),
+                   "nonfinite_instances": int(np.count_nonzero(st)),
+                   "max_rel_err_vs_fp64_oracle_sample": float(max(errs)), "sample": sample,
+                   "clocks": clk.summary()}
+            if arith == "fast":
+                gbs = ps * HEAT1D_BYTES_PER_PS[fp] / secs / 1e9
+                rec["roofline"] = {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                                   "peak_source": peak_kind, "bytes_per_point_step": HEAT1D_BYTES_PER_PS[fp]}
+                if fp == "f64":
+                    rec["fp64_pipe"] = {"fp64_ops_per_point_step": 5, "achieved_ops_per_s": 5 * ps / secs,
+                                        "frac_of_5.98e11": 5 * ps / secs / FP64_INSTR_PEAK}
+            else:
+                eq = [bool(np.array_equal(b.solution(i), O.solve_1d(oproblem(qs[i]), fp))) for i in idx[:16]]
+                rec["bitwise_equal_oracle_sample"] = f"{sum(eq)}/{len(eq)}"
+            print(json.dumps(rec), flush=True)
+            del b
+    base = {"config": "batched 1-D Black-Scholes CPU baselines", "oracle_point_steps_per_s_1core": cpu_ps / cpu_s,
+            "sample": f"{sample} instances of the batch, full time loops"}
+    if O.reference_1d_available():
+        t0 = time.perf_counter()
+        ref_ps = 0
+        for i in idx[:16]:
+            _, sec = O.run_reference_1d(oproblem(qs[i]), "f64")
+            ref_ps += qs[i].n * (qs[i].nt - 1) / sec
+        base["reference_point_steps_per_s_1core"] = ref_ps / 16
+        base["reference_sample"] = "16 instances, compiled reference host Thomas LU, solver time only"
+    print(json.dumps(base), flush=True)
 
 
 def run_config4(count=1024, sample=16):

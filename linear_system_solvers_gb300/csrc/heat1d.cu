@@ -15,8 +15,9 @@
 // instance, all walking their line in step) is one 256-byte (FP64) line.  Slots of a group's
 // point block (n*32 elements each):
 //   REFERENCE: 0 A_, 1 B_, 2 D_ (scheme coefficients), 4 gamma / L, 5 sol / K, 6 U
-//   FAST:      0 WA, 1 WB, 2 WD (right-hand-side weights scaled by the pivot reciprocal),
-//              3 M (a_t / beta_t), 4 G (gamma_t), 5 KR (k / beta_t), 6 U, 7 Y (forward sweep)
+//   FAST:      1 WB, 2 WD (right-hand-side weights of u_t, u_{t+1} scaled by the pivot reciprocal;
+//              the weight of u_{t-1} is -(1-theta)/theta * M), 3 M (a_t / beta_t), 4 G (gamma_t),
+//              5 KR (k / beta_t), 6 U, 7 Y (forward sweep); slot 0 keeps A_ (unused)
 // Per-step boundary values (2 per step) and source rows are interleaved the same way.  The
 // whole time loop of an instance runs in one thread of one launch: there is no exchange
 // between instances and no per-step launch.
@@ -37,6 +38,9 @@ namespace heat1d {
 
 constexpr int LANES = 32;
 constexpr int NSLOT = 8;
+constexpr int H1_PF = 8; // prefetch distance (points) of the factorised sweeps
+// elements after the last group: the sweeps may load up to H1_PF + 1 points past a row
+constexpr long long H1_PAD = (H1_PF + 2) * 32;
 enum { S_A = 0, S_B = 1, S_D = 2, S_M = 3, S_G = 4, S_K = 5, S_U = 6, S_Y = 7 };
 
 // One instance (device).  Solver-type scalars are stored as double (exact).
@@ -138,7 +142,7 @@ template <typename T> __device__ __forceinline__ void ref_split(T th, T A, T B, 
     c = R::mul(-th, D);
 }
 
-template <typename T, bool DS> __global__ void __launch_bounds__(128) k_h1_ref(const h1params<T> p)
+template <typename T, bool DS, int PF> __global__ void __launch_bounds__(128) k_h1_ref(const h1params<T> p)
 {
     using R = ar<true>;
     const int g = blockIdx.x * (blockDim.x / LANES) + threadIdx.x / LANES;
@@ -170,9 +174,18 @@ template <typename T, bool DS> __global__ void __launch_bounds__(128) k_h1_ref(c
         const T lv = BND[el(2 * s)], hv = BND[el(2 * s + 1)];
         const T *S0 = has_src ? SRC + static_cast<long long>(s) * NS : nullptr;
         const T *S1 = has_src ? S0 + NS : nullptr;
-        auto rhs = [&](int t, T um, T uc, T up) -> T {
-            return ref_rhs<T>(t, N, lo_kind, hi_kind, A[el(t)], B[el(t)], D[el(t)], um, uc, up, th, h, k, lv, ll, hv, hl,
-                              has_src, has_src ? S0[el(t)] : T(0), has_src ? S1[el(t)] : T(0));
+        auto rhs_v = [&](int t, T Av, T Bv, T Dv, T um, T uc, T up) -> T {
+            return ref_rhs<T>(t, N, lo_kind, hi_kind, Av, Bv, Dv, um, uc, up, th, h, k, lv, ll, hv, hl, has_src,
+                              has_src ? S0[el(t)] : T(0), has_src ? S1[el(t)] : T(0));
+        };
+        auto rhs = [&](int t, T um, T uc, T up) -> T { return rhs_v(t, A[el(t)], B[el(t)], D[el(t)], um, uc, up); };
+        // rings of PF points: the loads of point t + PF are issued before point t is computed
+        T ra[PF], rb[PF], rd[PF], ru[PF];
+        auto load_pt = [&](int j, int t) {
+            ra[j] = A[el(t)];
+            rb[j] = B[el(t)];
+            rd[j] = D[el(t)];
+            ru[j] = t < N ? U[el(t + 1)] : T(0);
         };
         if (!DS) {
             // thomas_lu_solver::kernel: init_coefficients, forward loops (fused: each value is
@@ -197,17 +210,28 @@ template <typename T, bool DS> __global__ void __launch_bounds__(128) k_h1_ref(c
             GM[el(start)] = gam;
             SL[el(start)] = z;
             T sol = z;
-            for (int t = start + 1; t < end; ++t) {
-                um = uc;
-                uc = up;
-                up = U[el(t + 1)];
-                ref_split(th, A[el(t)], B[el(t)], D[el(t)], a, b, c);
-                const T f = rhs(t, um, uc, up);
-                beta = R::sub(b, R::mul(a, gam));
-                gam = R::div(c, beta);
-                sol = R::div(R::sub(f, R::mul(a, sol)), beta);
-                GM[el(t)] = gam;
-                SL[el(t)] = sol;
+#pragma unroll
+            for (int j = 0; j < PF; ++j)
+                if (start + 1 + j < end) load_pt(j, start + 1 + j);
+            for (int tb = start + 1; tb < end; tb += PF) {
+#pragma unroll
+                for (int j = 0; j < PF; ++j) {
+                    const int t = tb + j;
+                    if (t < end) {
+                        const T Av = ra[j], Bv = rb[j], Dv = rd[j], un = ru[j];
+                        if (t + PF < end) load_pt(j, t + PF);
+                        um = uc;
+                        uc = up;
+                        up = un;
+                        ref_split(th, Av, Bv, Dv, a, b, c);
+                        const T f = rhs_v(t, Av, Bv, Dv, um, uc, up);
+                        beta = R::sub(b, R::mul(a, gam));
+                        gam = R::div(c, beta);
+                        sol = R::div(R::sub(f, R::mul(a, sol)), beta);
+                        GM[el(t)] = gam;
+                        SL[el(t)] = sol;
+                    }
+                }
             }
             // final_coefficients at the last solved row
             um = uc;
@@ -229,9 +253,26 @@ template <typename T, bool DS> __global__ void __launch_bounds__(128) k_h1_ref(c
             const T beta_e = R::sub(bn, R::mul(an, gam));
             T x = R::div(R::sub(rn, R::mul(an, sol)), beta_e);
             U[el(end)] = x;
-            for (int t = end - 1; t >= start; --t) {
-                x = R::sub(SL[el(t)], R::mul(GM[el(t)], x));
-                U[el(t)] = x;
+#pragma unroll
+            for (int j = 0; j < PF; ++j)
+                if (end - 1 - j >= start) {
+                    ra[j] = SL[el(end - 1 - j)];
+                    rb[j] = GM[el(end - 1 - j)];
+                }
+            for (int tb = end - 1; tb >= start; tb -= PF) {
+#pragma unroll
+                for (int j = 0; j < PF; ++j) {
+                    const int t = tb - j;
+                    if (t >= start) {
+                        const T sv = ra[j], gv = rb[j];
+                        if (t - PF >= start) {
+                            ra[j] = SL[el(t - PF)];
+                            rb[j] = GM[el(t - PF)];
+                        }
+                        x = R::sub(sv, R::mul(gv, x));
+                        U[el(t)] = x;
+                    }
+                }
             }
             if (start == 1) U[el(0)] = lv;
             if (end == N - 1) U[el(N)] = hv;
@@ -239,7 +280,6 @@ template <typename T, bool DS> __global__ void __launch_bounds__(128) k_h1_ref(c
             // double_sweep_solver::kernel
             const int start = lo_kind == LSS_HEAT1D_DIRICHLET ? 1 : 0;
             const int end = hi_kind == LSS_HEAT1D_DIRICHLET ? n - 2 : n - 1;
-            const T step2 = T(0); (void)step2;
             T Kp, Lp;
             T um = U[el(0)], uc = U[el(0)], up = U[el(1)];
             T a, b, c;
@@ -256,21 +296,32 @@ template <typename T, bool DS> __global__ void __launch_bounds__(128) k_h1_ref(c
             SL[el(0)] = Kp;
             GM[el(0)] = Lp;
             T Kq = T(0), Lq = T(0); // K_{N-1}, L_{N-1} when the loop ends at N
-            for (int t = 1; t <= end; ++t) {
-                um = uc;
-                uc = up;
-                up = t < N ? U[el(t + 1)] : T(0);
-                ref_split(th, A[el(t)], B[el(t)], D[el(t)], a, b, c);
-                const T f = rhs(t, um, uc, up);
-                const T tmp = R::add(b, R::mul(a, Lp));
-                const T Ln = R::div(R::mul(T(-1), c), tmp);
-                const T Kn = R::div(R::sub(f, R::mul(a, Kp)), tmp);
-                Kq = Kp;
-                Lq = Lp;
-                Kp = Kn;
-                Lp = Ln;
-                SL[el(t)] = Kn;
-                GM[el(t)] = Ln;
+#pragma unroll
+            for (int j = 0; j < PF; ++j)
+                if (1 + j <= end) load_pt(j, 1 + j);
+            for (int tb = 1; tb <= end; tb += PF) {
+#pragma unroll
+                for (int j = 0; j < PF; ++j) {
+                    const int t = tb + j;
+                    if (t <= end) {
+                        const T Av = ra[j], Bv = rb[j], Dv = rd[j], un = ru[j];
+                        if (t + PF <= end) load_pt(j, t + PF);
+                        um = uc;
+                        uc = up;
+                        up = un;
+                        ref_split(th, Av, Bv, Dv, a, b, c);
+                        const T f = rhs_v(t, Av, Bv, Dv, um, uc, up);
+                        const T tmp = R::add(b, R::mul(a, Lp));
+                        const T Ln = R::div(R::mul(T(-1), c), tmp);
+                        const T Kn = R::div(R::sub(f, R::mul(a, Kp)), tmp);
+                        Kq = Kp;
+                        Lq = Lp;
+                        Kp = Kn;
+                        Lp = Ln;
+                        SL[el(t)] = Kn;
+                        GM[el(t)] = Ln;
+                    }
+                }
             }
             T x;
             if (hi_kind == LSS_HEAT1D_DIRICHLET) {
@@ -284,9 +335,26 @@ template <typename T, bool DS> __global__ void __launch_bounds__(128) k_h1_ref(c
                 x = R::div(R::add(R::mul(Lp, R::sub(Kq, cst)), Kp), den);
             }
             U[el(N)] = x;
-            for (int t = N - 1; t >= start; --t) {
-                x = R::add(R::mul(GM[el(t)], x), SL[el(t)]);
-                U[el(t)] = x;
+#pragma unroll
+            for (int j = 0; j < PF; ++j)
+                if (N - 1 - j >= start) {
+                    ra[j] = SL[el(N - 1 - j)];
+                    rb[j] = GM[el(N - 1 - j)];
+                }
+            for (int tb = N - 1; tb >= start; tb -= PF) {
+#pragma unroll
+                for (int j = 0; j < PF; ++j) {
+                    const int t = tb - j;
+                    if (t >= start) {
+                        const T kv = ra[j], lv2 = rb[j];
+                        if (t - PF >= start) {
+                            ra[j] = SL[el(t - PF)];
+                            rb[j] = GM[el(t - PF)];
+                        }
+                        x = R::add(R::mul(lv2, x), kv);
+                        U[el(t)] = x;
+                    }
+                }
             }
             if (start == 1) U[el(0)] = lv;
         }
@@ -304,9 +372,10 @@ template <typename T, bool DS> __global__ void __launch_bounds__(128) k_h1_ref(c
 
 // ------------------------------------------------------------------------------------------
 // FAST: one factorisation per instance (set-up), then per step one fused right-hand-side +
-// forward sweep y_t = WD u_{t+1} + WB u_t + WA u_{t-1} - M y_{t-1} (+ boundary / source terms)
-// and one back substitution x_t = y_t - G x_{t+1}.  Five loads, one store and five FMAs per
-// point forward; two loads, one store and one FMA per point backward.
+// forward sweep y_t = WB u_t + WD u_{t+1} + M (kap u_{t-1} - y_{t-1}) (+ boundary / source
+// terms; kap = -(1-theta)/theta) and one back substitution x_t = y_t - G x_{t+1}.  Four loads,
+// one store and four FP64 operations per point forward; two loads, one store and one FMA per
+// point backward: 64 bytes per point-step in FP64.
 // ------------------------------------------------------------------------------------------
 template <typename T> __global__ void __launch_bounds__(128) k_h1_setup_fast(const h1params<T> p)
 {
@@ -329,7 +398,7 @@ template <typename T> __global__ void __launch_bounds__(128) k_h1_setup_fast(con
     for (int t = 0; t < n; ++t) {
         const T A = WA[el(t)], B = WB[el(t)], D = WD[el(t)];
         if (t < start || t > end) {
-            WA[el(t)] = WB[el(t)] = WD[el(t)] = M[el(t)] = GG[el(t)] = KR[el(t)] = T(0);
+            WB[el(t)] = WD[el(t)] = M[el(t)] = GG[el(t)] = KR[el(t)] = T(0);
             continue;
         }
         const T a = -th * A, b = one + T(2) * th * B, c = -th * D;
@@ -367,7 +436,7 @@ template <typename T> __global__ void __launch_bounds__(128) k_h1_setup_fast(con
             if (t == end) bh = -c * rb; // Dirichlet upper end: - c_{N-1} v_hi / beta_{N-1}
             KR[el(t)] = k * rb;
         }
-        WA[el(t)] = wa;
+        (void)wa; // = kap * m, formed by the sweep
         WB[el(t)] = wb;
         WD[el(t)] = wd;
         M[el(t)] = m;
@@ -379,7 +448,13 @@ template <typename T> __global__ void __launch_bounds__(128) k_h1_setup_fast(con
     L.bh = static_cast<double>(bh);
 }
 
-template <typename T> __global__ void __launch_bounds__(128) k_h1_fast(const h1params<T> p)
+// Per step: the first solved row, the interior rows in blocks of PF (the loads of point t + PF
+// are issued before point t is computed, from a ring of PF registers per array; loads past the
+// last row stay inside the group's block and are never used), the last solved row, then the
+// back substitution the same way downwards.  SRC: the batch has heat sources; KEEP: every time
+// level is written out.
+template <typename T, int PF, bool SRC, bool KEEP>
+__global__ void __launch_bounds__(128, 4) k_h1_fast(const h1params<T> p)
 {
     const int g = blockIdx.x * (blockDim.x / LANES) + threadIdx.x / LANES;
     const int lane = threadIdx.x % LANES;
@@ -388,60 +463,132 @@ template <typename T> __global__ void __launch_bounds__(128) k_h1_fast(const h1p
     if (lane >= G.lanes) return;
     const h1lane L = p.lanes[static_cast<long long>(g) * LANES + lane];
     const int n = G.n, N = n - 1;
-    const long long NS = static_cast<long long>(n) * LANES;
+    const int NS = n * LANES;
     T *base = p.pt + G.pt + lane;
-    const T *WA = base + S_A * NS, *WB = base + S_B * NS, *WD = base + S_D * NS;
-    const T *M = base + S_M * NS, *GG = base + S_G * NS, *KR = base + S_K * NS;
-    T *U = base + S_U * NS, *Y = base + S_Y * NS;
+    const T *__restrict__ WB = base + S_B * NS;
+    const T *__restrict__ WD = base + S_D * NS;
+    const T *__restrict__ M = base + S_M * NS;
+    const T *__restrict__ GG = base + S_G * NS;
+    const T *__restrict__ KR = base + S_K * NS;
+    T *__restrict__ U = base + S_U * NS;
+    T *__restrict__ Y = base + S_Y * NS;
     const T *BND = p.bnd + G.bnd + lane;
-    const bool has_src = L.has_src != 0;
-    const T *SRC = has_src ? p.src + G.src + lane : nullptr;
-    T *ALL = G.all >= 0 ? p.all + G.all + lane : nullptr;
+    const bool has_src = SRC && L.has_src != 0;
+    const T *SRCP = has_src ? p.src + G.src + lane : nullptr;
+    T *ALL = KEEP ? p.all + G.all + lane : nullptr;
     const T th = T(L.theta), omt = T(1) - th, bl = T(L.bl), bh = T(L.bh);
+    const T kap = -omt / th; // -1 (Crank-Nicolson) or 0 (Euler), exact
     const int start = L.start, end = L.end, steps = L.steps;
+    const int S = LANES;
 
-    for (int t = 0; t < n; ++t) U[el(t)] = p.init[L.init_off + t];
+    for (int t = 0; t < n; ++t) U[t * S] = p.init[L.init_off + t];
     int row = L.forward ? 0 : steps;
-    if (ALL)
-        for (int t = 0; t < n; ++t) ALL[(static_cast<long long>(row) * n + t) * LANES] = U[el(t)];
+    if (KEEP)
+        for (int t = 0; t < n; ++t) ALL[(static_cast<long long>(row) * n + t) * S] = U[t * S];
 
     for (int s = 0; s < steps; ++s) {
-        const T lv = BND[el(2 * s)], hv = BND[el(2 * s + 1)];
-        T um = start ? U[el(0)] : T(0), uc = U[el(start)];
-        T yp = start ? lv : T(0);
-        T y = T(0);
-#pragma unroll 4
-        for (int t = start; t <= end; ++t) {
-            const T up = t < N ? U[el(t + 1)] : T(0);
-            y = WB[el(t)] * uc + WD[el(t)] * up + WA[el(t)] * um - M[el(t)] * yp;
-            if (t == 0) y += bl * lv;
-            if (t == end) y += bh * hv;
-            if (has_src) {
-                const T *S0 = SRC + static_cast<long long>(s) * NS;
-                y += KR[el(t)] * (th * S0[NS + el(t)] + omt * S0[el(t)]);
+        const T lv = BND[(2 * s) * S], hv = BND[(2 * s + 1) * S];
+        const T *S0 = has_src ? SRCP + static_cast<long long>(s) * NS : nullptr;
+        auto src_term = [&](int t) -> T {
+            return has_src ? KR[t * S] * (th * S0[NS + t * S] + omt * S0[t * S]) : T(0);
+        };
+        // first solved row.  Every row's weight of u_{t-1} is kap * M_t (a_t = -theta A_t, so
+        // (1 - theta) A_t / beta_t = kap a_t / beta_t, also in the Neumann / Robin end rows):
+        // y_t = WB u_t + WD u_{t+1} + M (kap u_{t-1} - y_{t-1}), four loads per point
+        T um = start ? U[0] : T(0);
+        T uc = U[start * S];
+        T up = U[(start + 1) * S];
+        T yp = WB[start * S] * uc + WD[start * S] * up + M[start * S] * (kap * um - (start ? lv : T(0)));
+        if (start == 0) yp += bl * lv;
+        yp += src_term(start);
+        Y[start * S] = yp;
+        um = uc;
+        uc = up;
+        // interior rows start+1 .. end-1
+        T rwb[PF], rwd[PF], rm[PF], rup[PF];
+        int t = start + 1;
+#pragma unroll
+        for (int j = 0; j < PF; ++j) {
+            const int q = (t + j) * S;
+            rwb[j] = WB[q];
+            rwd[j] = WD[q];
+            rm[j] = M[q];
+            rup[j] = U[q + S];
+        }
+        for (; t + PF <= end; t += PF) {
+#pragma unroll
+            for (int j = 0; j < PF; ++j) {
+                const T wb = rwb[j], wd = rwd[j], m = rm[j], u1 = rup[j];
+                const int q = (t + j + PF) * S;
+                rwb[j] = WB[q];
+                rwd[j] = WD[q];
+                rm[j] = M[q];
+                rup[j] = U[q + S];
+                T y = wb * uc + wd * u1 + m * (kap * um - yp);
+                if (SRC) y += src_term(t + j);
+                Y[(t + j) * S] = y;
+                yp = y;
+                um = uc;
+                uc = u1;
             }
-            Y[el(t)] = y;
-            yp = y;
-            um = uc;
-            uc = up;
         }
-        T x = y;
-        U[el(end)] = x;
-#pragma unroll 4
-        for (int t = end - 1; t >= start; --t) {
-            x = Y[el(t)] - GG[el(t)] * x;
-            U[el(t)] = x;
+#pragma unroll
+        for (int j = 0; j < PF; ++j) {
+            if (t + j < end) {
+                T y = rwb[j] * uc + rwd[j] * rup[j] + rm[j] * (kap * um - yp);
+                if (SRC) y += src_term(t + j);
+                Y[(t + j) * S] = y;
+                yp = y;
+                um = uc;
+                uc = rup[j];
+            }
         }
-        if (start == 1) U[el(0)] = lv;
-        if (end == N - 1) U[el(N)] = hv;
+        // last solved row
+        T x = yp;
+        if (end > start) {
+            const int q = end * S;
+            const T u1 = end < N ? U[q + S] : T(0);
+            x = WB[q] * uc + WD[q] * u1 + M[q] * (kap * um - yp) + bh * hv;
+            x += src_term(end);
+        }
+        U[end * S] = x;
+        // back substitution end-1 .. start
+        T ry[PF], rg[PF];
+        t = end - 1;
+#pragma unroll
+        for (int j = 0; j < PF; ++j) {
+            const int q = (t - j) * S;
+            ry[j] = Y[q];
+            rg[j] = GG[q];
+        }
+        for (; t - PF >= start - 1; t -= PF) {
+#pragma unroll
+            for (int j = 0; j < PF; ++j) {
+                const T yv = ry[j], gv = rg[j];
+                const int q = (t - j - PF) * S;
+                ry[j] = Y[q];
+                rg[j] = GG[q];
+                x = yv - gv * x;
+                U[(t - j) * S] = x;
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < PF; ++j) {
+            if (t - j >= start) {
+                x = ry[j] - rg[j] * x;
+                U[(t - j) * S] = x;
+            }
+        }
+        if (start == 1) U[0] = lv;
+        if (end == N - 1) U[N * S] = hv;
         row += L.forward ? 1 : -1;
-        if (ALL)
-            for (int t = 0; t < n; ++t) ALL[(static_cast<long long>(row) * n + t) * LANES] = U[el(t)];
+        if (KEEP)
+            for (int q = 0; q < n; ++q) ALL[(static_cast<long long>(row) * n + q) * S] = U[q * S];
     }
     int bad = 0;
-    for (int t = 0; t < n; ++t) bad |= !isfinite(static_cast<double>(U[el(t)]));
+    for (int q = 0; q < n; ++q) bad |= !isfinite(static_cast<double>(U[q * S]));
     const int i = L.eval_i;
-    p.values[L.inst] = (1.0 - L.eval_w) * static_cast<double>(U[el(i)]) + L.eval_w * static_cast<double>(U[el(i + 1)]);
+    p.values[L.inst] = (1.0 - L.eval_w) * static_cast<double>(U[i * S]) + L.eval_w * static_cast<double>(U[(i + 1) * S]);
     p.status[L.inst] = bad;
 }
 
@@ -662,8 +809,8 @@ template <typename T> int batch_t<T>::build(std::vector<inst_info> &&inf, std::v
     LSS_CUDA_TRY(d_groups.upload(groups.data(), groups.size()), "heat1d: uploading groups");
     LSS_CUDA_TRY(d_lanes.alloc(lanes.size()), "heat1d: allocating lanes");
     LSS_CUDA_TRY(d_lanes.upload(lanes.data(), lanes.size()), "heat1d: uploading lanes");
-    LSS_CUDA_TRY(d_pt.alloc(pt), "heat1d: allocating point arrays");
-    LSS_CUDA_TRY(cudaMemset(d_pt.p, 0, pt * sizeof(T)), "heat1d: clearing point arrays");
+    LSS_CUDA_TRY(d_pt.alloc(pt + H1_PAD), "heat1d: allocating point arrays");
+    LSS_CUDA_TRY(cudaMemset(d_pt.p, 0, (pt + H1_PAD) * sizeof(T)), "heat1d: clearing point arrays");
     LSS_CUDA_TRY(d_bnd.alloc(std::max(1LL, bnd)), "heat1d: allocating boundary values");
     LSS_CUDA_TRY(cudaMemset(d_bnd.p, 0, d_bnd.n * sizeof(T)), "heat1d: clearing boundary values");
     if (src > 0) {
@@ -747,12 +894,17 @@ template <typename T> int batch_t<T>::run(cudaStream_t s)
 {
     const h1params<T> p = params();
     const int blocks = grid_for(static_cast<long long>(groups.size()) * LANES, 128);
-    if (arith == LSS_ADI_ARITH_FAST)
-        k_h1_fast<T><<<blocks, 128, 0, s>>>(p);
+    const bool keep = d_all.p != nullptr, src = d_src.p != nullptr;
+    if (arith == LSS_ADI_ARITH_FAST) {
+        if (keep && src) k_h1_fast<T, H1_PF, true, true><<<blocks, 128, 0, s>>>(p);
+        else if (keep) k_h1_fast<T, H1_PF, false, true><<<blocks, 128, 0, s>>>(p);
+        else if (src) k_h1_fast<T, H1_PF, true, false><<<blocks, 128, 0, s>>>(p);
+        else k_h1_fast<T, H1_PF, false, false><<<blocks, 128, 0, s>>>(p);
+    }
     else if (ds)
-        k_h1_ref<T, true><<<blocks, 128, 0, s>>>(p);
+        k_h1_ref<T, true, 4><<<blocks, 128, 0, s>>>(p);
     else
-        k_h1_ref<T, false><<<blocks, 128, 0, s>>>(p);
+        k_h1_ref<T, false, 4><<<blocks, 128, 0, s>>>(p);
     LSS_CUDA_TRY(cudaGetLastError(), "heat1d: launching the time loop");
     return LSS_ADI_OK;
 }
