@@ -1,5 +1,6 @@
 /*
- * lss_oracle.h -- CPU oracle for the 2-D Heston/SABR ADI hot path.
+ * lss_oracle.h -- CPU oracle for the 2-D Heston/SABR ADI hot path and the 1-D implicit heat
+ * path (the latter at the end of this header, lss_oracle_1d_impl.h).
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product (the CUDA library, its
  * C-ABI, the Python package) may include, link or call this code.  Only the

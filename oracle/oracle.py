@@ -8,6 +8,8 @@ imports it.
   the host Thomas-LU / double-sweep ADI path of MichalSara99/linear_system_solvers).
 * ``run_reference(problem, fp)`` runs the reference itself, compiled by
   ``build_ref.sh`` into ``oracle/_ref/ref_driver`` (only where it was built).
+* ``solve_1d`` / ``tables_1d`` / ``run_reference_1d``: the same for the 1-D implicit heat path
+  (``lss_oracle_1d_impl.h``, ``oracle/_ref/ref_driver_1d``).
 """
 from __future__ import annotations
 
