@@ -109,79 +109,83 @@ __device__ __forceinline__ void adj_v(const inst_view<double> &v, const double *
     }
 }
 
-// d(residual)/d(coefficient) at one S-stage point o (row t of line j): M, Z, P, M~, W, P~, C.
-// KIND 1: the first stage on U with output Yo = Y1.  KIND 2: the second stage, whose extra
-// terms on Delta = Y2 - U carry the weight zt (zeta - theta for MCS, zeta for HV, 0 for CS).
-struct s_terms {
-    double M, Z, P, Mt, W, Pt, C;
-};
-template <int KIND>
-__device__ __forceinline__ s_terms adj_s_terms(const bdesc &d, long long o, int ny, const double *__restrict__ U,
-                                               const double *__restrict__ Y1, const double *__restrict__ Y2,
-                                               const double *__restrict__ Yo, double th, double zt, bool hv)
-{
-    s_terms r;
-    const double Uw = U[o - ny], Uc = U[o], Ue = U[o + ny], Us = U[o - 1], Un = U[o + 1];
-    if constexpr (KIND == 1) {
-        const double omt = 1.0 - th;
-        r.M = omt * Uw + th * Yo[o - ny];
-        r.Z = -(omt * Uc + th * Yo[o]);
-        r.P = omt * Ue + th * Yo[o + ny];
-        r.Mt = Us;
-        r.W = -Uc;
-        r.Pt = Un;
-        r.C = d.a_gamma * ((U[o - ny - 1] - U[o - ny + 1]) + (U[o + ny + 1] - U[o + ny - 1]));
-    } else {
-        if (hv) {
-            const double Dw = Y2[o - ny] - Uw, Dc = Y2[o] - Uc, De = Y2[o + ny] - Ue;
-            r.M = th * (Yo[o - ny] - Y1[o - ny] - Dw) + zt * Dw;
-            r.Z = -th * (Yo[o] - Y1[o] - Dc) - zt * Dc;
-            r.P = th * (Yo[o + ny] - Y1[o + ny] - De) + zt * De;
-            r.W = -zt * Dc;
-            r.Mt = zt * (Y2[o - 1] - Us);
-            r.Pt = zt * (Y2[o + 1] - Un);
-        } else if (zt != 0.0) {
-            const double Dw = Y2[o - ny] - Uw, Dc = Y2[o] - Uc, De = Y2[o + ny] - Ue;
-            r.M = th * (Yo[o - ny] - Uw) + zt * Dw;
-            r.Z = -th * (Yo[o] - Uc) - zt * Dc;
-            r.P = th * (Yo[o + ny] - Ue) - zt * De; // the reference's sign of the P term
-            r.W = -zt * Dc;
-            r.Mt = zt * (Y2[o - 1] - Us);
-            r.Pt = zt * (Y2[o + 1] - Un);
-        } else {
-            // Craig-Sneyd: no extra term, only M, Z, P, C depend on this stage's residual
-            r.M = th * (Yo[o - ny] - Uw);
-            r.Z = -th * (Yo[o] - Uc);
-            r.P = th * (Yo[o + ny] - Ue);
-            r.W = 0.0;
-            r.Mt = 0.0;
-            r.Pt = 0.0;
-        }
-        const double mix = ((Y2[o - ny - 1] - U[o - ny - 1]) - (Y2[o - ny + 1] - U[o - ny + 1])) +
-                           ((Y2[o + ny + 1] - U[o + ny + 1]) - (Y2[o + ny - 1] - U[o + ny - 1]));
-        r.C = d.a_zeta * d.a_gamma * mix;
-    }
-    return r;
-}
-
 // Line sums of mu * d(residual)/d(parameter) pieces of an S line (the S-direction factors of the
 // coefficient derivatives applied per point; the v-direction ones once per line, adj_s_line).
 struct s_sums {
     double A, B, Q, D, E, Aa, Dd;
 };
-__device__ __forceinline__ void adj_s_sum(const inst_view<double> &v, s_sums &p, const s_terms &s, double mu, int t,
-                                          bool vterms, bool sabr)
+// Per point, mu times the coefficient derivatives of the stage residual (d/dM, d/dZ, d/dP,
+// d/dM~, d/dW, d/dP~, d/dC) enter the parameter sums only as P - M, Z + W, P~ - M~,
+// M~ + P~ + 2W, C and M + P + 2Z: a three-row window along the line (rows t+1, t, t-1, one new
+// row per point; adj_s_row) gives them from per-row quantities
+//   KIND 1 (first S stage, output Yo = Y1): f = (1-theta) U + theta Yo, c = U, s / n = U at
+//          j-1 / j+1, dd = s - n;
+//   KIND 2 (second S stage of CS/MCS/HV): the same on Delta = Y2 - U, with f = Yo - U
+//          (CS/MCS) or Yo - Y1 - Delta (HV).
+struct s_row {
+    double f, c, s, n, dd;
+};
+struct s_comb {
+    double PmM, ZpW, PtmMt, D2, C, MpP2Z;
+};
+template <int KIND>
+__device__ __forceinline__ s_row adj_s_row(const double *__restrict__ U, const double *__restrict__ Y1,
+                                           const double *__restrict__ Y2, const double *__restrict__ Yo, long long q,
+                                           double th, bool hv)
 {
-    p.A += mu * __ldg(v.X(X_HX) + t) * (s.P - s.M);
-    p.B += mu * (s.Z + s.W);
+    s_row w;
+    if constexpr (KIND == 1) {
+        w.s = U[q - 1];
+        w.c = U[q];
+        w.n = U[q + 1];
+        w.f = (1.0 - th) * w.c + th * Yo[q];
+    } else {
+        w.s = Y2[q - 1] - U[q - 1];
+        w.c = Y2[q] - U[q];
+        w.n = Y2[q + 1] - U[q + 1];
+        w.f = hv ? (Yo[q] - Y1[q] - w.c) : (Yo[q] - U[q]);
+    }
+    w.dd = w.s - w.n;
+    return w;
+}
+// terms at row t from the rows t+1 (rh), t (rc), t-1 (rl); zt weighs the Delta terms (MCS:
+// zeta - theta with the reference's sign of the P term, HV: zeta with the textbook sign, CS: 0)
+template <int KIND>
+__device__ __forceinline__ s_comb adj_s_comb(const bdesc &d, const s_row &rh, const s_row &rc, const s_row &rl,
+                                             double th, double zt, bool hv)
+{
+    s_comb cb;
+    if constexpr (KIND == 1) {
+        cb.PmM = rh.f - rl.f;
+        cb.ZpW = -rc.f - rc.c;
+        cb.PtmMt = rc.n - rc.s;
+        cb.D2 = rc.s + rc.n - 2.0 * rc.c;
+        cb.C = d.a_gamma * (rl.dd - rh.dd);
+        cb.MpP2Z = rl.f + rh.f - 2.0 * rc.f;
+    } else {
+        const double sp = hv ? 1.0 : -1.0;
+        cb.PmM = th * (rh.f - rl.f) + zt * (sp * rh.c - rl.c);
+        cb.ZpW = -th * rc.f - 2.0 * zt * rc.c;
+        cb.PtmMt = zt * (rc.n - rc.s);
+        cb.D2 = zt * (rc.s + rc.n - 2.0 * rc.c);
+        cb.C = d.a_zeta * d.a_gamma * (rl.dd - rh.dd);
+        cb.MpP2Z = th * (rl.f + rh.f - 2.0 * rc.f) + zt * (rl.c + sp * rh.c - 2.0 * rc.c);
+    }
+    return cb;
+}
+__device__ __forceinline__ void adj_s_sum_c(const inst_view<double> &v, s_sums &p, const s_comb &s, double mu, int t,
+                                            bool vterms, bool sabr)
+{
+    p.A += mu * __ldg(v.X(X_HX) + t) * s.PmM;
+    p.B += mu * s.ZpW;
     if (vterms) {
-        p.Q += mu * (s.Pt - s.Mt);
-        p.D += mu * (s.Mt + s.Pt + 2.0 * s.W);
+        p.Q += mu * s.PtmMt;
+        p.D += mu * s.D2;
     }
     p.E += mu * __ldg(v.X(X_HC) + t) * s.C;
     if (sabr) {
-        p.Aa += mu * __ldg(v.X(X_HA) + t) * (s.M + s.P + 2.0 * s.Z);
-        p.Dd += mu * __ldg(v.X(X_HDD) + t) * (s.P - s.M);
+        p.Aa += mu * __ldg(v.X(X_HA) + t) * s.MpP2Z;
+        p.Dd += mu * __ldg(v.X(X_HDD) + t) * s.PmM;
     }
 }
 __device__ __forceinline__ void adj_s_line(const inst_view<double> &v, const bdesc &d, int j, const s_sums &p,
@@ -230,9 +234,13 @@ __device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d
         double w = 0.0, la_next = 0.0, w_e = 0.0;
         double acc_t1 = 0.0, acc_t = 0.0;
         s_sums ps = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        // three-row window along the line (rows t+1, t, t-1; one new row per point)
+        auto load_row = [&](int r) -> s_row { return adj_s_row<KIND>(U, Y1, Y2, Yo, (long long)r * ny + j, th, hv); };
+        s_row rh = load_row(e + 1), rc = load_row(e);
 #pragma unroll 2
         for (int t = e; t >= 1; --t) {
             const long long o = (long long)t * ny + j;
+            const s_row rl = load_row(t - 1);
             w = TMP[o] - la_next * w;
             if (t == e) w_e = w;
             FB[o] = w;
@@ -253,9 +261,11 @@ __device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d
                     Y1B[o] = mu;
                 }
             }
-            const s_terms st = adj_s_terms<KIND>(d, o, ny, U, Y1, Y2, Yo, th, zt, hv);
-            adj_s_sum(v, ps, st, mu, t, KIND == 1 || zt != 0.0, sabr);
+            const s_comb cb = adj_s_comb<KIND>(d, rh, rc, rl, th, zt, hv);
+            adj_s_sum_c(v, ps, cb, mu, t, KIND == 1 || zt != 0.0, sabr);
             la_next = la;
+            rh = rc;
+            rc = rl;
         }
         if constexpr (KIND == 2) {
             if (hv) {

@@ -485,8 +485,9 @@ template <typename T, int BS> __global__ void __launch_bounds__(BS, 1024 / BS) k
 #include "adi_adjoint.cuh"
 
 // Forward + adjoint of each instance by one CTA: forward pass keeping a checkpoint every
-// d.ck steps, then per segment (last first) a forward recomputation that keeps the stage
-// values of every step, followed by the adjoint steps of the segment in reverse order.
+// d.ck steps (and the stage values of every step of the last segment), then per segment (last
+// first) a forward recomputation that keeps the stage values of every step (not needed for the
+// last segment), followed by the adjoint steps of the segment in reverse order.
 // Results: value, the 5 parameter sensitivities, the final surface (state U arena) and
 // dV/d(initial condition) (state V arena).
 // Register budget ~72 per thread (896 / BS CTAs per SM): more resident warps to cover the load
@@ -537,9 +538,17 @@ template <int BS> __global__ void __launch_bounds__(BS, 896 / BS) k_batch_fwdadj
             }
         }
         __syncthreads();
-        // forward pass with checkpoints
+        // forward pass with checkpoints; the steps of the last segment keep their stage values in
+        // the segment slots, so the reverse sweep starts without recomputing that segment
         const double *cur = CK;
+        const int n0_last = (nseg - 1) * c;
         for (int step = 0; step < d.steps; ++step) {
+            if (step >= n0_last) {
+                const int m = step - n0_last;
+                fwd_step<double, BS>(v, d.scheme, cur, slot(m, 1), slot(m, 2), slot(m, 3), slot(m + 1, 0), sb0, d.bnc);
+                cur = slot(m + 1, 0);
+                continue;
+            }
             double *next = ((step + 1) % c == 0 && step + 1 < d.steps) ? CK + (long long)((step + 1) / c) * n
                                                                         : ((step & 1) ? W1 : W0);
             fwd_step<double, BS>(v, d.scheme, cur, slot(0, 1), slot(0, 2), slot(0, 3), next, sb0, d.bnc);
@@ -578,7 +587,7 @@ template <int BS> __global__ void __launch_bounds__(BS, 896 / BS) k_batch_fwdadj
             const int n0 = sgi * c;
             const int L = min(c, d.steps - n0);
             const double *u0 = CK + (long long)sgi * n;
-            for (int m = 0; m < L; ++m) {
+            for (int m = 0; m < L && sgi < nseg - 1; ++m) {
                 const double *um = (m == 0) ? u0 : slot(m, 0);
                 fwd_step<double, BS>(v, d.scheme, um, slot(m, 1), slot(m, 2), slot(m, 3), slot(m + 1, 0), sb0, d.bnc);
             }
@@ -1004,8 +1013,12 @@ __global__ void __launch_bounds__(1024) k_wadj_s_chunk(const __grid_constant__ b
     acc_load(acc, acc_a, nacc, tid);
     const double *LA = v.S(SL_LA), *IB = v.S(SL_IB);
     s_sums ps = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    // three-row window over the chunk's rows (adj_s_row / adj_s_comb)
+    s_row rh = adj_s_row<KIND>(U, Y1, Y2, Yo, (long long)(t1 + 1) * ny + j, th, hv);
+    s_row rc = adj_s_row<KIND>(U, Y1, Y2, Yo, (long long)t1 * ny + j, th, hv);
     for (int t = t1; t >= t0; --t) {
         const long long o = (long long)t * ny + j;
+        const s_row rl = adj_s_row<KIND>(U, Y1, Y2, Yo, o - ny, th, hv);
         const double w0 = TMP[o];
         FB[o] = w0;
         const double mu = __ldg(IB + o) * w0;
@@ -1021,8 +1034,9 @@ __global__ void __launch_bounds__(1024) k_wadj_s_chunk(const __grid_constant__ b
                 Y1B[o] = mu;
             }
         }
-        const s_terms st = adj_s_terms<KIND>(d, o, ny, U, Y1, Y2, Yo, th, zt, hv);
-        adj_s_sum(v, ps, st, mu, t, KIND == 1 || zt != 0.0, sabr);
+        adj_s_sum_c(v, ps, adj_s_comb<KIND>(d, rh, rc, rl, th, zt, hv), mu, t, KIND == 1 || zt != 0.0, sabr);
+        rh = rc;
+        rc = rl;
     }
     if (c == 0) {
         const double w1 = TMP[(long long)ny + j], la1 = __ldg(LA + ny + j);
@@ -1828,7 +1842,15 @@ template <typename T> int batch_typed<T>::enqueue_wide_adjoint(cudaStream_t s)
         long long nl = 0;
         const int per_step = d.scheme == LSS_ADI_DOUGLAS_RACHFORD ? 4 : 6;
         const double *cur = CK;
+        const int n0_last = (nseg - 1) * c; // the last segment keeps its stage values: no recomputation
         for (int step = 0; step < d.steps; ++step) {
+            if (step >= n0_last) {
+                const int m = step - n0_last;
+                enqueue_wide_step(s, p, cur, slot(m, 1), slot(m, 2), slot(m, 3), slot(m + 1, 0));
+                nl += per_step;
+                cur = slot(m + 1, 0);
+                continue;
+            }
             double *next = ((step + 1) % c == 0 && step + 1 < d.steps) ? CK + static_cast<long long>((step + 1) / c) * n
                                                                         : ((step & 1) ? W1 : W0);
             enqueue_wide_step(s, p, cur, slot(0, 1), slot(0, 2), slot(0, 3), next);
@@ -1843,7 +1865,7 @@ template <typename T> int batch_typed<T>::enqueue_wide_adjoint(cudaStream_t s)
             const int n0 = sgi * c;
             const int L = std::min(c, d.steps - n0);
             const double *u0 = CK + static_cast<long long>(sgi) * n;
-            for (int m = 0; m < L; ++m) {
+            for (int m = 0; m < L && sgi < nseg - 1; ++m) {
                 const double *um = (m == 0) ? u0 : slot(m, 0);
                 enqueue_wide_step(s, p, um, slot(m, 1), slot(m, 2), slot(m, 3), slot(m + 1, 0));
                 nl += per_step;
