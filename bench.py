@@ -32,12 +32,33 @@ BYTES_PER_GPS_FWD = {"dr": 40, "cs": 96, "mcs": 96, "hv": 96}  # algorithmic byt
 # DRAM bytes (read + write) per grid-point-step of the batched kernels from one ncu capture of
 # the 512-instance, 20-step case (--count 512 --max-time-steps 20), scaled to a launch by the
 # grid-point-steps it processes: mode 0 = k_batch_forward, mode 1 = k_batch_fwdadj
-DRAM_BYTES_PER_GPS = {0: 303.0, 1: 1134.0}
+DRAM_BYTES_PER_GPS = {0: 303.0, 1: 1056.0}
 # FP64 instructions (DFMA + DADD + DMUL, thread level) per grid-point-step from the same capture
 # (smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum), and the FP64 pipe's rate:
-# 1.196 TFLOP/s of DFMA measured on this GPU model = 5.98e11 FP64 instructions/s
-FP64_INSTR_PER_GPS = {0: 34.7, 1: 184.4}
+# 1.196 TFLOP/s of DFMA measured on this GPU model = 5.98e11 FP64 instructions/s.
+# Forward + adjoint = one forward pass, the recomputation of every checkpoint segment but the
+# last (a fraction rf of the steps, from the workload) and the adjoint steps:
+# FP64_FWD * (1 + rf) + FP64_ADJ; the capture (20 steps, 4 segments of 5: rf = 0.75) counted
+# 169.1, so FP64_ADJ = 169.1 - 34.7 * 1.75.
+FP64_INSTR_FWD = 34.7
+FP64_INSTR_ADJ = 169.1 - 34.7 * 1.75
 FP64_INSTR_PEAK = 5.98e11
+
+
+def recompute_fraction(problems):
+    """Grid-point-step weighted fraction of the steps the adjoint recomputes (every checkpoint
+    segment of ceil(sqrt(steps)) steps but the last)."""
+    import math
+
+    num = den = 0.0
+    for p in problems:
+        steps = p.nt - 1
+        c = max(1, math.ceil(math.sqrt(steps)))
+        nseg = (steps + c - 1) // c
+        w = p.nx * p.ny
+        num += w * (nseg - 1) * c
+        den += w * steps
+    return num / den if den else 0.0
 
 
 def parse():
@@ -342,6 +363,7 @@ def main():
         return
     value = gps_all / (t_max * 1e-3)
     bpg = BYTES_PER_GPS_FWD["mcs"] * (1 if mode == 0 else 10.0 / 3.0)
+    fp64_per_gps = FP64_INSTR_FWD if mode == 0 else FP64_INSTR_FWD * (1.0 + recompute_fraction(problems)) + FP64_INSTR_ADJ
     peak, peak_kind = measured_peaks()
     achieved = gps * bpg / (ms * 1e-3) / 1e9
     out = {
@@ -364,10 +386,11 @@ def main():
                                        "grid-point-step, times this launch's grid-point-steps", "peak_source": peak_kind,
                      "algorithmic_bytes_per_grid_point_step": bpg,
                      "note": "FP64 pipe (1.196 TFLOP/s measured) binds before HBM on GB300"},
-        "fp64_pipe": {"instructions_per_grid_point_step": FP64_INSTR_PER_GPS[mode],
-                      "achieved": gps * FP64_INSTR_PER_GPS[mode] / (ms * 1e-3), "peak": FP64_INSTR_PEAK,
-                      "unit": "FP64 instructions/s", "frac": gps * FP64_INSTR_PER_GPS[mode] / (ms * 1e-3) / FP64_INSTR_PEAK,
-                      "note": "the binding resource of this path; instruction counts from ncu, peak from a DFMA probe"},
+        "fp64_pipe": {"instructions_per_grid_point_step": fp64_per_gps,
+                      "achieved": gps * fp64_per_gps / (ms * 1e-3), "peak": FP64_INSTR_PEAK,
+                      "unit": "FP64 instructions/s", "frac": gps * fp64_per_gps / (ms * 1e-3) / FP64_INSTR_PEAK,
+                      "note": "the binding resource of this path; instruction counts from ncu (forward + adjoint: "
+                              "forward x (1 + recomputed fraction) + adjoint), peak from a DFMA probe"},
         "e2e": {"value": gps_all / e2e_s, "unit": "grid-point-steps/s", "h2d_bytes_per_step": int(total_n * 8),
                 "d2h_bytes_per_step": int(len(problems) * 8 * (6 if mode == 1 else 1)), "matches_device_values": e2e_ok},
         "gpu_launches": launches,

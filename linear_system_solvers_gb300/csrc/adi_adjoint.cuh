@@ -125,9 +125,6 @@ struct s_sums {
 struct s_row {
     double f, c, s, n, dd;
 };
-struct s_comb {
-    double PmM, ZpW, PtmMt, D2, C, MpP2Z;
-};
 template <int KIND>
 __device__ __forceinline__ s_row adj_s_row(const double *__restrict__ U, const double *__restrict__ Y1,
                                            const double *__restrict__ Y2, const double *__restrict__ Yo, long long q,
@@ -148,44 +145,43 @@ __device__ __forceinline__ s_row adj_s_row(const double *__restrict__ U, const d
     w.dd = w.s - w.n;
     return w;
 }
-// terms at row t from the rows t+1 (rh), t (rc), t-1 (rl); zt weighs the Delta terms (MCS:
-// zeta - theta with the reference's sign of the P term, HV: zeta with the textbook sign, CS: 0)
+// Sums of one point from the rows t+1 (rh), t (rc), t-1 (rl); zt weighs the Delta terms (MCS:
+// zeta - theta with the reference's sign of the P term, HV: zeta with the textbook sign, CS: 0).
+// Each combination is formed only where a sum uses it.
 template <int KIND>
-__device__ __forceinline__ s_comb adj_s_comb(const bdesc &d, const s_row &rh, const s_row &rc, const s_row &rl,
-                                             double th, double zt, bool hv)
+__device__ __forceinline__ void adj_s_sum_w(const inst_view<double> &v, const bdesc &d, s_sums &p, const s_row &rh,
+                                            const s_row &rc, const s_row &rl, double th, double zt, bool hv,
+                                            double mu, int t, bool vterms, bool sabr)
 {
-    s_comb cb;
+    double PmM, ZpW, C;
     if constexpr (KIND == 1) {
-        cb.PmM = rh.f - rl.f;
-        cb.ZpW = -rc.f - rc.c;
-        cb.PtmMt = rc.n - rc.s;
-        cb.D2 = rc.s + rc.n - 2.0 * rc.c;
-        cb.C = d.a_gamma * (rl.dd - rh.dd);
-        cb.MpP2Z = rl.f + rh.f - 2.0 * rc.f;
+        PmM = rh.f - rl.f;
+        ZpW = -rc.f - rc.c;
+        C = d.a_gamma * (rl.dd - rh.dd);
     } else {
         const double sp = hv ? 1.0 : -1.0;
-        cb.PmM = th * (rh.f - rl.f) + zt * (sp * rh.c - rl.c);
-        cb.ZpW = -th * rc.f - 2.0 * zt * rc.c;
-        cb.PtmMt = zt * (rc.n - rc.s);
-        cb.D2 = zt * (rc.s + rc.n - 2.0 * rc.c);
-        cb.C = d.a_zeta * d.a_gamma * (rl.dd - rh.dd);
-        cb.MpP2Z = th * (rl.f + rh.f - 2.0 * rc.f) + zt * (rl.c + sp * rh.c - 2.0 * rc.c);
+        PmM = th * (rh.f - rl.f) + zt * (sp * rh.c - rl.c);
+        ZpW = -th * rc.f - 2.0 * zt * rc.c;
+        C = d.a_zeta * d.a_gamma * (rl.dd - rh.dd);
     }
-    return cb;
-}
-__device__ __forceinline__ void adj_s_sum_c(const inst_view<double> &v, s_sums &p, const s_comb &s, double mu, int t,
-                                            bool vterms, bool sabr)
-{
-    p.A += mu * __ldg(v.X(X_HX) + t) * s.PmM;
-    p.B += mu * s.ZpW;
+    p.A += mu * __ldg(v.X(X_HX) + t) * PmM;
+    p.B += mu * ZpW;
     if (vterms) {
-        p.Q += mu * s.PtmMt;
-        p.D += mu * s.D2;
+        const double zf = KIND == 1 ? 1.0 : zt;
+        p.Q += mu * zf * (rc.n - rc.s);
+        p.D += mu * zf * (rc.s + rc.n - 2.0 * rc.c);
     }
-    p.E += mu * __ldg(v.X(X_HC) + t) * s.C;
+    p.E += mu * __ldg(v.X(X_HC) + t) * C;
     if (sabr) {
-        p.Aa += mu * __ldg(v.X(X_HA) + t) * s.MpP2Z;
-        p.Dd += mu * __ldg(v.X(X_HDD) + t) * s.PmM;
+        double MpP2Z;
+        if constexpr (KIND == 1) {
+            MpP2Z = rl.f + rh.f - 2.0 * rc.f;
+        } else {
+            const double sp = hv ? 1.0 : -1.0;
+            MpP2Z = th * (rl.f + rh.f - 2.0 * rc.f) + zt * (rl.c + sp * rh.c - 2.0 * rc.c);
+        }
+        p.Aa += mu * __ldg(v.X(X_HA) + t) * MpP2Z;
+        p.Dd += mu * __ldg(v.X(X_HDD) + t) * PmM;
     }
 }
 __device__ __forceinline__ void adj_s_line(const inst_view<double> &v, const bdesc &d, int j, const s_sums &p,
@@ -261,8 +257,7 @@ __device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d
                     Y1B[o] = mu;
                 }
             }
-            const s_comb cb = adj_s_comb<KIND>(d, rh, rc, rl, th, zt, hv);
-            adj_s_sum_c(v, ps, cb, mu, t, KIND == 1 || zt != 0.0, sabr);
+            adj_s_sum_w<KIND>(v, d, ps, rh, rc, rl, th, zt, hv, mu, t, KIND == 1 || zt != 0.0, sabr);
             la_next = la;
             rh = rc;
             rc = rl;

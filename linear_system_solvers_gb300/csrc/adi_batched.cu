@@ -1013,7 +1013,7 @@ __global__ void __launch_bounds__(1024) k_wadj_s_chunk(const __grid_constant__ b
     acc_load(acc, acc_a, nacc, tid);
     const double *LA = v.S(SL_LA), *IB = v.S(SL_IB);
     s_sums ps = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    // three-row window over the chunk's rows (adj_s_row / adj_s_comb)
+    // three-row window over the chunk's rows (adj_s_row / adj_s_sum_w)
     s_row rh = adj_s_row<KIND>(U, Y1, Y2, Yo, (long long)(t1 + 1) * ny + j, th, hv);
     s_row rc = adj_s_row<KIND>(U, Y1, Y2, Yo, (long long)t1 * ny + j, th, hv);
     for (int t = t1; t >= t0; --t) {
@@ -1034,7 +1034,7 @@ __global__ void __launch_bounds__(1024) k_wadj_s_chunk(const __grid_constant__ b
                 Y1B[o] = mu;
             }
         }
-        adj_s_sum_c(v, ps, adj_s_comb<KIND>(d, rh, rc, rl, th, zt, hv), mu, t, KIND == 1 || zt != 0.0, sabr);
+        adj_s_sum_w<KIND>(v, d, ps, rh, rc, rl, th, zt, hv, mu, t, KIND == 1 || zt != 0.0, sabr);
         rh = rc;
         rc = rl;
     }
