@@ -217,3 +217,25 @@ def test_nonfinite_status(lss, oracle):
         vals, st = b.run_host()
         assert list(st) == [0, 1, 0]
         assert np.isfinite(vals[0]) and np.isfinite(vals[2])
+
+
+@pytest.mark.parametrize("fp", ["f64", "f32"])
+def test_heat1d_long_lines(lss, oracle, fp):
+    # long lines: the prefetch rings run many full blocks and load past the last row of the last
+    # group in the arena; sizes that are not multiples of the ring length
+    qs = [lss.BlackScholesProblem(n=n, nt=6, s_hi=40.0, strike=10.0, nonuniform=True, acc_point=10.0, eval_s=10.0,
+                                  theta_scheme=th) for n, th in ((997, "cn"), (2048, "euler"), (4099, "cn"))]
+    fast = lss.black_scholes_batch(qs, fp, "fast")
+    fast.run()
+    ref = lss.black_scholes_batch(qs, fp, "reference")
+    ref.run()
+    for i, q in enumerate(qs):
+        p = bs_oracle_problem(oracle, q)
+        want = oracle.solve_1d(p, fp)
+        assert np.array_equal(ref.solution(i), want), i
+        want64 = oracle.solve_1d(p, "f64")
+        if fp == "f64":
+            assert rel_err(fast.solution(i), want64) < 1e-10, i
+        else:
+            ok, e_dev, e_ref = fp32_ok(fast.solution(i), want, want64)
+            assert ok, (i, e_dev, e_ref)
