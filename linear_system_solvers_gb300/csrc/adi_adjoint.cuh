@@ -424,8 +424,7 @@ __device__ __forceinline__ void adj_gather(const inst_view<double> &v, const bde
                 if (hv && p >= 1 && p <= nx - 2) Y2B[o] += db; else Y2B[o] = db;
                 val = -db;
             } else {
-                val = dn_p + up_m + mid_c;
-                if (q <= 2) val += adj_b1_terms(v, d, U, LV, acc, tau, p, q);
+                val = dn_p + up_m + mid_c; // the B1^T terms of columns 0..2 follow in adj_b1_pass
             }
             if (p == 0) val += lsum;
             if (p == nx - 1) val += hsum;
@@ -435,6 +434,19 @@ __device__ __forceinline__ void adj_gather(const inst_view<double> &v, const bde
             mid_c = mid_p;
         }
     }
+}
+
+// B1^T terms of columns 0..2 (adj_b1_terms), spread over the CTA's threads by row after the
+// column walk of adj_gather<1> (which would otherwise leave the threads of columns 0..2 walking
+// their columns alone with this extra work, the rest of their warp idle).
+__device__ __forceinline__ void adj_b1_pass(const inst_view<double> &v, const bdesc &d, const double *__restrict__ U,
+                                            const double *__restrict__ LV, double *__restrict__ UB, adj_acc &acc,
+                                            double tau, int l0, int ls)
+{
+    const int nx = v.nx, ny = v.ny;
+    const int qn = ny < 3 ? ny : 3;
+    for (int p = l0; p < nx; p += ls)
+        for (int q = 0; q < qn; ++q) UB[(long long)p * ny + q] += adj_b1_terms(v, d, U, LV, acc, tau, p, q);
 }
 
 // Adjoint of one time step: VB = adjoint of the step output (modified in place), UB receives
@@ -469,6 +481,8 @@ __device__ __forceinline__ void adj_step(const inst_view<double> &v, const bdesc
     adj_s<1>(v, d, U, Y1, Y2, Y1, Y1B, FB, TMP, LS, HS, UB, Y1B, acc, tau, l0, BS);
     __syncthreads();
     adj_gather<1>(v, d, U, FB, LS, HS, LV, UB, Y2B, acc, tau, l0, BS);
+    __syncthreads();
+    adj_b1_pass(v, d, U, LV, UB, acc, tau, l0, BS);
     __syncthreads();
 }
 
