@@ -45,15 +45,16 @@ FP64_INSTR_ADJ = 169.1 - 34.7 * 1.75
 FP64_INSTR_PEAK = 5.98e11
 
 
-def recompute_fraction(problems):
+def recompute_fraction(problems, intervals=None):
     """Grid-point-step weighted fraction of the steps the adjoint recomputes (every checkpoint
-    segment of ceil(sqrt(steps)) steps but the last)."""
+    segment but the last); `intervals`: the checkpoint interval of every instance
+    (lss_adi_batch_checkpoints), default ceil(sqrt(steps))."""
     import math
 
     num = den = 0.0
-    for p in problems:
+    for k, p in enumerate(problems):
         steps = p.nt - 1
-        c = max(1, math.ceil(math.sqrt(steps)))
+        c = int(intervals[k]) if intervals is not None else max(1, math.ceil(math.sqrt(steps)))
         nseg = (steps + c - 1) // c
         w = p.nx * p.ny
         num += w * (nseg - 1) * c
@@ -363,7 +364,8 @@ def main():
         return
     value = gps_all / (t_max * 1e-3)
     bpg = BYTES_PER_GPS_FWD["mcs"] * (1 if mode == 0 else 10.0 / 3.0)
-    fp64_per_gps = FP64_INSTR_FWD if mode == 0 else FP64_INSTR_FWD * (1.0 + recompute_fraction(problems)) + FP64_INSTR_ADJ
+    rf = recompute_fraction(problems, batch.checkpoints()) if mode == 1 else 0.0
+    fp64_per_gps = FP64_INSTR_FWD if mode == 0 else FP64_INSTR_FWD * (1.0 + rf) + FP64_INSTR_ADJ
     peak, peak_kind = measured_peaks()
     achieved = gps * bpg / (ms * 1e-3) / 1e9
     out = {
@@ -386,7 +388,7 @@ def main():
                                        "grid-point-step, times this launch's grid-point-steps", "peak_source": peak_kind,
                      "algorithmic_bytes_per_grid_point_step": bpg,
                      "note": "FP64 pipe (1.196 TFLOP/s measured) binds before HBM on GB300"},
-        "fp64_pipe": {"instructions_per_grid_point_step": fp64_per_gps,
+        "fp64_pipe": {"instructions_per_grid_point_step": fp64_per_gps, "recomputed_fraction": rf,
                       "achieved": gps * fp64_per_gps / (ms * 1e-3), "peak": FP64_INSTR_PEAK,
                       "unit": "FP64 instructions/s", "frac": gps * fp64_per_gps / (ms * 1e-3) / FP64_INSTR_PEAK,
                       "note": "the binding resource of this path; instruction counts from ncu (forward + adjoint: "

@@ -209,8 +209,9 @@ int lss_adi_batch_create(const lss_adi_problem *problems, int count, lss_adi_bat
 /* mode 0 = forward values only, 1 = forward + adjoint (values, the 5 parameter
  * sensitivities and dV/d(initial condition) per instance; FP64, every splitting, Heston and
  * SABR with r = 0).
- * The adjoint keeps a checkpoint every ceil(sqrt(steps)) steps and recomputes each segment
- * once.  Device-resident: inputs were uploaded by batch_create. */
+ * The adjoint keeps a checkpoint every ceil(sqrt(steps)) steps or more (lss_adi_batch_checkpoints)
+ * and recomputes each segment but the last once.  Device-resident: inputs were uploaded by
+ * batch_create. */
 int lss_adi_batch_run(lss_adi_batch *b, int mode, void *stream);
 
 /* Captures lss_adi_batch_run(b, mode) once into a CUDA graph and launches the graph. */
@@ -241,6 +242,12 @@ int lss_adi_batch_autotune(lss_adi_batch *b, int mode, int *threads_per_instance
 
 /* Kernel launches made by the last lss_adi_batch_run / graph launch (own kernels only). */
 int lss_adi_batch_launch_count(const lss_adi_batch *b);
+
+/* Checkpoint interval of every instance (creation order) that the last mode-1 run or autotune
+ * planned: at least ceil(sqrt(steps)); longer where the adjoint workspace (one slice per
+ * resident CTA, up to half of the device memory free when it is planned) holds more stage
+ * values, down to no recomputation at all when one segment covers the whole time loop. */
+int lss_adi_batch_checkpoints(const lss_adi_batch *b, int *intervals);
 
 void lss_adi_batch_destroy(lss_adi_batch *b);
 

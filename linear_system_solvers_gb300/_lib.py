@@ -98,6 +98,7 @@ SIGNATURES = {
     "lss_adi_batch_payoff_gradient": (c_int, [c_void_p, c_int, c_void_p]),
     "lss_adi_batch_autotune": (c_int, [c_void_p, c_int, P(c_int), c_void_p]),
     "lss_adi_batch_launch_count": (c_int, [c_void_p]),
+    "lss_adi_batch_checkpoints": (c_int, [c_void_p, P(c_int)]),
     "lss_adi_batch_destroy": (None, [c_void_p]),
     "lss_tridiag_thomas_lu": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                       c_void_p, c_void_p, c_void_p]),

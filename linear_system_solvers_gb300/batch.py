@@ -113,3 +113,9 @@ class BatchSolver:
 
     def launch_count(self) -> int:
         return int(self.lib.lss_adi_batch_launch_count(self._b))
+
+    def checkpoints(self) -> np.ndarray:
+        """Checkpoint interval of every instance planned by the last adjoint run / autotune."""
+        out = np.zeros(len(self.problems), dtype=np.int32)
+        L.check(self.lib.lss_adi_batch_checkpoints(self._b, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+        return out

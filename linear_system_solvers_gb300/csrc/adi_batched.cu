@@ -1223,7 +1223,9 @@ template <typename T> struct batch_typed {
 
     int create(const lss_adi_problem *ps, int n);
     int prepare_adjoint(cudaStream_t s);
-    int ensure_ws(int bs, bool shrink = false); // shrink: release slices the size `bs` does not use
+    int ensure_ws(int bs, bool shrink = false); // workspace (and checkpoint plan) for CTA size `bs`
+    int plan_checkpoints(int slices);
+    int plan_slices = 0, plan_override = -1;    // what the current plan was made for
     // threads per instance (CTA size) of the persistent kernels, per mode; chosen by autotune()
     int bs_mode[2] = {64, 64};
     template <int BS> int launch_forward(cudaStream_t s);
@@ -1473,25 +1475,68 @@ template <typename T> int batch_typed<T>::prepare_adjoint(cudaStream_t s)
 {
     (void)s;
     if (!adjoint_ok) return set_error(LSS_ADI_EUNSUPPORTED, "batch: " + adjoint_why);
+    return ensure_ws(bs_mode[1]);
+}
+
+// Workspace (doubles) of one CTA slice for an instance checkpointed every c steps: nseg
+// checkpoints, the stage values of one segment (4 arrays per step plus the segment's end), two
+// scratch states, seven adjoint arrays and three line-end vectors.
+static long long adj_ws_need(const bdesc &d, int c)
+{
+    const long long nn = static_cast<long long>(d.nx) * d.ny;
+    const long long nseg = (d.steps + c - 1) / c;
+    return (nseg + 4LL * (c + 1) + 2 + 7) * nn + d.nx + 2LL * d.ny;
+}
+
+// Checkpoint interval of every instance for `slices` CTA slices.  The forward pass keeps the
+// stage values of the last segment, so an instance recomputes all its segments but one: the
+// longer the segments, the less it recomputes (none when one segment holds the whole loop).
+// Each slice gets at least the sqrt(steps) need of the largest instance and, when the device has
+// room, up to half of the free memory over the slices; every instance then takes the longest
+// interval whose workspace fits the slice.  checkpoint_every (ck_override) fixes the interval.
+template <typename T> int batch_typed<T>::plan_checkpoints(int slices)
+{
+    long long base = 0, full = 0;
+    std::vector<int> c0(count);
+    for (int k = 0; k < count; ++k) {
+        const bdesc &d = desc[k];
+        c0[k] = ck_override > 0 ? std::min(ck_override, d.steps)
+                                : std::max(1, static_cast<int>(std::ceil(std::sqrt(static_cast<double>(d.steps)))));
+        base = std::max(base, adj_ws_need(d, c0[k]));
+        full = std::max(full, adj_ws_need(d, d.steps));
+    }
+    long long budget = base;
+    if (ck_override <= 0) {
+        size_t free_b = 0, total_b = 0;
+        LSS_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b), "batch: device memory");
+        const double held = d_ws.p ? static_cast<double>(d_ws.n) * sizeof(double) : 0.0;
+        const long long avail = static_cast<long long>(0.5 * (static_cast<double>(free_b) + held) / sizeof(double) /
+                                                       std::max(1, slices));
+        budget = std::max(base, std::min(full, avail));
+    }
+    bool changed = false;
     long long need = 0;
     for (int k = 0; k < count; ++k) {
         bdesc &d = desc[k];
-        const int c = ck_override > 0 ? std::min(ck_override, d.steps) : d.ck;
+        int c = c0[k];
+        if (ck_override <= 0)
+            for (int cc = d.steps; cc > c0[k]; --cc)
+                if (adj_ws_need(d, cc) <= budget) { c = cc; break; }
         if (c != d.ck) {
             d.ck = c;
-            LSS_CUDA_TRY(cudaMemcpy(d_desc.p + k, &d, sizeof(bdesc), cudaMemcpyHostToDevice), "batch: descriptor");
+            changed = true;
         }
-        const long long nn = static_cast<long long>(d.nx) * d.ny;
-        const long long nseg = (d.steps + c - 1) / c;
-        need = std::max(need, (nseg + 4LL * (c + 1) + 2 + 7) * nn + d.nx + 2LL * d.ny);
+        need = std::max(need, adj_ws_need(d, c));
     }
+    if (changed) LSS_CUDA_TRY(cudaMemcpy(d_desc.p, desc.data(), count * sizeof(bdesc), cudaMemcpyHostToDevice), "batch: descriptors");
     ws_need = (need + 31) / 32 * 32;
-    return ensure_ws(bs_mode[1]);
+    return LSS_ADI_OK;
 }
 
 // Adjoint workspace for every resident CTA of k_batch_fwdadj<bs> (one slice per CTA).
 template <typename T> int batch_typed<T>::ensure_ws(int bs, bool shrink)
 {
+    (void)shrink;
     int per_sm = 0;
     switch (bs) {
     case 32: LSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_fwdadj<32>, 32, 0), "occupancy"); break;
@@ -1500,12 +1545,18 @@ template <typename T> int batch_typed<T>::ensure_ws(int bs, bool shrink)
     default: LSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_fwdadj<64>, 64, 0), "occupancy"); break;
     }
     const int want = std::max(1, std::min(sms * std::max(1, per_sm), count));
-    if (d_ws.p && ws_stride == ws_need && (shrink ? grid_adj == want : grid_adj >= want)) return LSS_ADI_OK;
-    const int slices = (d_ws.p && ws_stride == ws_need && !shrink) ? std::max(want, grid_adj) : want;
-    ws_stride = ws_need;
-    grid_adj = slices;
-    LSS_CUDA_TRY(d_ws.alloc(static_cast<size_t>(ws_stride) * grid_adj), "batch: allocating adjoint workspace");
-    if (graph) { // a captured launch holds the old workspace pointer
+    if (d_ws.p && grid_adj == want && plan_slices == want && plan_override == ck_override) return LSS_ADI_OK;
+    int rc = plan_checkpoints(want);
+    if (rc) return rc;
+    if (!(d_ws.p && ws_stride == ws_need && grid_adj == want)) {
+        ws_stride = ws_need;
+        grid_adj = want;
+        d_ws.release();
+        LSS_CUDA_TRY(d_ws.alloc(static_cast<size_t>(ws_stride) * grid_adj), "batch: allocating adjoint workspace");
+    }
+    plan_slices = want;
+    plan_override = ck_override;
+    if (graph) { // a captured launch holds the old workspace pointer and checkpoint plan
         cudaGraphExecDestroy(graph);
         graph = nullptr;
         graph_mode = -1;
@@ -2310,6 +2361,14 @@ int lss_adi_batch_launch_count(const lss_adi_batch *b)
 {
     if (!b) return 0;
     return static_cast<int>(b->b64 ? b->b64->launches : b->b32->launches);
+}
+
+int lss_adi_batch_checkpoints(const lss_adi_batch *b, int *intervals)
+{
+    if (!b || !intervals) return set_error(LSS_ADI_EINVAL, "lss_adi_batch_checkpoints: null argument");
+    const int count = b->b64 ? b->b64->count : b->b32->count;
+    for (int k = 0; k < count; ++k) intervals[k] = b->b64 ? b->b64->desc[k].ck : b->b32->desc[k].ck;
+    return LSS_ADI_OK;
 }
 
 void lss_adi_batch_destroy(lss_adi_batch *b) { delete b; }

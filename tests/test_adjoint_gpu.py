@@ -163,6 +163,31 @@ def test_batch_mode1_matches_single_instance_and_mode0(lss):
         np.testing.assert_allclose(b.payoff_gradient(k), lam, rtol=1e-13, atol=1e-15)
 
 
+def test_batch_checkpoint_plan(lss):
+    """The batch plans each instance's checkpoint interval from the workspace it can hold: at
+    least ceil(sqrt(steps)); a small batch on a large device keeps every step (one segment,
+    no recomputation).  Results do not depend on the plan."""
+    import math
+
+    from linear_system_solvers_gb300.batch import draw_batch
+
+    probs = draw_batch(6, seed=5)
+    for p in probs:
+        p.nt = 41
+    b = lss.BatchSolver(probs, precision="f64")
+    b.run(1)
+    ck = b.checkpoints()
+    v1, g1, _ = b.results()
+    for k, p in enumerate(probs):
+        steps = p.nt - 1
+        assert math.ceil(math.sqrt(steps)) <= ck[k] <= steps
+    assert (ck == 40).any()
+    for k in (0, 3):
+        val, g, _ = lss.ImplicitHestonSolver(probs[k], precision="f64", arith="fast").adjoint(checkpoint_every=7)
+        assert val == v1[k]
+        np.testing.assert_allclose(g1[k], g, rtol=1e-13, atol=1e-15)
+
+
 def test_batch_gradients_finite_difference_sample(lss):
     """Config-4 style instances (uneven batch, MCS): stable members checked against FD."""
     from linear_system_solvers_gb300.batch import draw_batch
