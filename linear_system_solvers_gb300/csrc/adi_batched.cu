@@ -1223,7 +1223,7 @@ template <typename T> struct batch_typed {
 
     int create(const lss_adi_problem *ps, int n);
     int prepare_adjoint(cudaStream_t s);
-    int ensure_ws(int bs, bool shrink = false); // workspace (and checkpoint plan) for CTA size `bs`
+    int ensure_ws(int bs); // workspace (and checkpoint plan) for CTA size `bs`
     int plan_checkpoints(int slices);
     int plan_slices = 0, plan_override = -1;    // what the current plan was made for
     // threads per instance (CTA size) of the persistent kernels, per mode; chosen by autotune()
@@ -1534,9 +1534,8 @@ template <typename T> int batch_typed<T>::plan_checkpoints(int slices)
 }
 
 // Adjoint workspace for every resident CTA of k_batch_fwdadj<bs> (one slice per CTA).
-template <typename T> int batch_typed<T>::ensure_ws(int bs, bool shrink)
+template <typename T> int batch_typed<T>::ensure_ws(int bs)
 {
-    (void)shrink;
     int per_sm = 0;
     switch (bs) {
     case 32: LSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_fwdadj<32>, 32, 0), "occupancy"); break;
@@ -1667,8 +1666,8 @@ template <typename T> int batch_typed<T>::autotune(int mode, int *chosen, cudaSt
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         bs_mode[m] = best_bs;
-        if (mode == 1) { // the candidates' workspace (one-warp CTAs: the most slices) down to the chosen size's
-            int rc = ensure_ws(best_bs, true);
+        if (mode == 1) { // the workspace and checkpoint plan of the chosen size
+            int rc = ensure_ws(best_bs);
             if (rc) return rc;
         }
     }
