@@ -592,15 +592,8 @@ __global__ void __launch_bounds__(128, 4) k_h1_fast(const h1params<T> p)
     p.status[L.inst] = bad;
 }
 
-// scatter of per-instance contiguous tables into the interleaved group layout
-struct h1scatter {
-    const int *inst_group; // group of instance
-    const int *inst_lane;  // lane of instance
-    const long long *inst_off; // offset of the instance's contiguous rows
-    const long long *row_start; // prefix sums of rows*len per instance (for the flat index)
-    int count;
-};
-
+// scatter of per-instance contiguous tables into the interleaved group layout (the instance of
+// a flat position found by binary search over the instances' offsets)
 // coef (3 rows of n) -> slots 0..2
 template <typename T>
 __global__ void k_h1_scatter_coef(const h1group *groups, const int *ig, const int *il, const long long *off,
@@ -717,7 +710,7 @@ template <typename T> int batch_t<T>::build(std::vector<inst_info> &&inf, std::v
     inst_group.assign(count, 0);
     inst_lane.assign(count, 0);
     long long pt = 0, bnd = 0, src = 0, all = 0;
-    bool any_src = false, keep_all = (options & LSS_HEAT1D_OPT_ALL_STEPS) != 0;
+    const bool keep_all = (options & LSS_HEAT1D_OPT_ALL_STEPS) != 0;
     for (int q = 0; q < count;) {
         const int n = info[order[q]].n;
         h1group G{};
@@ -736,7 +729,6 @@ template <typename T> int batch_t<T>::build(std::vector<inst_info> &&inf, std::v
         bnd += 2LL * steps * LANES;
         G.src = gsrc ? src : -1;
         if (gsrc) src += static_cast<long long>(steps + 1) * n * LANES;
-        any_src |= gsrc != 0;
         G.all = keep_all ? all : -1;
         if (keep_all) all += static_cast<long long>(steps + 1) * n * LANES;
         const int gi = static_cast<int>(groups.size());
@@ -747,7 +739,6 @@ template <typename T> int batch_t<T>::build(std::vector<inst_info> &&inf, std::v
         groups.push_back(G);
         q += l;
     }
-    (void)any_src;
     // lanes and contiguous initial conditions
     lanes.assign(groups.size() * LANES, h1lane{});
     for (auto &L : lanes) L.inst = -1;
@@ -1049,9 +1040,8 @@ static int create_tab(const lss_heat1d_tables *ps, int count, int arith, int opt
         f.t_hi = q.t_hi;
         f.lo_lin = q.lo_kind == LSS_HEAT1D_ROBIN ? static_cast<double>(bnd[1]) : 0.0;
         f.hi_lin = q.hi_kind == LSS_HEAT1D_ROBIN ? static_cast<double>(bnd[3]) : 0.0;
-        f.eval_i = n / 2 - 1 >= 0 ? n / 2 : 0;
+        f.eval_i = n / 2; // value = the solution's middle point (n >= 4: n/2 + 1 < n)
         f.eval_w = 0.0;
-        if (f.eval_i + 1 >= n) f.eval_i = n - 2;
     }
     auto bt = std::make_unique<batch_t<T>>();
     bt->precision = std::is_same<T, double>::value ? LSS_ADI_FP64 : LSS_ADI_FP32;
