@@ -490,10 +490,11 @@ template <typename T, int BS> __global__ void __launch_bounds__(BS, 1024 / BS) k
 // last segment), followed by the adjoint steps of the segment in reverse order.
 // Results: value, the 5 parameter sensitivities, the final surface (state U arena) and
 // dV/d(initial condition) (state V arena).
-// Register budget ~72 per thread (896 / BS CTAs per SM): more resident warps to cover the load
-// latency of the adjoint's workspace traffic beat the spills (+15 % over 128 registers,
-// measured; 64 and 80 registers were slower).
-template <int BS> __global__ void __launch_bounds__(BS, 896 / BS) k_batch_fwdadj(const __grid_constant__ bparams<double> p)
+// Register budget ~80 per thread (768 / BS CTAs per SM).  Measured on the 4096-instance batch
+// with the planned checkpoints (fewer resident CTAs also means more workspace per CTA, so
+// longer checkpoint segments): 1024 / 896 / 768 / 640 / 512 over BS CTAs per SM (64 / 72 / 80 /
+// ~100 / 128 registers) gave 2.28e9 / 2.18e9 / 2.54e9 / 2.54e9 / 2.38e9 grid-point-steps/s.
+template <int BS> __global__ void __launch_bounds__(BS, 768 / BS) k_batch_fwdadj(const __grid_constant__ bparams<double> p)
 {
     __shared__ int s_idx;
     __shared__ int s_bad;
