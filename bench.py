@@ -31,8 +31,9 @@ METRIC = "grid-point-steps/s, batched fwd+adjoint vs plain path, FP64 \u22641e-1
 BYTES_PER_GPS_FWD = {"dr": 40, "cs": 96, "mcs": 96, "hv": 96}  # algorithmic bytes per grid-point-step (FP64)
 # DRAM bytes (read + write) per grid-point-step of the batched kernels from one ncu capture of
 # the 512-instance, 20-step case (--count 512 --max-time-steps 20), scaled to a launch by the
-# grid-point-steps it processes: mode 0 = k_batch_forward, mode 1 = k_batch_fwdadj
-DRAM_BYTES_PER_GPS = {0: 303.0, 1: 1056.0}
+# grid-point-steps it processes: mode 0 = k_batch_forward, mode 1 = k_batch_fwdadj (that capture
+# recomputes nothing: its 20-step loops fit one checkpoint segment)
+DRAM_BYTES_PER_GPS = {0: 303.0, 1: 821.0}
 # FP64 instructions (DFMA + DADD + DMUL, thread level) per grid-point-step from the same capture
 # (smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum), and the FP64 pipe's rate:
 # 1.196 TFLOP/s of DFMA measured on this GPU model = 5.98e11 FP64 instructions/s.
