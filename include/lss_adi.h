@@ -180,7 +180,9 @@ int lss_adi_forward_graph(lss_adi_handle *h, const void *payoff, void *out_surfa
  * dV/d(payoff grid) in dv_dpayoff (Nx*Ny, may be NULL).  FP64, all four splittings, Heston
  * and SABR with r = 0 (the r sensitivity includes the discount factors D(t)).  Instances
  * larger than 256 x 160 points run the adjoint as one kernel per stage over the whole GPU.
- * Checkpoints every `checkpoint_every` steps (0 = ~sqrt(steps)). */
+ * Checkpoints every `checkpoint_every` steps; 0 = planned: instances of up to 256 x 160 points
+ * take the longest interval the workspace allows (at least ceil(sqrt(steps))), larger ones
+ * ceil(sqrt(steps)).  Results do not depend on the interval. */
 int lss_adi_adjoint(lss_adi_handle *h, const void *payoff, double *out_value, double *dv_dparams,
                     void *dv_dpayoff, int checkpoint_every, int flags, void *stream);
 

@@ -1180,7 +1180,7 @@ template <typename T> struct batch_typed {
     // forward + adjoint
     bool adjoint_ok = false;      // FP64, Heston and SABR with r = 0
     std::string adjoint_why;
-    int ck_override = 0;          // checkpoint interval (0 = ceil(sqrt(steps)))
+    int ck_override = 0;          // checkpoint interval (0 = planned by plan_checkpoints)
     int grid_adj = 0;                 // CTAs the workspace has slices for
     long long ws_stride = 0, ws_need = 0;
     dbuf<double> d_grads, d_ws;
