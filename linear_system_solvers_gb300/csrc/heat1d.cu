@@ -38,9 +38,11 @@ namespace heat1d {
 
 constexpr int LANES = 32;
 constexpr int NSLOT = 8;
-constexpr int H1_PF = 8; // prefetch distance (points) of the factorised sweeps
-// elements after the last group: the sweeps may load up to H1_PF + 1 points past a row
-constexpr long long H1_PAD = (H1_PF + 2) * 32;
+// prefetch distance (points) of the factorised sweeps: 8 in FP64, 16 in FP32 (a ring entry is
+// one register there)
+template <typename T> constexpr int h1_pf() { return sizeof(T) == 4 ? 16 : 8; }
+// elements after the last group: the sweeps may load up to the prefetch distance + 1 points past a row
+constexpr long long H1_PAD = (16 + 2) * 32;
 enum { S_A = 0, S_B = 1, S_D = 2, S_M = 3, S_G = 4, S_K = 5, S_U = 6, S_Y = 7 };
 
 // One instance (device).  Solver-type scalars are stored as double (exact).
@@ -887,10 +889,10 @@ template <typename T> int batch_t<T>::run(cudaStream_t s)
     const int blocks = grid_for(static_cast<long long>(groups.size()) * LANES, 128);
     const bool keep = d_all.p != nullptr, src = d_src.p != nullptr;
     if (arith == LSS_ADI_ARITH_FAST) {
-        if (keep && src) k_h1_fast<T, H1_PF, true, true><<<blocks, 128, 0, s>>>(p);
-        else if (keep) k_h1_fast<T, H1_PF, false, true><<<blocks, 128, 0, s>>>(p);
-        else if (src) k_h1_fast<T, H1_PF, true, false><<<blocks, 128, 0, s>>>(p);
-        else k_h1_fast<T, H1_PF, false, false><<<blocks, 128, 0, s>>>(p);
+        if (keep && src) k_h1_fast<T, h1_pf<T>(), true, true><<<blocks, 128, 0, s>>>(p);
+        else if (keep) k_h1_fast<T, h1_pf<T>(), false, true><<<blocks, 128, 0, s>>>(p);
+        else if (src) k_h1_fast<T, h1_pf<T>(), true, false><<<blocks, 128, 0, s>>>(p);
+        else k_h1_fast<T, h1_pf<T>(), false, false><<<blocks, 128, 0, s>>>(p);
     }
     else if (ds)
         k_h1_ref<T, true, 4><<<blocks, 128, 0, s>>>(p);
