@@ -82,3 +82,46 @@ def test_draw_black_scholes_is_seeded(lss):
     b = lss.draw_black_scholes(16, seed=1)
     assert a == b
     assert {q.n for q in lss.draw_black_scholes(200)} <= {128, 256, 384, 512}
+
+
+def test_python_front_end_tables_are_the_reference_tables(lss, oracle):
+    """GeneralHeatEquation1D samples the user's callables as the reference does (grid map,
+    coefficient and boundary transforms, time sequence of the loop): its tables equal the
+    oracle's bit for bit in FP64, so a device run from them is the reference's run."""
+    import math
+
+    from cases_1d import SMALL_1D
+
+    # the reference's Black-Scholes test problem
+    sig, r, K, T = 0.25, 0.2, 10.0, 1.0
+    eq = lss.GeneralHeatEquation1D(
+        a=lambda t, x: 0.5 * sig * sig * x * x, b=lambda t, x: r * x, c=lambda t, x: -r,
+        initial=lambda x: max(0.0, x - K),
+        boundary=(lss.Dirichlet(lambda t: 0.0), lss.Dirichlet(lambda t: 20.0 - K * math.exp(-r * (T - t)))),
+        space=(0.0, 20.0), n=100, time=(0.0, T), nt=100, theta_scheme="cn", forward=False)
+    want = oracle.tables_1d(oracle.Heat1DProblem())
+    got = eq._tables
+    assert np.array_equal(got["coef"], want["coef"])
+    assert np.array_equal(got["initial"], want["init"])
+    assert np.array_equal(got["boundary"], want["bnd"])
+    np.testing.assert_array_equal(eq.grid(), oracle.grid_1d(oracle.Heat1DProblem()))
+    # Neumann / Robin ends, a heat source, a sinh grid, backward stepping
+    for key in ("heat_source_neumann_robin_ds_f64", "advdiff_source_nonuniform_bwd_f64", "heat_robin_robin_cn_f64"):
+        kw, _ = SMALL_1D[key]
+        p = oracle.Heat1DProblem(**kw)
+        kinds = {"dirichlet": lambda v, l: lss.Dirichlet(lambda t: v), "neumann": lambda v, l: lss.Neumann(lambda t: v),
+                 "robin": lambda v, l: lss.Robin(lambda t: l, lambda t: v)}
+        eq = lss.GeneralHeatEquation1D(
+            a=lambda t, x: p.diff, b=lambda t, x: p.conv, c=lambda t, x: p.react,
+            initial=lambda x: p.init0 + p.init1 * x,
+            source=(lambda t, x: p.src0 + p.src1 * x) if p.has_source else None,
+            boundary=(kinds[p.lo_kind](p.lo_value, p.lo_linear), kinds[p.hi_kind](p.hi_value, p.hi_linear)),
+            space=(p.x_lo, p.x_hi), n=p.n, time=(p.t_lo, p.t_hi), nt=p.nt, theta_scheme=p.theta_scheme,
+            forward=p.forward, nonuniform=p.nonuniform, acc_point=p.acc_point, alpha_scale=p.alpha_scale)
+        want = oracle.tables_1d(p)
+        got = eq._tables
+        assert np.array_equal(got["coef"], want["coef"]), key
+        assert np.array_equal(got["initial"], want["init"]), key
+        assert np.array_equal(got["boundary"], want["bnd"]), key
+        if p.has_source:
+            assert np.array_equal(got["source"], want["src"]), key
