@@ -34,8 +34,10 @@ BYTES_PER_GPS_FWD = {"dr": 40, "cs": 96, "mcs": 96, "hv": 96}  # algorithmic byt
 # grid-point-steps it processes: mode 0 = k_batch_forward, mode 1 = k_batch_fwdadj (that capture
 # recomputes nothing: its 20-step loops fit one checkpoint segment)
 DRAM_BYTES_PER_GPS = {0: 303.0, 1: 821.0}
-# FP64 instructions (DFMA + DADD + DMUL, thread level) per grid-point-step from the same capture
-# (smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum), and the FP64 pipe's rate:
+# FP64 instructions (DFMA + DADD + DMUL, thread level) per grid-point-step from an ncu capture of
+# the same 512-instance, 20-step case taken while the checkpoint interval was still
+# ceil(sqrt(steps)) (smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum), and the
+# FP64 pipe's rate:
 # 1.196 TFLOP/s of DFMA measured on this GPU model = 5.98e11 FP64 instructions/s.
 # Forward + adjoint = one forward pass, the recomputation of every checkpoint segment but the
 # last (a fraction rf of the steps, from the workload) and the adjoint steps:
