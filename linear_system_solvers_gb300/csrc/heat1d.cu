@@ -25,6 +25,7 @@
 
 #include "adi_common.hpp"
 #include "adi_device.cuh"
+#include "heat1d_schedule.hpp"
 
 #include <algorithm>
 #include <cmath>
@@ -38,6 +39,7 @@ namespace heat1d {
 
 constexpr int LANES = 32;
 constexpr int NSLOT = 8;
+constexpr int H1_FAST_WARPS = 16; // warps per CTA of the factorised sweep (one CTA per SM)
 // prefetch distance (points) of the factorised sweeps: 8 in FP64, 16 in FP32 (a ring entry is
 // one register there)
 template <typename T> constexpr int h1_pf() { return sizeof(T) == 4 ? 16 : 8; }
@@ -81,6 +83,9 @@ template <typename T> struct h1params {
     const T *init;
     double *values;
     int *status;
+    const int *warp_first; // factorised sweep: the groups of warp w are
+    const int *warp_group; // warp_group[warp_first[w] .. warp_first[w + 1])
+    int nwarps;
 };
 
 __device__ __forceinline__ long long el(int t) { return static_cast<long long>(t) * LANES; }
@@ -450,17 +455,14 @@ template <typename T> __global__ void __launch_bounds__(128) k_h1_setup_fast(con
     L.bh = static_cast<double>(bh);
 }
 
-// Per step: the first solved row, the interior rows in blocks of PF (the loads of point t + PF
-// are issued before point t is computed, from a ring of PF registers per array; loads past the
-// last row stay inside the group's block and are never used), the last solved row, then the
-// back substitution the same way downwards.  SRC: the batch has heat sources; KEEP: every time
-// level is written out.
+// Time loop of group g in one warp.  Per step: the first solved row, the interior rows in
+// blocks of PF (the loads of point t + PF are issued before point t is computed, from a ring of
+// PF registers per array; loads past the last row stay inside the group's block and are never
+// used), the last solved row, then the back substitution the same way downwards.  SRC: the
+// batch has heat sources; KEEP: every time level is written out.
 template <typename T, int PF, bool SRC, bool KEEP>
-__global__ void __launch_bounds__(128, 4) k_h1_fast(const h1params<T> p)
+__device__ __forceinline__ void h1_fast_group(const h1params<T> p, const int g, const int lane)
 {
-    const int g = blockIdx.x * (blockDim.x / LANES) + threadIdx.x / LANES;
-    const int lane = threadIdx.x % LANES;
-    if (g >= p.ngroups) return;
     const h1group G = p.groups[g];
     if (lane >= G.lanes) return;
     const h1lane L = p.lanes[static_cast<long long>(g) * LANES + lane];
@@ -594,6 +596,19 @@ __global__ void __launch_bounds__(128, 4) k_h1_fast(const h1params<T> p)
     p.status[L.inst] = bad;
 }
 
+// One CTA of H1_FAST_WARPS warps per SM (128 registers per thread: the register file holds one
+// CTA); warp w runs the groups warp_group[warp_first[w] .. warp_first[w + 1]) placed by
+// schedule_groups.
+template <typename T, int PF, bool SRC, bool KEEP>
+__global__ void __launch_bounds__(H1_FAST_WARPS * LANES, 1) k_h1_fast(const h1params<T> p)
+{
+    const int w = blockIdx.x * (blockDim.x / LANES) + threadIdx.x / LANES;
+    const int lane = threadIdx.x % LANES;
+    if (w >= p.nwarps) return;
+    const int q1 = p.warp_first[w + 1];
+    for (int q = p.warp_first[w]; q < q1; ++q) h1_fast_group<T, PF, SRC, KEEP>(p, p.warp_group[q], lane);
+}
+
 // scatter of per-instance contiguous tables into the interleaved group layout (the instance of
 // a flat position found by binary search over the instances' offsets)
 // coef (3 rows of n) -> slots 0..2
@@ -672,6 +687,8 @@ template <typename T> struct batch_t : batch_base {
     dbuf<T> d_pt, d_bnd, d_src, d_all, d_init;
     dbuf<double> d_values;
     dbuf<int> d_status;
+    warp_schedule sched;          // placement of the groups for the factorised sweep
+    dbuf<int> d_wfirst, d_wgroup;
     bool ds = false;
 
     h1params<T> params()
@@ -687,6 +704,9 @@ template <typename T> struct batch_t : batch_base {
         p.init = d_init.p;
         p.values = d_values.p;
         p.status = d_status.p;
+        p.warp_first = d_wfirst.p;
+        p.warp_group = d_wgroup.p;
+        p.nwarps = sched.ctas * sched.warps_per_cta;
         return p;
     }
     int build(std::vector<inst_info> &&inf, std::vector<host_tables<T>> &tabs);
@@ -875,6 +895,16 @@ template <typename T> int batch_t<T>::build(std::vector<inst_info> &&inf, std::v
         }
     }
     if (arith == LSS_ADI_ARITH_FAST) {
+        int dev = 0, sms = 0;
+        LSS_CUDA_TRY(cudaGetDevice(&dev), "heat1d: device");
+        LSS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "heat1d: SM count");
+        std::vector<double> work(groups.size());
+        for (size_t g = 0; g < groups.size(); ++g) work[g] = static_cast<double>(groups[g].n) * groups[g].steps;
+        sched = schedule_groups(work, sms, H1_FAST_WARPS);
+        LSS_CUDA_TRY(d_wfirst.alloc(sched.first.size()), "heat1d: allocating the warp schedule");
+        LSS_CUDA_TRY(d_wfirst.upload(sched.first.data(), sched.first.size()), "heat1d: uploading the warp schedule");
+        LSS_CUDA_TRY(d_wgroup.alloc(sched.group.size()), "heat1d: allocating the warp schedule");
+        LSS_CUDA_TRY(d_wgroup.upload(sched.group.data(), sched.group.size()), "heat1d: uploading the warp schedule");
         const h1params<T> p = params();
         k_h1_setup_fast<T><<<grid_for(static_cast<long long>(groups.size()) * LANES, 128), 128>>>(p);
         LSS_CUDA_TRY(cudaGetLastError(), "heat1d: launching the factorisation");
@@ -889,10 +919,11 @@ template <typename T> int batch_t<T>::run(cudaStream_t s)
     const int blocks = grid_for(static_cast<long long>(groups.size()) * LANES, 128);
     const bool keep = d_all.p != nullptr, src = d_src.p != nullptr;
     if (arith == LSS_ADI_ARITH_FAST) {
-        if (keep && src) k_h1_fast<T, h1_pf<T>(), true, true><<<blocks, 128, 0, s>>>(p);
-        else if (keep) k_h1_fast<T, h1_pf<T>(), false, true><<<blocks, 128, 0, s>>>(p);
-        else if (src) k_h1_fast<T, h1_pf<T>(), true, false><<<blocks, 128, 0, s>>>(p);
-        else k_h1_fast<T, h1_pf<T>(), false, false><<<blocks, 128, 0, s>>>(p);
+        const int ctas = sched.ctas, th = H1_FAST_WARPS * LANES;
+        if (keep && src) k_h1_fast<T, h1_pf<T>(), true, true><<<ctas, th, 0, s>>>(p);
+        else if (keep) k_h1_fast<T, h1_pf<T>(), false, true><<<ctas, th, 0, s>>>(p);
+        else if (src) k_h1_fast<T, h1_pf<T>(), true, false><<<ctas, th, 0, s>>>(p);
+        else k_h1_fast<T, h1_pf<T>(), false, false><<<ctas, th, 0, s>>>(p);
     }
     else if (ds)
         k_h1_ref<T, true, 4><<<blocks, 128, 0, s>>>(p);
