@@ -43,6 +43,9 @@ constexpr int H1_FAST_WARPS = 16; // warps per CTA of the factorised sweep (one 
 // prefetch distance (points) of the factorised sweeps: 8 in FP64, 16 in FP32 (a ring entry is
 // one register there)
 template <typename T> constexpr int h1_pf() { return sizeof(T) == 4 ? 16 : 8; }
+// prefetch distance of the back substitution (two arrays: 12 in FP64, the most that fits in 128
+// registers without spilling; 16 in FP32).  At most 16: the loads below row 0 stay in the group.
+template <typename T> __host__ __device__ constexpr int h1_pfb() { return sizeof(T) == 4 ? 16 : 12; }
 // elements after the last group: the sweeps may load up to the prefetch distance + 1 points past a row
 constexpr long long H1_PAD = (16 + 2) * 32;
 enum { S_A = 0, S_B = 1, S_D = 2, S_M = 3, S_G = 4, S_K = 5, S_U = 6, S_Y = 7 };
@@ -89,6 +92,8 @@ template <typename T> struct h1params {
 };
 
 __device__ __forceinline__ long long el(int t) { return static_cast<long long>(t) * LANES; }
+__device__ __forceinline__ double h1_fma(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float h1_fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 
 // ------------------------------------------------------------------------------------------
 // Reference order (bit-identical to the reference's host policies)
@@ -482,6 +487,7 @@ __device__ __forceinline__ void h1_fast_group(const h1params<T> p, const int g, 
     T *ALL = KEEP ? p.all + G.all + lane : nullptr;
     const T th = T(L.theta), omt = T(1) - th, bl = T(L.bl), bh = T(L.bh);
     const T kap = -omt / th; // -1 (Crank-Nicolson) or 0 (Euler), exact
+    const bool cn = kap != T(0);
     const int start = L.start, end = L.end, steps = L.steps;
     const int S = LANES;
 
@@ -508,7 +514,9 @@ __device__ __forceinline__ void h1_fast_group(const h1params<T> p, const int g, 
         Y[start * S] = yp;
         um = uc;
         uc = up;
-        // interior rows start+1 .. end-1
+        // interior rows start+1 .. end-1 as y_t = c_t - M_t y_{t-1}, c_t = WB u_t + WD u_{t+1}
+        // - [CN] M_t u_{t-1} (+ source): c_t does not depend on the recurrence, so the dependent
+        // chain through y is one FMA per point
         T rwb[PF], rwd[PF], rm[PF], rup[PF];
         int t = start + 1;
 #pragma unroll
@@ -528,8 +536,9 @@ __device__ __forceinline__ void h1_fast_group(const h1params<T> p, const int g, 
                 rwd[j] = WD[q];
                 rm[j] = M[q];
                 rup[j] = U[q + S];
-                T y = wb * uc + wd * u1 + m * (kap * um - yp);
-                if (SRC) y += src_term(t + j);
+                T c = h1_fma(-m, cn ? um : T(0), h1_fma(wd, u1, wb * uc));
+                if (SRC) c += src_term(t + j);
+                const T y = h1_fma(-m, yp, c);
                 Y[(t + j) * S] = y;
                 yp = y;
                 um = uc;
@@ -539,8 +548,9 @@ __device__ __forceinline__ void h1_fast_group(const h1params<T> p, const int g, 
 #pragma unroll
         for (int j = 0; j < PF; ++j) {
             if (t + j < end) {
-                T y = rwb[j] * uc + rwd[j] * rup[j] + rm[j] * (kap * um - yp);
-                if (SRC) y += src_term(t + j);
+                T c = h1_fma(-rm[j], cn ? um : T(0), h1_fma(rwd[j], rup[j], rwb[j] * uc));
+                if (SRC) c += src_term(t + j);
+                const T y = h1_fma(-rm[j], yp, c);
                 Y[(t + j) * S] = y;
                 yp = y;
                 um = uc;
@@ -556,20 +566,22 @@ __device__ __forceinline__ void h1_fast_group(const h1params<T> p, const int g, 
             x += src_term(end);
         }
         U[end * S] = x;
-        // back substitution end-1 .. start
-        T ry[PF], rg[PF];
+        // back substitution end-1 .. start (loads down to PFB <= 16 rows below row start - 1 stay
+        // inside the group's block: G and Y have at least 4n >= 16 rows of other slots below them)
+        constexpr int PFB = h1_pfb<T>();
+        T ry[PFB], rg[PFB];
         t = end - 1;
 #pragma unroll
-        for (int j = 0; j < PF; ++j) {
+        for (int j = 0; j < PFB; ++j) {
             const int q = (t - j) * S;
             ry[j] = Y[q];
             rg[j] = GG[q];
         }
-        for (; t - PF >= start - 1; t -= PF) {
+        for (; t - PFB >= start - 1; t -= PFB) {
 #pragma unroll
-            for (int j = 0; j < PF; ++j) {
+            for (int j = 0; j < PFB; ++j) {
                 const T yv = ry[j], gv = rg[j];
-                const int q = (t - j - PF) * S;
+                const int q = (t - j - PFB) * S;
                 ry[j] = Y[q];
                 rg[j] = GG[q];
                 x = yv - gv * x;
@@ -577,7 +589,7 @@ __device__ __forceinline__ void h1_fast_group(const h1params<T> p, const int g, 
             }
         }
 #pragma unroll
-        for (int j = 0; j < PF; ++j) {
+        for (int j = 0; j < PFB; ++j) {
             if (t - j >= start) {
                 x = ry[j] - rg[j] * x;
                 U[(t - j) * S] = x;
