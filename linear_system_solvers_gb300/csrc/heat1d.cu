@@ -39,15 +39,17 @@ namespace heat1d {
 
 constexpr int LANES = 32;
 constexpr int NSLOT = 8;
-constexpr int H1_FAST_WARPS = 16; // warps per CTA of the factorised sweep (one CTA per SM)
-// prefetch distance (points) of the factorised sweeps: 8 in FP64, 16 in FP32 (a ring entry is
-// one register there)
-template <typename T> constexpr int h1_pf() { return sizeof(T) == 4 ? 16 : 8; }
-// prefetch distance of the back substitution (two arrays: 12 in FP64, the most that fits in 128
-// registers without spilling; 16 in FP32).  At most 16: the loads below row 0 stay in the group.
-template <typename T> __host__ __device__ constexpr int h1_pfb() { return sizeof(T) == 4 ? 16 : 12; }
+// Warps per CTA of the factorised sweep, one CTA per SM: 16 in FP32 (at most 128 registers per
+// thread), 8 in FP64, whose 16-point rings take ~200 registers per thread (the deeper ring
+// keeps more loads in flight in each warp, which is what the longest instances, running alone
+// at the end of a batch, are bound by)
+template <typename T> __host__ __device__ constexpr int h1_warps() { return sizeof(T) == 4 ? 16 : 8; }
+// prefetch distance (points) of the forward sweep and of the back substitution.  At most 16:
+// the loads past the last row stay in H1_PAD, those below row 0 in the group's block.
+constexpr int H1_PF = 16;
+constexpr int H1_PFB = 16;
 // elements after the last group: the sweeps may load up to the prefetch distance + 1 points past a row
-constexpr long long H1_PAD = (16 + 2) * 32;
+constexpr long long H1_PAD = (H1_PF + 2) * LANES;
 enum { S_A = 0, S_B = 1, S_D = 2, S_M = 3, S_G = 4, S_K = 5, S_U = 6, S_Y = 7 };
 
 // One instance (device).  Solver-type scalars are stored as double (exact).
@@ -568,7 +570,7 @@ __device__ __forceinline__ void h1_fast_group(const h1params<T> p, const int g, 
         U[end * S] = x;
         // back substitution end-1 .. start (loads down to PFB <= 16 rows below row start - 1 stay
         // inside the group's block: G and Y have at least 4n >= 16 rows of other slots below them)
-        constexpr int PFB = h1_pfb<T>();
+        constexpr int PFB = H1_PFB;
         T ry[PFB], rg[PFB];
         t = end - 1;
 #pragma unroll
@@ -608,11 +610,10 @@ __device__ __forceinline__ void h1_fast_group(const h1params<T> p, const int g, 
     p.status[L.inst] = bad;
 }
 
-// One CTA of H1_FAST_WARPS warps per SM (128 registers per thread: the register file holds one
-// CTA); warp w runs the groups warp_group[warp_first[w] .. warp_first[w + 1]) placed by
+// One CTA of h1_warps<T>() warps per SM (the register file holds one CTA); warp w runs the groups warp_group[warp_first[w] .. warp_first[w + 1]) placed by
 // schedule_groups.
 template <typename T, int PF, bool SRC, bool KEEP>
-__global__ void __launch_bounds__(H1_FAST_WARPS * LANES, 1) k_h1_fast(const h1params<T> p)
+__global__ void __launch_bounds__(h1_warps<T>() * LANES, 1) k_h1_fast(const h1params<T> p)
 {
     const int w = blockIdx.x * (blockDim.x / LANES) + threadIdx.x / LANES;
     const int lane = threadIdx.x % LANES;
@@ -912,7 +913,7 @@ template <typename T> int batch_t<T>::build(std::vector<inst_info> &&inf, std::v
         LSS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "heat1d: SM count");
         std::vector<double> work(groups.size());
         for (size_t g = 0; g < groups.size(); ++g) work[g] = static_cast<double>(groups[g].n) * groups[g].steps;
-        sched = schedule_groups(work, sms, H1_FAST_WARPS);
+        sched = schedule_groups(work, sms, h1_warps<T>());
         LSS_CUDA_TRY(d_wfirst.alloc(sched.first.size()), "heat1d: allocating the warp schedule");
         LSS_CUDA_TRY(d_wfirst.upload(sched.first.data(), sched.first.size()), "heat1d: uploading the warp schedule");
         LSS_CUDA_TRY(d_wgroup.alloc(sched.group.size()), "heat1d: allocating the warp schedule");
@@ -931,11 +932,11 @@ template <typename T> int batch_t<T>::run(cudaStream_t s)
     const int blocks = grid_for(static_cast<long long>(groups.size()) * LANES, 128);
     const bool keep = d_all.p != nullptr, src = d_src.p != nullptr;
     if (arith == LSS_ADI_ARITH_FAST) {
-        const int ctas = sched.ctas, th = H1_FAST_WARPS * LANES;
-        if (keep && src) k_h1_fast<T, h1_pf<T>(), true, true><<<ctas, th, 0, s>>>(p);
-        else if (keep) k_h1_fast<T, h1_pf<T>(), false, true><<<ctas, th, 0, s>>>(p);
-        else if (src) k_h1_fast<T, h1_pf<T>(), true, false><<<ctas, th, 0, s>>>(p);
-        else k_h1_fast<T, h1_pf<T>(), false, false><<<ctas, th, 0, s>>>(p);
+        const int ctas = sched.ctas, th = h1_warps<T>() * LANES;
+        if (keep && src) k_h1_fast<T, H1_PF, true, true><<<ctas, th, 0, s>>>(p);
+        else if (keep) k_h1_fast<T, H1_PF, false, true><<<ctas, th, 0, s>>>(p);
+        else if (src) k_h1_fast<T, H1_PF, true, false><<<ctas, th, 0, s>>>(p);
+        else k_h1_fast<T, H1_PF, false, false><<<ctas, th, 0, s>>>(p);
     }
     else if (ds)
         k_h1_ref<T, true, 4><<<blocks, 128, 0, s>>>(p);

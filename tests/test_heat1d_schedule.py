@@ -42,10 +42,10 @@ def subpartition_loads(work, ctas, wpc, lists):
     return loads
 
 
-def check(work, ctas, wpc, lists, sms=SMS):
+def check(work, ctas, wpc, lists, sms=SMS, warps=WARPS):
     got = sorted(g for gl in lists for g in gl)
     assert got == list(range(len(work)))          # every group exactly once
-    assert 0 <= ctas <= sms and wpc == WARPS
+    assert 0 <= ctas <= sms and wpc == warps
     if len(work):
         loads = subpartition_loads(work, ctas, wpc, lists)
         # greedy placement of the costliest first: no bin exceeds the mean over all bins by more
@@ -75,12 +75,13 @@ def test_schedule_rejects_bad_arguments(schedule_binary):
     assert schedule(schedule_binary, [5.0, 3.0], warps=6)[0] == 0  # not a multiple of 4: nothing placed
 
 
-@pytest.mark.parametrize("count", [1, 7, 152, 153, 608, 2432, 2433, 9000])
-def test_schedule_places_every_group_once_and_balances(schedule_binary, count):
+@pytest.mark.parametrize("warps", [8, 16])  # CTA sizes of the FP64 and FP32 sweeps
+@pytest.mark.parametrize("count", [1, 7, 152, 153, 608, 1216, 2432, 2433, 9000])
+def test_schedule_places_every_group_once_and_balances(schedule_binary, count, warps):
     rng = np.random.default_rng(count)
     work = list(rng.integers(1, 1000, size=count) * rng.choice([128, 256, 384, 512], size=count))
-    ctas, wpc, lists = schedule(schedule_binary, work)
-    check(work, ctas, wpc, lists)
+    ctas, wpc, lists = schedule(schedule_binary, work, warps=warps)
+    check(work, ctas, wpc, lists, warps=warps)
     if count <= SMS:  # few groups: one per SM
         assert ctas == count
         assert all(len([g for w in range(c * wpc, (c + 1) * wpc) for g in lists[w]]) == 1 for c in range(ctas))
@@ -93,15 +94,16 @@ def test_schedule_on_a_small_device(schedule_binary):
     assert ctas == 3
 
 
-def test_schedule_balances_the_black_scholes_batch(schedule_binary):
+@pytest.mark.parametrize("warps", [8, 16])
+def test_schedule_balances_the_black_scholes_batch(schedule_binary, warps):
     """65536 uneven calls (n 128-512, 99-999 steps): placed one group per warp in creation order the
     busiest SM carries ~1.8x the mean; placed by cost every SM sub-partition is within a few per
     cent of the mean."""
     from linear_system_solvers_gb300.heat1d import draw_black_scholes
 
     work = groups_of(draw_black_scholes(65536))
-    ctas, wpc, lists = schedule(schedule_binary, work)
-    check(work, ctas, wpc, lists)
+    ctas, wpc, lists = schedule(schedule_binary, work, warps=warps)
+    check(work, ctas, wpc, lists, warps=warps)
     assert ctas == SMS
     loads = subpartition_loads(work, ctas, wpc, lists)
     mean = sum(work) / (SMS * SUBPARTITIONS)
