@@ -76,6 +76,12 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=32, help="instances timed on the host cores")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip timing the plain per-instance device path")
+    ap.add_argument("--no-parity", action="store_true", help="skip the oracle check of the timed batch's sample")
+    ap.add_argument("--workspace-gb", type=float, default=0.0,
+                    help="cap of the forward + adjoint workspace in GB (0 = the library default, a quarter of the "
+                         "device memory)")
+    ap.add_argument("--checkpoint-every", type=int, default=0,
+                    help="fixed checkpoint interval of the adjoint (0 = planned from the workspace cap)")
     ap.add_argument("--max-time-steps", type=int, default=0,
                     help="cap every instance's time loop (a smaller workload for profiler captures; 0 = no cap)")
     ap.add_argument("--configs", default="", help="comma list of configurations to measure instead of the batched "
@@ -119,7 +125,7 @@ def cpu_sample(problems, m):
 def oracle_kwargs(p):
     import dataclasses
 
-    return {k: v for k, v in dataclasses.asdict(p).items() if k not in ("eval_s", "eval_v", "fp64_tables", "line_per_thread")}
+    return p.pde_fields()
 
 
 def run_cpu_baseline(problems, m, cores, kind, max_steps=None):
@@ -306,6 +312,7 @@ def main():
 
     lib = L.load()
     batch = lss.BatchSolver(problems, precision="f64")
+    batch.set_workspace(args.workspace_gb * 1e9, args.checkpoint_every)
     mode = 0
     if args.mode in ("auto", "fwdadj"):
         try:
@@ -404,6 +411,8 @@ def main():
     }
     if cpu is not None:
         out["cpu_baseline"] = cpu
+    if world == 1 and not args.no_parity:
+        out["parity"] = headline_parity(batch, problems, mode, values, grads)
     if world == 1 and not args.no_plain:
         out["plain_path"] = time_plain_path(lss, problems, stream, value, mode)
     print(json.dumps(out))
@@ -457,7 +466,7 @@ def run_configs(args):
     wanted = [c.strip() for c in args.configs.split(",") if c.strip()]
 
     def oracle_problem(p, nt=None):
-        kw = {k: v for k, v in dataclasses.asdict(p).items() if k not in ("eval_s", "eval_v", "fp64_tables", "line_per_thread")}
+        kw = p.pde_fields()
         if nt is not None:
             kw["nt"] = nt
         return O.Problem(**kw)
@@ -807,6 +816,112 @@ def run_config4(count=1024, sample=16):
           flush=True)
 
 
+def _oracle_surface(kw):
+    """FP64 oracle surface of one instance (the reference's host Thomas-LU path, restated)."""
+    from oracle import oracle as O
+
+    return O.solve(O.Problem(**kw), "f64")
+
+
+def stratified_sample(problems, m=64):
+    """Indices of `m` instances covering every (Nx, Ny) bucket: one per bucket in batch order,
+    then a second per bucket, and so on."""
+    buckets = {}
+    for k, p in enumerate(problems):
+        buckets.setdefault((p.nx, p.ny), []).append(k)
+    keys = sorted(buckets)
+    out, depth = [], 0
+    while len(out) < min(m, len(problems)):
+        added = False
+        for key in keys:
+            if depth < len(buckets[key]) and len(out) < m:
+                out.append(buckets[key][depth])
+                added = True
+        if not added:
+            break
+        depth += 1
+    return sorted(out)
+
+
+def headline_parity(batch, problems, mode, values, grads, m=64, grad_members=4):
+    """Parity of the timed batch: the final surfaces of a stratified sample (every Nx x Ny bucket,
+    full time loops) against the FP64 oracle, relative error with the denominator
+    max(|V|, 1e-3 max|V|) (tolerance 1e-10).  Oracle-unstable members (non-finite or
+    max|V| > 10 S_max: the reference scheme itself diverges) are counted and their error stated
+    apart.  Mode 1: the gradients of the cheapest stable members against Richardson-extrapolated
+    central differences of the oracle (relative bumps 1e-3 / 5e-4, tolerance 1e-6), and the plain
+    central difference at the relative bump 1e-5 for reference."""
+    import numpy as np
+
+    idx = stratified_sample(problems, m)
+    kws = [oracle_kwargs(problems[k]) for k in idx]
+    order = sorted(range(len(idx)), key=lambda q: -kws[q]["nx"] * kws[q]["ny"] * kws[q]["nt"])
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(min(len(idx), os.cpu_count() or 1)) as pool:
+        res = pool.map(_oracle_surface, [kws[q] for q in order], chunksize=1)
+    refs = [None] * len(idx)
+    for q, r in zip(order, res):
+        refs[q] = r
+    stable_err, unstable_err, stable = 0.0, 0.0, []
+    n_unstable = 0
+    for q, k in enumerate(idx):
+        ref = refs[q]
+        got = batch.surface(k)
+        unstable = (not np.all(np.isfinite(ref))) or float(np.abs(ref).max()) > 10 * problems[k].s_hi
+        if unstable:
+            n_unstable += 1
+            if np.all(np.isfinite(ref)):
+                den = np.maximum(np.abs(ref), 1e-3 * np.abs(ref).max())
+                unstable_err = max(unstable_err, float(np.max(np.abs(got - ref) / den)))
+            continue
+        den = np.maximum(np.abs(ref), 1e-3 * np.abs(ref).max())
+        stable_err = max(stable_err, float(np.max(np.abs(got - ref) / den)))
+        stable.append(k)
+    out = {"sample": f"{len(idx)} instances of the timed batch covering all "
+                     f"{len({(p.nx, p.ny) for p in problems})} Nx x Ny buckets, full time loops, FP64 oracle "
+                     f"(C restatement of the reference's host Thomas-LU ADI, pinned bit-exact to the compiled reference)",
+           "stable_instances": len(stable), "max_rel_err_vs_fp64_oracle": stable_err, "tolerance": 1e-10,
+           "oracle_unstable_instances": n_unstable,
+           "max_rel_err_oracle_unstable": unstable_err if n_unstable else None,
+           "rel_err": "max over grid points of |V - V_ref| / max(|V_ref|, 1e-3 max|V_ref|)"}
+    if mode == 1 and stable:
+        names = ("kappa", "theta_v", "sigma", "rho", "rate")
+        members = sorted(stable, key=lambda k: problems[k].nx * problems[k].ny * problems[k].nt)[:grad_members]
+        jobs = []
+        for k in members:
+            p = problems[k]
+            kw = oracle_kwargs(p)
+            for name in names:
+                for rel in (1e-5, 1e-3, 5e-4):
+                    h = rel * abs(kw[name])
+                    for sgn in (+1, -1):
+                        qkw = dict(kw)
+                        qkw[name] = kw[name] + sgn * h
+                        jobs.append((qkw, p.eval_s, p.eval_v))
+        with ctx.Pool(min(len(jobs), os.cpu_count() or 1)) as pool:
+            fdv = pool.map(_oracle_value, jobs, chunksize=1)
+        worst = worst_rich = 0.0
+        q = 0
+        for k in members:
+            kw = oracle_kwargs(problems[k])
+            for c, name in enumerate(names):
+                fd = (fdv[q] - fdv[q + 1]) / (2 * 1e-5 * abs(kw[name]))
+                H = 1e-3 * abs(kw[name])
+                rich = (4.0 * (fdv[q + 4] - fdv[q + 5]) / H - (fdv[q + 2] - fdv[q + 3]) / (2 * H)) / 3.0
+                q += 6
+                den = max(abs(rich), 1e-3 * abs(values[k]))
+                worst = max(worst, abs(grads[k, c] - fd) / den)
+                worst_rich = max(worst_rich, abs(grads[k, c] - rich) / den)
+        out["gradients"] = {"members": [int(k) for k in members],
+                            "max_rel_err_vs_oracle_richardson_fd": worst_rich, "tolerance": 1e-6,
+                            "max_rel_err_vs_oracle_central_fd_1e-5": worst,
+                            "fd": "oracle bump-and-revalue of dV/d(kappa, theta, sigma, rho, r); Richardson from "
+                                  "relative bumps 1e-3 / 5e-4; denominator max(|FD|, 1e-3 |V|)"}
+    out["oracle_seconds"] = time.perf_counter() - t0
+    return out
+
+
 def time_plain_path(lss, problems, stream, batched_value, mode, m=64):
     """The plain device path (one instance per launch sequence, kernel per sweep, FMA
     arithmetic) on a bounded sample of the same batch, for the batched/plain ratio."""
@@ -834,9 +949,13 @@ def time_plain_path(lss, problems, stream, batched_value, mode, m=64):
                   "graph replay), host copies per instance",
            "batched_over_plain": batched_value / plain}
     if mode == 1:
-        # like for like: forward + adjoint through lss_adi_adjoint, one instance per call
+        # like for like: forward + adjoint through lss_adi_adjoint, one instance per call, each on
+        # the whole GPU (kernel per stage, partitioned line solves) rather than one CTA
+        import dataclasses
+
         sub = cpu_sample(problems, 16)
-        adj = [lss.ImplicitHestonSolver(p, precision="f64", arith="fast") for p in sub]
+        adj = [lss.ImplicitHestonSolver(dataclasses.replace(p, wide_adjoint=True), precision="f64", arith="fast")
+               for p in sub]
         gps_a = sum(p.nx * p.ny * (p.nt - 1) for p in sub)
         adj[0].adjoint(stream=sptr)
         torch.cuda.synchronize()
@@ -846,7 +965,9 @@ def time_plain_path(lss, problems, stream, batched_value, mode, m=64):
         torch.cuda.synchronize()
         plain_a = gps_a / (time.perf_counter() - t0)
         out = {"value": plain_a, "unit": "grid-point-steps/s", "sample_instances": len(sub),
-               "how": "lss_adi_adjoint per instance (forward + adjoint, the same work as the batched run)",
+               "how": "lss_adi_adjoint per instance with LSS_ADI_OPT_WIDE_ADJOINT (forward + adjoint, the same "
+                      "work as the batched run, each instance on the whole GPU: kernel per stage, partitioned "
+                      "line solves, autotuned chunks)",
                "batched_over_plain": batched_value / plain_a, "forward_only": out}
     return out
 

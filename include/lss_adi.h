@@ -129,6 +129,10 @@ typedef struct lss_adi_problem {
  *   solves, which cut each line into chunks to occupy the whole GPU on one instance and
  *   differ from it by rounding only. */
 #define LSS_ADI_OPT_LINE_PER_THREAD 4
+/* WIDE_ADJOINT: lss_adi_adjoint runs the forward + adjoint of this instance as one kernel per
+ *   stage over the whole GPU (partitioned line solves unless LINE_PER_THREAD) whatever its
+ *   size, instead of one CTA for instances of up to 256 x 160 points. */
+#define LSS_ADI_OPT_WIDE_ADJOINT 8
 
 /*
  * Tabulated drop-in: time-invariant scheme coefficients already sampled on the grid by
@@ -247,9 +251,22 @@ int lss_adi_batch_launch_count(const lss_adi_batch *b);
 
 /* Checkpoint interval of every instance (creation order) that the last mode-1 run or autotune
  * planned: at least ceil(sqrt(steps)); longer where the adjoint workspace (one slice per
- * resident CTA, up to half of the device memory free when it is planned) holds more stage
+ * resident CTA, within the cap of lss_adi_batch_set_workspace) holds more stage
  * values, down to no recomputation at all when one segment covers the whole time loop. */
 int lss_adi_batch_checkpoints(const lss_adi_batch *b, int *intervals);
+
+/* Bounds the forward + adjoint workspace (checkpoints and the stored stage values of one
+ * checkpoint segment, one slice per resident CTA): max_bytes = 0 restores the default, a
+ * quarter of the device memory (never more than half of what is free when it is planned).
+ * checkpoint_every > 0 fixes every instance's checkpoint interval (capped at its step count);
+ * 0 plans it from the cap.  A cap too small for one slice per resident CTA runs fewer CTAs; one
+ * too small for a single slice makes the next mode-1 run return LSS_ADI_ENOMEM.  Takes effect
+ * at the next mode-1 run or autotune.  Results do not depend on either setting.  No counterpart
+ * in the reference, which has no adjoint. */
+int lss_adi_batch_set_workspace(lss_adi_batch *b, double max_bytes, int checkpoint_every);
+
+/* Bytes of device memory the batch's adjoint workspace holds now (0 before a mode-1 run). */
+double lss_adi_batch_workspace_bytes(const lss_adi_batch *b);
 
 void lss_adi_batch_destroy(lss_adi_batch *b);
 
@@ -272,8 +289,13 @@ int lss_tridiag_thomas_lu(int precision, int n, int lines, const void *lo, const
  * It allocates nothing: its scratch is a fixed 8 MiB array inside the library, held by every
  * GPU that loads the library until the process exits, so n*lines*element size must not exceed
  * 8 MiB (larger requests return LSS_ADI_EINVAL).  The first call on a device looks up the
- * array's device address; make that first call before any stream capture.  All calls on a
- * device share the array: calls whose kernels overlap on the GPU race. */
+ * array's device address and, under CUDA's lazy module loading (the default), that lookup
+ * loads the array and the solver's code onto the device: the first call is the one time it
+ * allocates.  Make a warm-up call with lines = 0 (it only does this set-up; other pointers may
+ * be NULL) on every device before the code that must not allocate, and before any stream
+ * capture -- or run with CUDA_MODULE_LOADING=EAGER.  A cudaDeviceReset between calls is not
+ * supported (the looked-up address belongs to the reset context).  All calls on a device
+ * share the array: calls whose kernels overlap on the GPU race. */
 int lss_tridiag_thomas_lu_noalloc(int precision, int n, int lines, const void *lo, const void *diag,
                                   const void *up, const void *rhs, const void *bnd_lo, const void *bnd_hi,
                                   void *x, void *stream);

@@ -21,6 +21,7 @@ ARITH_FAST, ARITH_REFERENCE = 0, 1
 OPT_FP64_TABLES = 1
 OPT_DOUBLE_SWEEP = 2
 OPT_LINE_PER_THREAD = 4
+OPT_WIDE_ADJOINT = 8
 HESTON, SABR = 0, 1
 SCHEMES = {"dr": 0, "cs": 1, "mcs": 2, "hv": 3, "euler": 4}
 THETAS = {"euler": 0, "theta30": 1, "cn": 2, "theta80": 3}
@@ -99,6 +100,8 @@ SIGNATURES = {
     "lss_adi_batch_autotune": (c_int, [c_void_p, c_int, P(c_int), c_void_p]),
     "lss_adi_batch_launch_count": (c_int, [c_void_p]),
     "lss_adi_batch_checkpoints": (c_int, [c_void_p, P(c_int)]),
+    "lss_adi_batch_set_workspace": (c_int, [c_void_p, c_double, c_int]),
+    "lss_adi_batch_workspace_bytes": (c_double, [c_void_p]),
     "lss_adi_batch_destroy": (None, [c_void_p]),
     "lss_tridiag_thomas_lu": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                       c_void_p, c_void_p, c_void_p]),

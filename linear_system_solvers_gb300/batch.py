@@ -114,6 +114,14 @@ class BatchSolver:
     def launch_count(self) -> int:
         return int(self.lib.lss_adi_batch_launch_count(self._b))
 
+    def set_workspace(self, max_bytes: float = 0.0, checkpoint_every: int = 0):
+        """Cap the forward + adjoint workspace (bytes; 0 = a quarter of the device memory) and
+        optionally fix the checkpoint interval (0 = planned from the cap)."""
+        L.check(self.lib.lss_adi_batch_set_workspace(self._b, float(max_bytes), int(checkpoint_every)))
+
+    def workspace_bytes(self) -> float:
+        return float(self.lib.lss_adi_batch_workspace_bytes(self._b))
+
     def checkpoints(self) -> np.ndarray:
         """Checkpoint interval of every instance planned by the last adjoint run / autotune."""
         out = np.zeros(len(self.problems), dtype=np.int32)

@@ -43,7 +43,8 @@ int validate_problem(const lss_adi_problem &p, std::string &why)
     const double vals[] = {p.kappa, p.theta_v, p.sigma, p.rho, p.rate, p.sabr_beta, p.strike, p.zeta, p.neumann_value, p.acc_point};
     for (double v : vals)
         if (!std::isfinite(v)) return why = "non-finite model parameter", LSS_ADI_EINVAL;
-    if (p.options & ~(LSS_ADI_OPT_FP64_TABLES | LSS_ADI_OPT_DOUBLE_SWEEP | LSS_ADI_OPT_LINE_PER_THREAD))
+    if (p.options & ~(LSS_ADI_OPT_FP64_TABLES | LSS_ADI_OPT_DOUBLE_SWEEP | LSS_ADI_OPT_LINE_PER_THREAD |
+                      LSS_ADI_OPT_WIDE_ADJOINT))
         return why = "unknown option bits", LSS_ADI_EINVAL;
     return LSS_ADI_OK;
 }

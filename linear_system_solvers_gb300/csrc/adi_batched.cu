@@ -1181,6 +1181,7 @@ template <typename T> struct batch_typed {
     bool adjoint_ok = false;      // FP64, Heston and SABR with r = 0
     std::string adjoint_why;
     int ck_override = 0;          // checkpoint interval (0 = planned by plan_checkpoints)
+    double ws_cap = 0.0;          // adjoint workspace cap in bytes (0 = a quarter of the device memory)
     int grid_adj = 0;                 // CTAs the workspace has slices for
     long long ws_stride = 0, ws_need = 0;
     dbuf<double> d_grads, d_ws;
@@ -1227,6 +1228,8 @@ template <typename T> struct batch_typed {
     int ensure_ws(int bs); // workspace (and checkpoint plan) for CTA size `bs`
     int plan_checkpoints(int slices);
     int plan_slices = 0, plan_override = -1;    // what the current plan was made for
+    double plan_cap = -1.0;
+    double ws_bytes_allowed();
     // threads per instance (CTA size) of the persistent kernels, per mode; chosen by autotune()
     int bs_mode[2] = {64, 64};
     template <int BS> int launch_forward(cudaStream_t s);
@@ -1489,6 +1492,21 @@ static long long adj_ws_need(const bdesc &d, int c)
     return (nseg + 4LL * (c + 1) + 2 + 7) * nn + d.nx + 2LL * d.ny;
 }
 
+// Bytes the adjoint workspace may take: the cap set by lss_adi_batch_set_workspace, by default
+// a quarter of the device memory, and never more than half of what is free (counting the
+// workspace already held, which a new plan replaces).
+template <typename T> double batch_typed<T>::ws_bytes_allowed()
+{
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        cudaGetLastError();
+        return ws_cap > 0.0 ? ws_cap : 0.0;
+    }
+    const double held = d_ws.p ? static_cast<double>(d_ws.n) * sizeof(double) : 0.0;
+    const double cap = ws_cap > 0.0 ? ws_cap : 0.25 * static_cast<double>(total_b);
+    return std::min(cap, 0.5 * (static_cast<double>(free_b) + held));
+}
+
 // Checkpoint interval of every instance for `slices` CTA slices.  The forward pass keeps the
 // stage values of the last segment, so an instance recomputes all its segments but one: the
 // longer the segments, the less it recomputes (none when one segment holds the whole loop).
@@ -1508,11 +1526,7 @@ template <typename T> int batch_typed<T>::plan_checkpoints(int slices)
     }
     long long budget = base;
     if (ck_override <= 0) {
-        size_t free_b = 0, total_b = 0;
-        LSS_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b), "batch: device memory");
-        const double held = d_ws.p ? static_cast<double>(d_ws.n) * sizeof(double) : 0.0;
-        const long long avail = static_cast<long long>(0.5 * (static_cast<double>(free_b) + held) / sizeof(double) /
-                                                       std::max(1, slices));
+        const long long avail = static_cast<long long>(ws_bytes_allowed() / sizeof(double) / std::max(1, slices));
         budget = std::max(base, std::min(full, avail));
     }
     bool changed = false;
@@ -1544,8 +1558,26 @@ template <typename T> int batch_typed<T>::ensure_ws(int bs)
     case 256: LSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_fwdadj<256>, 256, 0), "occupancy"); break;
     default: LSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_fwdadj<64>, 64, 0), "occupancy"); break;
     }
-    const int want = std::max(1, std::min(sms * std::max(1, per_sm), count));
-    if (d_ws.p && grid_adj == want && plan_slices == want && plan_override == ck_override) return LSS_ADI_OK;
+    int want = std::max(1, std::min(sms * std::max(1, per_sm), count));
+    {
+        // fewer resident CTAs when the cap does not hold one minimal slice (ceil(sqrt(steps))
+        // checkpoints, or the fixed interval) per CTA
+        long long base = 0;
+        for (int k = 0; k < count; ++k) {
+            const bdesc &d = desc[k];
+            const int c = ck_override > 0 ? std::min(ck_override, d.steps)
+                                          : std::max(1, static_cast<int>(std::ceil(std::sqrt(static_cast<double>(d.steps)))));
+            base = std::max(base, adj_ws_need(d, c));
+        }
+        const double allowed = ws_bytes_allowed();
+        const long long fit = static_cast<long long>(allowed / (static_cast<double>((base + 31) / 32 * 32) * sizeof(double)));
+        if (fit < 1)
+            return set_error(LSS_ADI_ENOMEM, "batch: the adjoint workspace cap (" + std::to_string(allowed / 1e6) +
+                                                 " MB) does not hold the checkpoints of the largest instance");
+        want = static_cast<int>(std::min<long long>(want, fit));
+    }
+    if (d_ws.p && grid_adj == want && plan_slices == want && plan_override == ck_override && plan_cap == ws_cap)
+        return LSS_ADI_OK;
     int rc = plan_checkpoints(want);
     if (rc) return rc;
     if (!(d_ws.p && ws_stride == ws_need && grid_adj == want)) {
@@ -1556,6 +1588,7 @@ template <typename T> int batch_typed<T>::ensure_ws(int bs)
     }
     plan_slices = want;
     plan_override = ck_override;
+    plan_cap = ws_cap;
     if (graph) { // a captured launch holds the old workspace pointer and checkpoint plan
         cudaGraphExecDestroy(graph);
         graph = nullptr;
@@ -2154,7 +2187,7 @@ int adjoint_solver::init(const lss_adi_problem &p)
     int rc = impl->b.create(&q, 1);
     if (rc) return rc;
     // one CTA carries an instance of up to 256 x 160 points well; larger ones run wide
-    impl->wide = p.nx > 256 || static_cast<long long>(p.nx) * p.ny > 40960;
+    impl->wide = p.nx > 256 || static_cast<long long>(p.nx) * p.ny > 40960 || (p.options & LSS_ADI_OPT_WIDE_ADJOINT);
     if (impl->wide && !(p.options & LSS_ADI_OPT_LINE_PER_THREAD)) {
         rc = impl->b.autotune_wide(nullptr);
         if (rc) return rc;
@@ -2193,6 +2226,18 @@ int adjoint_solver::run(const void *payoff, double *out_value, double *dv_dparam
                                      dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s),
                      "lss_adi_adjoint: payoff gradient");
     LSS_CUDA_TRY(cudaStreamSynchronize(s), "lss_adi_adjoint: run");
+    return LSS_ADI_OK;
+}
+
+template <typename T> static int set_workspace_t(batch_typed<T> &bt, double max_bytes, int checkpoint_every)
+{
+    bt.ws_cap = max_bytes;
+    bt.ck_override = checkpoint_every;
+    if (bt.graph && bt.graph_mode == 1) { // a captured launch holds the old workspace and plan
+        cudaGraphExecDestroy(bt.graph);
+        bt.graph = nullptr;
+        bt.graph_mode = -1;
+    }
     return LSS_ADI_OK;
 }
 
@@ -2369,6 +2414,22 @@ int lss_adi_batch_checkpoints(const lss_adi_batch *b, int *intervals)
     const int count = b->b64 ? b->b64->count : b->b32->count;
     for (int k = 0; k < count; ++k) intervals[k] = b->b64 ? b->b64->desc[k].ck : b->b32->desc[k].ck;
     return LSS_ADI_OK;
+}
+
+int lss_adi_batch_set_workspace(lss_adi_batch *b, double max_bytes, int checkpoint_every)
+{
+    clear_error();
+    if (!b) return set_error(LSS_ADI_EINVAL, "lss_adi_batch_set_workspace: null batch");
+    if (!(max_bytes >= 0.0) || checkpoint_every < 0)
+        return set_error(LSS_ADI_EINVAL, "lss_adi_batch_set_workspace: negative cap or interval");
+    return b->b64 ? set_workspace_t(*b->b64, max_bytes, checkpoint_every)
+                  : set_workspace_t(*b->b32, max_bytes, checkpoint_every);
+}
+
+double lss_adi_batch_workspace_bytes(const lss_adi_batch *b)
+{
+    if (!b) return 0.0;
+    return b->b64 ? static_cast<double>(b->b64->d_ws.n) * sizeof(double) : 0.0;
 }
 
 void lss_adi_batch_destroy(lss_adi_batch *b) { delete b; }

@@ -111,7 +111,12 @@ void *g_noalloc_ptr[64] = {};
 }
 
 // Device address of the scratch array for the current device, looked up once per device
-// with that device current (the host-side symbol is not a device address).
+// with that device current (the host-side symbol is not a device address).  Under CUDA's lazy
+// module loading (the default) this first lookup is what loads this file's module -- the 8 MiB
+// array and the kernels' code -- onto the device, so it allocates device memory once; the
+// kernels' code is loaded here too (cudaFuncGetAttributes) so that the first real solve loads
+// nothing.  The cached address belongs to the device's primary context: a cudaDeviceReset
+// between calls invalidates it and is not supported.
 static int noalloc_scratch(void **out)
 {
     int dev = 0;
@@ -121,6 +126,9 @@ static int noalloc_scratch(void **out)
     if (!g_noalloc_ptr[dev]) {
         void *p = nullptr;
         LSS_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch), "lss_tridiag_thomas_lu_noalloc: cudaGetSymbolAddress");
+        cudaFuncAttributes fa;
+        LSS_CUDA_TRY(cudaFuncGetAttributes(&fa, k_thomas_lu_lines<double>), "lss_tridiag_thomas_lu_noalloc: loading the kernel");
+        LSS_CUDA_TRY(cudaFuncGetAttributes(&fa, k_thomas_lu_lines<float>), "lss_tridiag_thomas_lu_noalloc: loading the kernel");
         g_noalloc_ptr[dev] = p;
     }
     *out = g_noalloc_ptr[dev];
@@ -134,6 +142,9 @@ extern "C" int lss_tridiag_thomas_lu_noalloc(int precision, int n, int lines, co
     clear_error();
     if (n < 4) return set_error(LSS_ADI_EINVAL, "lss_tridiag_thomas_lu_noalloc: n must be >= 4");
     if (lines < 0) return set_error(LSS_ADI_EINVAL, "lss_tridiag_thomas_lu_noalloc: lines must be >= 0");
+    void *scratch = nullptr;
+    int rc = noalloc_scratch(&scratch); // lines == 0: the per-device warm-up, nothing else
+    if (rc) return rc;
     if (lines == 0) return LSS_ADI_OK;
     if (!lo || !diag || !up || !rhs || !bnd_lo || !bnd_hi || !x)
         return set_error(LSS_ADI_EINVAL, "lss_tridiag_thomas_lu_noalloc: null pointer");
@@ -145,9 +156,6 @@ extern "C" int lss_tridiag_thomas_lu_noalloc(int precision, int n, int lines, co
         return set_error(LSS_ADI_EINVAL, "lss_tridiag_thomas_lu_noalloc: n*lines*element size " + std::to_string(need) +
                                              " bytes exceeds the fixed scratch of " +
                                              std::to_string(LSS_NOALLOC_SCRATCH_BYTES) + " bytes");
-    void *scratch = nullptr;
-    int rc = noalloc_scratch(&scratch);
-    if (rc) return rc;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int bs = 128;
     if (precision == LSS_ADI_FP64)

@@ -48,10 +48,18 @@ class HestonProblem:
     fp64_tables: bool = False  # FP32 only: tables and index_of remaps built in double
     solver: str = "tlu"  # tridiagonal_method_enum: "tlu" ThomasLUSolver | "ds" DoubleSweepSolver
     line_per_thread: bool = False  # fast single instance: no partitioned line solves (batched-kernel bits)
+    wide_adjoint: bool = False  # adjoint(): whole-GPU kernel-per-stage path at any size (not one CTA)
+
+    # fields that choose how the device runs a problem, not which PDE it is
+    EXECUTION_FIELDS = ("eval_s", "eval_v", "fp64_tables", "line_per_thread", "wide_adjoint")
 
     @property
     def steps(self) -> int:
         return self.nt - 1
+
+    def pde_fields(self) -> dict:
+        """The fields that define the PDE problem (model, grid, scheme, boundaries)."""
+        return {k: v for k, v in dataclasses.asdict(self).items() if k not in self.EXECUTION_FIELDS}
 
     def to_c(self, precision: str = "f64", arith: str = "fast") -> L.LssAdiProblem:
         c = L.LssAdiProblem()
@@ -70,7 +78,8 @@ class HestonProblem:
         if self.solver not in ("tlu", "ds"):
             raise ValueError(f"solver must be 'tlu' or 'ds', not {self.solver!r}")
         c.options = ((L.OPT_FP64_TABLES if self.fp64_tables else 0) | (L.OPT_DOUBLE_SWEEP if self.solver == "ds" else 0)
-                     | (L.OPT_LINE_PER_THREAD if self.line_per_thread else 0))
+                     | (L.OPT_LINE_PER_THREAD if self.line_per_thread else 0)
+                     | (L.OPT_WIDE_ADJOINT if self.wide_adjoint else 0))
         return c
 
 

@@ -2,8 +2,8 @@
 # build_ref.sh -- compile the reference's own host ADI path into oracle/_ref/ref_driver and its
 # 1-D implicit heat path into oracle/_ref/ref_driver_1d.
 #
-# TEST INFRASTRUCTURE ONLY.  Reads the reference sources where they lie (default
-# /root/reference, override with LSS_REFERENCE_DIR), copies the headers it needs into
+# TEST INFRASTRUCTURE ONLY.  Reads the reference sources where they lie ($LSS_REFERENCE_DIR,
+# else a `reference` folder beside the repository's folder), copies the headers it needs into
 # oracle/_ref/src (git-ignored, never committed), applies four mechanical portability
 # patches (MSVC-only std::exception(const char*) ctor; two shadowed template-template
 # parameter names; one decltype on a non-class), and compiles oracle/ref_driver.cu and
@@ -11,7 +11,7 @@
 # thrust device headers.  -ffp-contract=off keeps the reference's two-rounding a*b+c.
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF="${LSS_REFERENCE_DIR:-/root/reference}"
+REF="${LSS_REFERENCE_DIR:-$(cd "$HERE/../.." && pwd)/reference}"
 OUT="$HERE/_ref"
 mkdir -p "$OUT"
 fresh() { [ -x "$OUT/$1" ] && [ "$OUT/$1" -nt "$HERE/$1.cu" ] && [ "$OUT/$1" -nt "$0" ]; }

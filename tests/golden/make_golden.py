@@ -1,5 +1,5 @@
 """Regenerates the committed fixtures of tests/golden/ (run in a checkout that has the
-reference at LSS_REFERENCE_DIR, default /root/reference, and oracle/_ref built):
+reference at LSS_REFERENCE_DIR, default: a `reference` folder beside the repository's folder, and oracle/_ref built):
 
 * reference_outputs.npz: the reference's own golden surfaces outputs/<name>_{double,float}.txt
   (6 significant digits) parsed into arrays x, y, values;
@@ -19,7 +19,7 @@ sys.path.insert(0, HERE)
 from cases import GOLDEN, SMALL  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 
-REF = os.environ.get("LSS_REFERENCE_DIR", "/root/reference")
+REF = os.environ.get("LSS_REFERENCE_DIR") or os.path.join(os.path.dirname(ROOT), "reference")
 
 
 def parse_surface(path):

@@ -1,5 +1,5 @@
 """Regenerates the 1-D fixtures of tests/golden/ (run in a checkout that has the reference at
-LSS_REFERENCE_DIR, default /root/reference, and oracle/_ref/ref_driver_1d built):
+LSS_REFERENCE_DIR, default: a `reference` folder beside the repository's folder, and oracle/_ref/ref_driver_1d built):
 
 * reference_outputs_1d.npz: the reference's own printed 1-D outputs
   outputs/<name>_approx_{double,float}.txt (6 significant digits; lss_print::print,
@@ -20,7 +20,7 @@ sys.path.insert(0, HERE)
 from cases_1d import GOLDEN_1D, SMALL_1D  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 
-REF = os.environ.get("LSS_REFERENCE_DIR", "/root/reference")
+REF = os.environ.get("LSS_REFERENCE_DIR") or os.path.join(os.path.dirname(ROOT), "reference")
 
 
 def parse_curve(path):

@@ -45,7 +45,7 @@ def device_value(lss, p):
 
 
 def oracle_value(oracle, lss, p):
-    kw = {k: v for k, v in dataclasses.asdict(p).items() if k not in ("eval_s", "eval_v", "fp64_tables", "line_per_thread")}
+    kw = p.pde_fields()
     op = oracle.Problem(**kw)
     surf = oracle.solve(op, "f64")
     x, y = oracle.grid(op, "f64")

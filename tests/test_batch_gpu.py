@@ -28,8 +28,7 @@ def mixed_batch(lss, schemes=("dr", "cs", "mcs", "hv"), seed=3, count=12):
 def oracle_of(oracle, p):
     import dataclasses
 
-    return oracle.Problem(**{k: v for k, v in dataclasses.asdict(p).items()
-                             if k not in ("eval_s", "eval_v", "fp64_tables", "line_per_thread")})
+    return oracle.Problem(**p.pde_fields())
 
 
 @pytest.mark.parametrize("graph", [False, True])

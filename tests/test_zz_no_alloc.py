@@ -4,7 +4,9 @@ real-time paths, hosts that reserve all device memory up front).
 
 It is checked through the C-ABI against lss_tridiag_thomas_lu (the allocating entry point,
 same kernel) on two calls in a row -- the second with different inputs, so state left in the
-shared fixed scratch by the first call cannot leak into the result -- and for its size limit.
+shared fixed scratch by the first call cannot leak into the result -- for its size limit, and for
+what it exists for: after the per-device warm-up (a call with lines = 0) a solve leaves the
+device's free memory unchanged.
 This file is collected last so a failure here stops a -x run only after every other test.
 """
 import ctypes
@@ -64,3 +66,32 @@ def test_noalloc_rejects_sizes_beyond_its_scratch(lss):
     rc = lib.lss_tridiag_thomas_lu_noalloc(0, 1025, 1024, 1, 1, 1, 1, 1, 1, 1, None)
     assert rc == L.EINVAL
     assert "exceeds the fixed scratch" in lib.lss_adi_last_error().decode()
+
+
+def test_noalloc_call_after_warm_up_allocates_nothing(lss):
+    import torch
+
+    from linear_system_solvers_gb300 import _lib as L
+
+    lib = L.load()
+    stream = torch.cuda.current_stream().cuda_stream
+    # the per-device warm-up: address lookup and module load, no solve
+    assert lib.lss_tridiag_thomas_lu_noalloc(0, 64, 0, None, None, None, None, None, None, None,
+                                             ctypes.c_void_p(stream)) == L.OK
+    rng = np.random.default_rng(5)
+    arrays = _inputs(rng, 200, 3000, np.float64)
+    dev = [torch.as_tensor(np.ascontiguousarray(a), device="cuda") for a in arrays]
+    x = torch.empty_like(dev[3])
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        rc = lib.lss_tridiag_thomas_lu_noalloc(0, 200, 3000, dev[0].data_ptr(), dev[1].data_ptr(), dev[2].data_ptr(),
+                                               dev[3].data_ptr(), dev[4].data_ptr(), dev[5].data_ptr(), x.data_ptr(),
+                                               ctypes.c_void_p(stream))
+        assert rc == L.OK, lib.lss_adi_last_error()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    rc_ref, ref = _call(lib, "lss_tridiag_thomas_lu", 0, arrays, stream)
+    assert rc_ref == L.OK
+    assert np.array_equal(x.cpu().numpy(), ref)
