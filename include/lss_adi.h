@@ -302,6 +302,12 @@ int lss_tridiag_thomas_lu_noalloc(int precision, int n, int lines, const void *l
 
 /* --- diagnostics ---------------------------------------------------------------------- */
 
+/* Measured FP64 pipe rate of the current device (thread-level DFMA instructions per second):
+ * eight independent DFMA chains per thread on four 256-thread CTAs per SM, best of three timed
+ * launches after a warm-up.  The roofline denominator of the FP64-bound batched kernels.  No
+ * counterpart in the reference. */
+int lss_diag_fp64_rate(double *dfma_per_second, void *stream);
+
 const char *lss_adi_last_error(void);
 int lss_adi_abi_version(void);
 

@@ -107,6 +107,7 @@ SIGNATURES = {
                                       c_void_p, c_void_p, c_void_p]),
     "lss_tridiag_thomas_lu_noalloc": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
                                               c_void_p, c_void_p, c_void_p, c_void_p]),
+    "lss_diag_fp64_rate": (c_int, [P(c_double), c_void_p]),
     "lss_heat1d_batch_create": (c_int, [P(LssHeat1DTables), c_int, c_int, c_int, c_int, P(c_void_p)]),
     "lss_heat1d_batch_create_bs": (c_int, [P(LssHeat1DBs), c_int, c_int, c_int, c_int, P(c_void_p)]),
     "lss_heat1d_batch_run": (c_int, [c_void_p, c_void_p]),

@@ -58,6 +58,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
                      "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math", "-Xptxas", "-O3"]
     if os.environ.get("LSS_PTXAS_VERBOSE"):
         common += ["-Xptxas", "-v"]
+    # extra nvcc flags, e.g. -DLSS_FWDADJ_MIN_CTAS=4 (register budget of the forward + adjoint kernel)
+    common += os.environ.get("LSS_EXTRA_NVCC_FLAGS", "").split()
 
     def compile_one(src: str) -> str:
         obj = os.path.join(OUT, os.path.basename(src)[:-3] + ".o")

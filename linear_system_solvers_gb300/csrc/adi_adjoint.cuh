@@ -111,8 +111,11 @@ __device__ __forceinline__ void adj_v(const inst_view<double> &v, const double *
 
 // Line sums of mu * d(residual)/d(parameter) pieces of an S line (the S-direction factors of the
 // coefficient derivatives applied per point; the v-direction ones once per line, adj_s_line).
+// The stage's constant factors (theta, the Delta weight, gamma, zeta gamma) are taken out of the
+// per-point work: the second S stage keeps the theta parts (A, B, Aa, Dd) and the Delta parts
+// (A2, B2, Aa2, Dd2, Q, D) apart and adj_s_line weighs them once per line.
 struct s_sums {
-    double A, B, Q, D, E, Aa, Dd;
+    double A, A2, B, B2, Q, D, E, Aa, Aa2, Dd, Dd2;
 };
 // Per point, mu times the coefficient derivatives of the stage residual (d/dM, d/dZ, d/dP,
 // d/dM~, d/dW, d/dP~, d/dC) enter the parameter sums only as P - M, Z + W, P~ - M~,
@@ -125,78 +128,102 @@ struct s_sums {
 struct s_row {
     double f, c, s, n, dd;
 };
-template <int KIND>
+template <int KIND, int SCH>
 __device__ __forceinline__ s_row adj_s_row(const double *__restrict__ U, const double *__restrict__ Y1,
                                            const double *__restrict__ Y2, const double *__restrict__ Yo, long long q,
-                                           double th, bool hv)
+                                           double th, double omth)
 {
     s_row w;
     if constexpr (KIND == 1) {
         w.s = U[q - 1];
         w.c = U[q];
         w.n = U[q + 1];
-        w.f = (1.0 - th) * w.c + th * Yo[q];
+        w.f = omth * w.c + th * Yo[q];
     } else {
         w.s = Y2[q - 1] - U[q - 1];
         w.c = Y2[q] - U[q];
         w.n = Y2[q + 1] - U[q + 1];
-        w.f = hv ? (Yo[q] - Y1[q] - w.c) : (Yo[q] - U[q]);
+        w.f = SCH == LSS_ADI_HUNDSDORFER_VERWER ? (Yo[q] - Y1[q] - w.c) : (Yo[q] - U[q]);
     }
     w.dd = w.s - w.n;
     return w;
 }
-// Sums of one point from the rows t+1 (rh), t (rc), t-1 (rl); zt weighs the Delta terms (MCS:
-// zeta - theta with the reference's sign of the P term, HV: zeta with the textbook sign, CS: 0).
-// Each combination is formed only where a sum uses it.
-template <int KIND>
-__device__ __forceinline__ void adj_s_sum_w(const inst_view<double> &v, const bdesc &d, s_sums &p, const s_row &rh,
-                                            const s_row &rc, const s_row &rl, double th, double zt, bool hv,
-                                            double mu, int t, bool vterms, bool sabr)
+// Weight of the Delta = Y2 - U terms of the second S stage: zeta - theta for MCS (with the
+// reference's sign of the P term), zeta for HV (textbook sign), none for CS.
+template <int SCH> __device__ __forceinline__ double delta_weight(const bdesc &d)
 {
-    double PmM, ZpW, C;
-    if constexpr (KIND == 1) {
-        PmM = rh.f - rl.f;
-        ZpW = -rc.f - rc.c;
-        C = d.a_gamma * (rl.dd - rh.dd);
-    } else {
-        const double sp = hv ? 1.0 : -1.0;
-        PmM = th * (rh.f - rl.f) + zt * (sp * rh.c - rl.c);
-        ZpW = -th * rc.f - 2.0 * zt * rc.c;
-        C = d.a_zeta * d.a_gamma * (rl.dd - rh.dd);
+    return SCH == LSS_ADI_MODIFIED_CRAIG_SNEYD ? d.a_zeta - d.a_theta
+                                               : SCH == LSS_ADI_HUNDSDORFER_VERWER ? d.a_zeta : 0.0;
+}
+// Sums of one point from the rows t+1 (rh), t (rc), t-1 (rl); muX = mu (S/A)(t), muC = mu times
+// the S factor of c^ (the same table for Heston).
+template <int KIND, int SCH>
+__device__ __forceinline__ void adj_s_point(const inst_view<double> &v, s_sums &p, const s_row &rh, const s_row &rc,
+                                            const s_row &rl, double mu, double muX, double muC, int t, bool sabr)
+{
+    constexpr bool xt = KIND == 2 && (SCH == LSS_ADI_MODIFIED_CRAIG_SNEYD || SCH == LSS_ADI_HUNDSDORFER_VERWER);
+    constexpr double sp = SCH == LSS_ADI_HUNDSDORFER_VERWER ? 1.0 : -1.0;
+    const double PmM = rh.f - rl.f;
+    p.A += muX * PmM;
+    if constexpr (KIND == 1)
+        p.B -= mu * (rc.f + rc.c);
+    else
+        p.B -= mu * rc.f;
+    p.E += muC * (rl.dd - rh.dd);
+    if constexpr (KIND == 1 || xt) {
+        p.Q -= mu * rc.dd;
+        p.D += mu * (rc.s + rc.n - 2.0 * rc.c);
     }
-    p.A += mu * __ldg(v.X(X_HX) + t) * PmM;
-    p.B += mu * ZpW;
-    if (vterms) {
-        const double zf = KIND == 1 ? 1.0 : zt;
-        p.Q += mu * zf * (rc.n - rc.s);
-        p.D += mu * zf * (rc.s + rc.n - 2.0 * rc.c);
+    double PmM2 = 0.0;
+    if constexpr (xt) {
+        PmM2 = sp * rh.c - rl.c;
+        p.A2 += muX * PmM2;
+        p.B2 -= mu * rc.c;
     }
-    p.E += mu * __ldg(v.X(X_HC) + t) * C;
     if (sabr) {
-        double MpP2Z;
-        if constexpr (KIND == 1) {
-            MpP2Z = rl.f + rh.f - 2.0 * rc.f;
-        } else {
-            const double sp = hv ? 1.0 : -1.0;
-            MpP2Z = th * (rl.f + rh.f - 2.0 * rc.f) + zt * (rl.c + sp * rh.c - 2.0 * rc.c);
+        const double ha = mu * __ldg(v.X(X_HA) + t), hd = mu * __ldg(v.X(X_HDD) + t);
+        p.Aa += ha * (rl.f + rh.f - 2.0 * rc.f);
+        p.Dd += hd * PmM;
+        if constexpr (xt) {
+            p.Aa2 += ha * (rl.c + sp * rh.c - 2.0 * rc.c);
+            p.Dd2 += hd * PmM2;
         }
-        p.Aa += mu * __ldg(v.X(X_HA) + t) * MpP2Z;
-        p.Dd += mu * __ldg(v.X(X_HDD) + t) * PmM;
     }
 }
+// The line's sums, weighed by the stage's constants and the v-direction factors of the line.
+template <int KIND, int SCH>
 __device__ __forceinline__ void adj_s_line(const inst_view<double> &v, const bdesc &d, int j, const s_sums &p,
                                            double tau, bool sabr, adj_acc &acc)
 {
+    double A, B, Q, D, E, Aa, Dd;
+    if constexpr (KIND == 1) {
+        A = p.A;
+        B = p.B;
+        Q = p.Q;
+        D = p.D;
+        E = d.a_gamma * p.E;
+        Aa = p.Aa;
+        Dd = p.Dd;
+    } else {
+        const double th = d.a_theta, zt = delta_weight<SCH>(d);
+        A = th * p.A + zt * p.A2;
+        B = th * p.B + 2.0 * zt * p.B2;
+        Q = zt * p.Q;
+        D = zt * p.D;
+        E = d.a_zeta * d.a_gamma * p.E;
+        Aa = th * p.Aa + zt * p.Aa2;
+        Dd = th * p.Dd + zt * p.Dd2;
+    }
     const double ek = __ldg(v.Yv(Y_EK) + j), et = __ldg(v.Yv(Y_ET) + j), es = __ldg(v.Yv(Y_ES) + j);
     const double bs = __ldg(v.Yv(Y_BS) + j), hy = __ldg(v.Yv(Y_HY) + j);
-    acc.s[0] += d.a_delta * p.A + d.a_halfk * p.B;
+    acc.s[0] += d.a_delta * A + d.a_halfk * B;
     if (sabr) // D(t) terms of a^, d^ and c^
         acc.s[0] += tau * d.a_omb *
-                    (__ldg(v.Yv(Y_HV2) + j) * (2.0 * d.a_delta * p.Dd - 2.0 * d.a_alphat * p.Aa) - d.a_rho * d.a_sigma * hy * p.E);
-    acc.s[1] += d.a_ni * ek * p.Q;
-    acc.s[2] += d.a_ni * et * p.Q;
-    acc.s[3] += d.a_ni * es * p.Q + d.a_betat * bs * p.D + d.a_rho * hy * p.E;
-    acc.s[4] += d.a_sigma * hy * p.E;
+                    (__ldg(v.Yv(Y_HV2) + j) * (2.0 * d.a_delta * Dd - 2.0 * d.a_alphat * Aa) - d.a_rho * d.a_sigma * hy * E);
+    acc.s[1] += d.a_ni * ek * Q;
+    acc.s[2] += d.a_ni * et * Q;
+    acc.s[3] += d.a_ni * es * Q + d.a_betat * bs * D + d.a_rho * hy * E;
+    acc.s[4] += d.a_sigma * hy * E;
 }
 
 // S-line stage adjoint.  KIND 1: S1 (explicit operator on U, output Y1).  KIND 2: second S
@@ -204,7 +231,7 @@ __device__ __forceinline__ void adj_s_line(const inst_view<double> &v, const bde
 // right-hand-side adjoint w; LS/HS the lo/hi adjoints of the line.  The along-line terms of
 // the second stage act on U for CS/MCS and on Y1 for HV, whose right-hand side is
 // (I - theta k A1) Y1 + (zeta k A - theta k A1)(Y2 - U) (hundsdorfer_verwer_method.hpp:128-194).
-template <int KIND>
+template <int KIND, int SCH>
 __device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d, const double *__restrict__ U,
                                       const double *__restrict__ Y1, const double *__restrict__ Y2,
                                       const double *__restrict__ Yo, const double *__restrict__ XB,
@@ -212,12 +239,10 @@ __device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d
                                       double *__restrict__ HS, double *__restrict__ UB, double *__restrict__ Y1B,
                                       adj_acc &acc, double tau, int l0, int ls)
 {
+    constexpr bool hv = SCH == LSS_ADI_HUNDSDORFER_VERWER;
     const int nx = v.nx, ny = v.ny, e = nx - 2;
     const bool sabr = d.model == LSS_ADI_SABR;
-    const double th = d.a_theta;
-    const bool hv = d.scheme == LSS_ADI_HUNDSDORFER_VERWER;
-    // weight of the extra Delta = Y2 - U terms: zeta - theta (MCS), zeta (HV), none (CS)
-    const double zt = (d.scheme == LSS_ADI_MODIFIED_CRAIG_SNEYD) ? (d.a_zeta - th) : hv ? d.a_zeta : 0.0;
+    const double th = d.a_theta, omth = 1.0 - d.a_theta;
     for (int j = 1 + l0; j <= ny - 2; j += ls) {
         double z = 0.0;
 #pragma unroll 4
@@ -229,9 +254,9 @@ __device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d
         }
         double w = 0.0, la_next = 0.0, w_e = 0.0;
         double acc_t1 = 0.0, acc_t = 0.0;
-        s_sums ps = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        s_sums ps = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
         // three-row window along the line (rows t+1, t, t-1; one new row per point)
-        auto load_row = [&](int r) -> s_row { return adj_s_row<KIND>(U, Y1, Y2, Yo, (long long)r * ny + j, th, hv); };
+        auto load_row = [&](int r) -> s_row { return adj_s_row<KIND, SCH>(U, Y1, Y2, Yo, (long long)r * ny + j, th, omth); };
         s_row rh = load_row(e + 1), rc = load_row(e);
 #pragma unroll 2
         for (int t = e; t >= 1; --t) {
@@ -241,8 +266,7 @@ __device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d
             if (t == e) w_e = w;
             FB[o] = w;
             const double la = __ldg(v.S(SL_LA) + o);
-            const double ib = __ldg(v.S(SL_IB) + o);
-            const double mu = ib * w;
+            const double mu = __ldg(v.S(SL_IB) + o) * w;
             if constexpr (KIND == 2) {
                 // along-line terms of the second S stage: la A(t-1) + sc A(t) + se A(t+1) (+ ib Y1(t)),
                 // A = U for CS/MCS, A = Y1 for HV (its rows are written once here: no accumulation)
@@ -250,20 +274,22 @@ __device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d
                 const double fin = acc_t1 + se * w;
                 acc_t1 = acc_t + sc * w;
                 acc_t = la * w;
-                if (hv) {
+                if constexpr (hv) {
                     Y1B[o + ny] = fin;
                 } else {
                     UB[o + ny] += fin;
                     Y1B[o] = mu;
                 }
             }
-            adj_s_sum_w<KIND>(v, d, ps, rh, rc, rl, th, zt, hv, mu, t, KIND == 1 || zt != 0.0, sabr);
+            const double muX = mu * __ldg(v.X(X_HX) + t);
+            const double muC = sabr ? mu * __ldg(v.X(X_HC) + t) : muX;
+            adj_s_point<KIND, SCH>(v, ps, rh, rc, rl, mu, muX, muC, t, sabr);
             la_next = la;
             rh = rc;
             rc = rl;
         }
         if constexpr (KIND == 2) {
-            if (hv) {
+            if constexpr (hv) {
                 Y1B[(long long)ny + j] = acc_t1;
                 Y1B[j] = acc_t;
             } else {
@@ -273,7 +299,7 @@ __device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d
         }
         LS[j] = -la_next * w + XB[j];
         HS[j] = -__ldg(v.Yv(Y_CHS) + j) * w_e + XB[(long long)(nx - 1) * ny + j];
-        adj_s_line(v, d, j, ps, tau, sabr, acc);
+        adj_s_line<KIND, SCH>(v, d, j, ps, tau, sabr, acc);
     }
 }
 
@@ -367,13 +393,14 @@ __device__ __forceinline__ void adj_line_ends(const inst_view<double> &v, const 
 // Gather pass over columns q (thread per column), walking down the column with a window of three
 // rows.  The transposed stencil at (p, q) is  down(p+1) + up(p-1) + mid(p)  where each row r
 // contributes, from FB and the weight tables at columns q-1, q, q+1 of that row,
-//   KIND 1:  down = WW F + g+ - g-,  up = WE F - g+ + g-,  mid = WS(q+1) F(q+1) + WN(q-1) F(q-1) + WC F
-//            with g+- = WG(q+-1) F(q+-1)   (mixed term of the explicit operator);
-//   KIND 2:  the same with S2MZ for WG and, for MCS/HV, X1 / X3 / X2, X4, X5 for WW / WE / WC, WS, WN.
+//   KIND 1:  down = WW F + g,  up = WE F - g,  mid = WS(q+1) F(q+1) + WN(q-1) F(q-1) + WC F
+//            with g = WG(q+1) F(q+1) - WG(q-1) F(q-1)   (mixed term of the explicit operator);
+//   KIND 2:  the same with S2MZ for WG and, for MCS/HV, X1 / X3 / X2, X4, X5 for WW / WE / WC, WS,
+//            WN; for CS only the mixed term: down = g, up = -g, mid = 0.
 // FB and the tables are zero on the boundary rows and columns of an instance (never written), so
 // only the rows and columns outside the instance need guards.  Each row's table and FB values are
 // loaded once instead of once per neighbour.
-template <int KIND>
+template <int KIND, int SCH>
 __device__ __forceinline__ void adj_gather(const inst_view<double> &v, const bdesc &d, const double *__restrict__ U,
                                            const double *__restrict__ FB, const double *__restrict__ LS,
                                            const double *__restrict__ HS, const double *__restrict__ LV,
@@ -381,8 +408,8 @@ __device__ __forceinline__ void adj_gather(const inst_view<double> &v, const bde
                                            int l0, int ls)
 {
     const int nx = v.nx, ny = v.ny;
-    const bool xterms = KIND == 2 && d.scheme != LSS_ADI_CRAIG_SNEYD;
-    const bool hv = d.scheme == LSS_ADI_HUNDSDORFER_VERWER;
+    constexpr bool xterms = KIND == 1 || SCH != LSS_ADI_CRAIG_SNEYD;
+    constexpr bool hv = SCH == LSS_ADI_HUNDSDORFER_VERWER;
     const double *WG = v.S(KIND == 1 ? SL_WG : SL_S2MZ);
     const double *WD = v.S(KIND == 1 ? SL_WW : SL_X1), *WU = v.S(KIND == 1 ? SL_WE : SL_X3);
     const double *WM = v.S(KIND == 1 ? SL_WC : SL_X2), *WR = v.S(KIND == 1 ? SL_WS : SL_X4);
@@ -391,6 +418,7 @@ __device__ __forceinline__ void adj_gather(const inst_view<double> &v, const bde
         double lsum, hsum;
         adj_line_ends(v, LS, HS, q, lsum, hsum);
         const bool ql = q >= 1, qr = q + 1 <= ny - 1;
+        // row r: its down term dn (used at row r-1), up term (used at row r+1) and mid (row r)
         auto row = [&](int r, double &dn, double &up, double &mid) {
             if (r < 0 || r > nx - 1) {
                 dn = up = mid = 0.0;
@@ -398,14 +426,15 @@ __device__ __forceinline__ void adj_gather(const inst_view<double> &v, const bde
             }
             const long long o = (long long)r * ny + q;
             const double f0 = FB[o], fm = ql ? FB[o - 1] : 0.0, fp = qr ? FB[o + 1] : 0.0;
-            const double gp = qr ? __ldg(WG + o + 1) * fp : 0.0, gm = ql ? __ldg(WG + o - 1) * fm : 0.0;
-            if (KIND == 1 || xterms) {
-                dn = __ldg(WD + o) * f0 + gp - gm;
-                up = __ldg(WU + o) * f0 - gp + gm;
+            const double gm = ql ? __ldg(WG + o - 1) * fm : 0.0;
+            const double g = qr ? fma(__ldg(WG + o + 1), fp, -gm) : -gm;
+            if constexpr (xterms) {
+                dn = fma(__ldg(WD + o), f0, g);
+                up = fma(__ldg(WU + o), f0, -g);
                 mid = (qr ? __ldg(WR + o + 1) * fp : 0.0) + (ql ? __ldg(WL + o - 1) * fm : 0.0) + __ldg(WM + o) * f0;
             } else {
-                dn = gp - gm;
-                up = gm - gp;
+                dn = g;
+                up = -g;
                 mid = 0.0;
             }
         };
@@ -419,7 +448,7 @@ __device__ __forceinline__ void adj_gather(const inst_view<double> &v, const bde
             const long long o = (long long)p * ny + q;
             double val;
             if constexpr (KIND == 2) {
-                const double db = dn_p + up_m + mid_c;
+                const double db = xterms ? dn_p + up_m + mid_c : dn_p + up_m;
                 // HV: rows 1..nx-2 already hold the last v stage's adjoint of its input Y2
                 if (hv && p >= 1 && p <= nx - 2) Y2B[o] += db; else Y2B[o] = db;
                 val = -db;
@@ -449,40 +478,40 @@ __device__ __forceinline__ void adj_b1_pass(const inst_view<double> &v, const bd
         for (int q = 0; q < qn; ++q) UB[(long long)p * ny + q] += adj_b1_terms(v, d, U, LV, acc, tau, p, q);
 }
 
-// Adjoint of one time step: VB = adjoint of the step output (modified in place), UB receives
-// the adjoint of the step input.  U/Y1/Y2/Y3/Vo: the step's input, stage outputs and output.
-template <int BS>
+// Adjoint of one time step of scheme SCH: VB = adjoint of the step output (modified in place),
+// UB receives the adjoint of the step input.  U/Y1/Y2/Y3/Vo: the step's input, stage outputs and
+// output.  Work split over the threads of group g, group barriers between the stages.
+template <int SCH>
 __device__ __forceinline__ void adj_step(const inst_view<double> &v, const bdesc &d, const double *U, const double *Y1,
                                          const double *Y2, const double *Y3, const double *Vo, double *VB, double *UB,
                                          double *Y1B, double *Y2B, double *Y3B, double *FB, double *TMP, double *LV,
-                                         double *LS, double *HS, adj_acc &acc, double tau)
+                                         double *LS, double *HS, adj_acc &acc, double tau, const grp &g)
 {
-    const int l0 = threadIdx.x;
-    const bool hv = d.scheme == LSS_ADI_HUNDSDORFER_VERWER;
-    adj_b2(v, VB, UB, hv, l0, BS);
-    __syncthreads();
-    if (d.scheme == LSS_ADI_DOUGLAS_RACHFORD) {
-        adj_v<true>(v, U, Vo, VB, UB, Y1B, TMP, LV, acc, l0, BS);
-        __syncthreads();
+    const int l0 = g.t, ls = g.n;
+    constexpr bool hv = SCH == LSS_ADI_HUNDSDORFER_VERWER;
+    adj_b2(v, VB, UB, hv, l0, ls);
+    g.sync();
+    if constexpr (SCH == LSS_ADI_DOUGLAS_RACHFORD) {
+        adj_v<true>(v, U, Vo, VB, UB, Y1B, TMP, LV, acc, l0, ls);
+        g.sync();
     } else {
         // last v stage: in = U (CS/MCS) or Y2 (HV)
-        if (hv)
-            adj_v<true>(v, Y2, Vo, VB, Y2B, Y3B, TMP, LV, acc, l0, BS);
+        if constexpr (hv)
+            adj_v<true>(v, Y2, Vo, VB, Y2B, Y3B, TMP, LV, acc, l0, ls);
         else
-            adj_v<true>(v, U, Vo, VB, UB, Y3B, TMP, LV, acc, l0, BS);
-        __syncthreads();
-        adj_s<2>(v, d, U, Y1, Y2, Y3, Y3B, FB, TMP, LS, HS, UB, Y1B, acc, tau, l0, BS);
-        __syncthreads();
-        adj_gather<2>(v, d, U, FB, LS, HS, LV, UB, Y2B, acc, tau, l0, BS);
-        __syncthreads();
-        adj_v<false>(v, U, Y2, Y2B, UB, Y1B, TMP, LV, acc, l0, BS);
-        __syncthreads();
+            adj_v<true>(v, U, Vo, VB, UB, Y3B, TMP, LV, acc, l0, ls);
+        g.sync();
+        adj_s<2, SCH>(v, d, U, Y1, Y2, Y3, Y3B, FB, TMP, LS, HS, UB, Y1B, acc, tau, l0, ls);
+        g.sync();
+        adj_gather<2, SCH>(v, d, U, FB, LS, HS, LV, UB, Y2B, acc, tau, l0, ls);
+        g.sync();
+        adj_v<false>(v, U, Y2, Y2B, UB, Y1B, TMP, LV, acc, l0, ls);
+        g.sync();
     }
-    adj_s<1>(v, d, U, Y1, Y2, Y1, Y1B, FB, TMP, LS, HS, UB, Y1B, acc, tau, l0, BS);
-    __syncthreads();
-    adj_gather<1>(v, d, U, FB, LS, HS, LV, UB, Y2B, acc, tau, l0, BS);
-    __syncthreads();
-    adj_b1_pass(v, d, U, LV, UB, acc, tau, l0, BS);
-    __syncthreads();
+    adj_s<1, SCH>(v, d, U, Y1, Y2, Y1, Y1B, FB, TMP, LS, HS, UB, Y1B, acc, tau, l0, ls);
+    g.sync();
+    adj_gather<1, SCH>(v, d, U, FB, LS, HS, LV, UB, Y2B, acc, tau, l0, ls);
+    g.sync();
+    adj_b1_pass(v, d, U, LV, UB, acc, tau, l0, ls);
+    g.sync();
 }
-

@@ -53,12 +53,21 @@ struct bdesc {
     double a_alphat, a_omb, a_tau0, a_dtau;
 };
 
+// Instances are split into classes by the number of warps that work on one of them (1..4 for
+// the persistent kernels: about one thread per S line).  Class c's instances are
+// order[cls_start[c] .. cls_start[c] + cls_count[c]), longest first, pulled through counter[c].
+constexpr int MAX_GROUP_WARPS = 4;
+
 template <typename T> struct bparams {
     const bdesc *desc;
     const int *order;
     int count;
-    int *counter;
+    int *counter;                     // one work counter per class (index 1..4)
+    int cls_start[MAX_GROUP_WARPS + 1], cls_count[MAX_GROUP_WARPS + 1];
+    long long cls_need[MAX_GROUP_WARPS + 1]; // largest adjoint workspace (doubles) of a class's instances
+    const int *layout;                // per CTA: sizes of its warp groups, one hex digit each, lowest first
     T *U, *V, *Y1, *Y2, *Y3;          // state arenas (sum nx*ny each)
+    T *B0;                            // nx arena: the explicit v = v_lo boundary column of a step
     const T *S[SL_COUNT];             // S-direction tables
     const T *Vt[VL_COUNT];            // v-direction tables
     const T *X[X_COUNT];              // nx arenas
@@ -69,10 +78,69 @@ template <typename T> struct bparams {
     int *final_in_v;                  // count: 1 if the final surface is in V
     // forward + adjoint (mode 1, FP64 only)
     double *grads;                    // 5 * count: d value / d(kappa, theta, sigma, rho, r)
-    double *ws;                       // per-CTA adjoint workspace
-    long long ws_stride;              // doubles per CTA
+    double *ws;                       // adjoint workspace: a slice of ws_per_warp doubles per warp
+    long long ws_per_warp;            // a group of w warps owns w consecutive slices
     const T *payoff;                  // sum nx*ny initial conditions
 };
+
+// The warps of one CTA that work on one instance together, synchronised by their own named
+// barrier (a one-warp group by __syncwarp), so that the groups of a CTA run independently.
+struct grp {
+    int t;      // thread index in the group
+    int n;      // threads in the group (a multiple of 32)
+    int gi;     // group index in the CTA (barrier 1 + gi)
+    int warp0;  // first warp of the group in the CTA
+    __device__ __forceinline__ void sync() const
+    {
+        // constant barrier ids: a run-time id makes the compiler reserve all 16 of the CTA's
+        // named barriers, which would cap the CTAs per SM at 4
+        if (n == 32) {
+            __syncwarp();
+        } else {
+            switch (gi) {
+            case 0: __barrier_sync_count(1, n); break;
+            case 1: __barrier_sync_count(2, n); break;
+            case 2: __barrier_sync_count(3, n); break;
+            default: __barrier_sync_count(4, n); break;
+            }
+        }
+    }
+};
+
+// This thread's group from the CTA's layout word (group sizes in warps, one hex digit each).
+__device__ __forceinline__ grp make_grp(int layout)
+{
+    const int w = threadIdx.x >> 5;
+    int first = 0, gi = 0, size = layout & 15;
+    while (size > 0 && w >= first + size) {
+        first += size;
+        layout >>= 4;
+        size = layout & 15;
+        ++gi;
+    }
+    grp g;
+    g.gi = gi;
+    g.warp0 = first;
+    g.n = 32 * (size > 0 ? size : 1);
+    g.t = threadIdx.x - 32 * first;
+    return g;
+}
+
+// Next instance for a group whose home class is `cls` (updated in place as classes run dry):
+// its own class first, then the classes of fewer warps per instance; with max_need >= 0 only
+// classes whose instances' workspace fits max_need doubles.  Called by the group's thread 0.
+template <typename T>
+__device__ __forceinline__ int next_instance(const bparams<T> &p, int &cls, long long max_need)
+{
+    while (cls >= 1) {
+        if (p.cls_count[cls] > 0 && (max_need < 0 || p.cls_need[cls] <= max_need)) {
+            const int q = atomicAdd(p.counter + cls, 1);
+            if (q < p.cls_count[cls]) return p.order[p.cls_start[cls] + q];
+        }
+        --cls;
+    }
+    return -1;
+}
 
 // ------------------------------------------------------------------------------------------
 // set-up: factorise the S-lines and v-lines of every instance once (double arithmetic)
@@ -246,28 +314,30 @@ template <typename T> __device__ __forceinline__ void b2_stage(const inst_view<T
     }
 }
 
-// S-line sweeps.  KIND 1: explicit operator on U (Y1).  KIND 2: second S stage of
-// CS/MCS/HV on U, Y1, Y2 (scheme chooses the weights).  Thread per line j; every access
-// of a warp is one coalesced row segment.
+// S-line sweeps.  KIND 1: explicit operator on U (Y1).  KIND 2: second S stage of CS/MCS/HV
+// (scheme SCH) on U, Y1, Y2.  Thread per line j; every access of a warp is one coalesced row
+// segment.  The mixed difference (x(t-1,j-1) - x(t-1,j+1)) - (x(t+1,j-1) - x(t+1,j+1)) is formed
+// from a rolling window of the per-row differences x(r,j-1) - x(r,j+1): one subtraction per row.
 //
 // s_line_fwd: right-hand side and forward recurrence y_t = f_t - la_t y_{t-1} of line j over
 // rows t0..t1, starting from y = y_{t0-1}; writes y_t into Y and returns y_{t1}.
-template <typename T, int KIND>
-__device__ __forceinline__ T s_line_fwd(const inst_view<T> &v, int scheme, const T *__restrict__ U,
-                                        const T *__restrict__ Y1, const T *__restrict__ Y2, T *__restrict__ Y, int j,
-                                        int t0, int t1, T y, T hi)
+template <typename T, int KIND, int SCH>
+__device__ __forceinline__ T s_line_fwd(const inst_view<T> &v, const T *__restrict__ U, const T *__restrict__ Y1,
+                                        const T *__restrict__ Y2, T *__restrict__ Y, int j, int t0, int t1, T y, T hi)
 {
     const int ny = v.ny, e = v.e_s;
     const long long b = (long long)(t0 - 1) * ny + j;
     if constexpr (KIND == 1) {
-        // sliding 3x3 window of U
-        T u0m = U[b - 1], u0c = U[b], u0p = U[b + 1];
-        T u1m = U[b + ny - 1], u1c = U[b + ny], u1p = U[b + ny + 1];
+        // centre column of U (rows t-1, t, t+1), its side columns at row t, per-row differences
+        T u0c = U[b], u1c = U[b + ny];
+        T u1m = U[b + ny - 1], u1p = U[b + ny + 1];
+        T q0 = U[b - 1] - U[b + 1], q1 = u1m - u1p;
 #pragma unroll 4
         for (int t = t0; t <= t1; ++t) {
             const long long o = (long long)t * ny + j;
             const T u2m = U[o + ny - 1], u2c = U[o + ny], u2p = U[o + ny + 1];
-            const T mix = (u0m - u0p) + (u2p - u2m);
+            const T q2 = u2m - u2p;
+            const T mix = q0 - q2;
             T f = ldg(v.S(SL_WG) + o) * mix;
             f += ldg(v.S(SL_WW) + o) * u0c;
             f += ldg(v.S(SL_WS) + o) * u1m;
@@ -277,26 +347,32 @@ __device__ __forceinline__ T s_line_fwd(const inst_view<T> &v, int scheme, const
             y = f - ldg(v.S(SL_LA) + o) * y;
             if (t == e) y -= ldg(v.Yv(Y_CHS) + j) * hi;
             Y[o] = y;
-            u0m = u1m; u0c = u1c; u0p = u1p;
-            u1m = u2m; u1c = u2c; u1p = u2p;
+            u0c = u1c; u1c = u2c;
+            u1m = u2m; u1p = u2p;
+            q0 = q1; q1 = q2;
         }
     } else {
-        // windows: U centre column, Y1 centre column, Delta = Y2 - U 3x3
+        constexpr bool xt = SCH == LSS_ADI_MODIFIED_CRAIG_SNEYD || SCH == LSS_ADI_HUNDSDORFER_VERWER;
+        constexpr bool hv = SCH == LSS_ADI_HUNDSDORFER_VERWER;
+        // windows: U centre column, Y1 centre column, Delta = Y2 - U (centre column and, at row t,
+        // its side columns), per-row differences of Delta
         T uc0 = U[b], uc1 = U[b + ny];
         T y10 = Y1[b], y11 = Y1[b + ny];
-        T d0m = Y2[b - 1] - U[b - 1], d0c = Y2[b] - uc0, d0p = Y2[b + 1] - U[b + 1];
-        T d1m = Y2[b + ny - 1] - U[b + ny - 1], d1c = Y2[b + ny] - uc1, d1p = Y2[b + ny + 1] - U[b + ny + 1];
+        T d0c = Y2[b] - uc0, d1c = Y2[b + ny] - uc1;
+        T d1m = Y2[b + ny - 1] - U[b + ny - 1], d1p = Y2[b + ny + 1] - U[b + ny + 1];
+        T q0 = (Y2[b - 1] - U[b - 1]) - (Y2[b + 1] - U[b + 1]), q1 = d1m - d1p;
 #pragma unroll 4
         for (int t = t0; t <= t1; ++t) {
             const long long o = (long long)t * ny + j;
             const T uc2 = U[o + ny];
-            const T y12 = Y1[o + ny];
             const T d2m = Y2[o + ny - 1] - U[o + ny - 1];
-            const T d2c = Y2[o + ny] - uc2;
             const T d2p = Y2[o + ny + 1] - U[o + ny + 1];
-            const T mix = (d0m - d0p) + (d2p - d2m);
-            T f;
-            if (scheme == LSS_ADI_HUNDSDORFER_VERWER) {
+            const T q2 = d2m - d2p;
+            const T mix = q0 - q2;
+            T f, y12 = T(0), d2c = T(0);
+            if constexpr (hv || KIND == 2) y12 = Y1[o + ny];
+            if constexpr (xt) d2c = Y2[o + ny] - uc2;
+            if constexpr (hv) {
                 f = ldg(v.S(SL_LA) + o) * y10;
                 f += ldg(v.S(SL_S2SC) + o) * y11;
                 f += ldg(v.S(SL_S2SE) + o) * y12;
@@ -312,7 +388,7 @@ __device__ __forceinline__ T s_line_fwd(const inst_view<T> &v, int scheme, const
                 f += ldg(v.S(SL_S2SE) + o) * uc2;
                 f += ldg(v.S(SL_S2IB) + o) * y11;
                 f += ldg(v.S(SL_S2MZ) + o) * mix;
-                if (scheme == LSS_ADI_MODIFIED_CRAIG_SNEYD) {
+                if constexpr (xt) {
                     f += ldg(v.S(SL_X1) + o) * d0c;
                     f += ldg(v.S(SL_X2) + o) * d1c;
                     f += ldg(v.S(SL_X3) + o) * d2c;
@@ -325,23 +401,23 @@ __device__ __forceinline__ T s_line_fwd(const inst_view<T> &v, int scheme, const
             Y[o] = y;
             uc0 = uc1; uc1 = uc2;
             y10 = y11; y11 = y12;
-            d0m = d1m; d0c = d1c; d0p = d1p;
-            d1m = d2m; d1c = d2c; d1p = d2p;
+            d0c = d1c; d1c = d2c;
+            d1m = d2m; d1p = d2p;
+            q0 = q1; q1 = q2;
         }
     }
     return y;
 }
 
-template <typename T, int KIND>
-__device__ __forceinline__ void s_stage(const inst_view<T> &v, int scheme, const T *__restrict__ U,
-                                        const T *__restrict__ Y1, const T *__restrict__ Y2, T *__restrict__ Y, int l0,
-                                        int ls)
+template <typename T, int KIND, int SCH>
+__device__ __forceinline__ void s_stage(const inst_view<T> &v, const T *__restrict__ U, const T *__restrict__ Y1,
+                                        const T *__restrict__ Y2, T *__restrict__ Y, int l0, int ls)
 {
     const int nx = v.nx, ny = v.ny, e = v.e_s;
     for (int j = 1 + l0; j <= ny - 2; j += ls) {
         const int jj = ldg(v.jmap() + j);
         const T lo = U[jj], hi = U[(long long)(nx - 1) * ny + jj];
-        T x = s_line_fwd<T, KIND>(v, scheme, U, Y1, Y2, Y, j, 1, e, lo, hi);
+        T x = s_line_fwd<T, KIND, SCH>(v, U, Y1, Y2, Y, j, 1, e, lo, hi);
 #pragma unroll 4
         for (int t = e - 1; t >= 1; --t) {
             const long long o = (long long)t * ny + j;
@@ -350,6 +426,17 @@ __device__ __forceinline__ void s_stage(const inst_view<T> &v, int scheme, const
         }
         Y[j] = lo;
         Y[(long long)(nx - 1) * ny + j] = hi;
+    }
+}
+
+// The scheme as a template argument: calls f(std::integral_constant<int, SCH>{}).
+template <typename F> __device__ __forceinline__ void with_scheme(int scheme, F &&f)
+{
+    switch (scheme) {
+    case LSS_ADI_DOUGLAS_RACHFORD: f(std::integral_constant<int, LSS_ADI_DOUGLAS_RACHFORD>{}); break;
+    case LSS_ADI_CRAIG_SNEYD: f(std::integral_constant<int, LSS_ADI_CRAIG_SNEYD>{}); break;
+    case LSS_ADI_MODIFIED_CRAIG_SNEYD: f(std::integral_constant<int, LSS_ADI_MODIFIED_CRAIG_SNEYD>{}); break;
+    default: f(std::integral_constant<int, LSS_ADI_HUNDSDORFER_VERWER>{}); break;
     }
 }
 
@@ -413,107 +500,114 @@ template <typename T> __device__ __forceinline__ inst_view<T> make_view(const bp
     return v;
 }
 
-// One time step U -> Vn with stage outputs in Y1, Y2, Y3; ends with a CTA barrier.
-template <typename T, int BS>
-__device__ __forceinline__ void fwd_step(const inst_view<T> &v, int scheme, const T *U, T *Y1, T *Y2, T *Y3, T *Vn,
-                                         T *sb0, double bnc)
+// One time step U -> Vn of scheme SCH with stage outputs in Y1, Y2, Y3; ends with a group barrier.
+template <typename T, int SCH>
+__device__ __forceinline__ void fwd_step(const inst_view<T> &v, const T *U, T *Y1, T *Y2, T *Y3, T *Vn, T *sb0,
+                                         double bnc, const grp &g)
 {
-    const int l0 = threadIdx.x;
-    b1_stage<T>(v, U, sb0, bnc, l0, BS);
-    s_stage<T, 1>(v, scheme, U, nullptr, nullptr, Y1, l0, BS);
-    __syncthreads();
-    if (scheme == LSS_ADI_DOUGLAS_RACHFORD) {
-        v_stage<T>(v, U, Y1, sb0, Vn, l0, BS);
+    const int l0 = g.t, ls = g.n;
+    b1_stage<T>(v, U, sb0, bnc, l0, ls);
+    s_stage<T, 1, SCH>(v, U, nullptr, nullptr, Y1, l0, ls);
+    g.sync();
+    if constexpr (SCH == LSS_ADI_DOUGLAS_RACHFORD) {
+        v_stage<T>(v, U, Y1, sb0, Vn, l0, ls);
     } else {
-        v_stage<T>(v, U, Y1, sb0, Y2, l0, BS);
-        __syncthreads();
-        s_stage<T, 2>(v, scheme, U, Y1, Y2, Y3, l0, BS);
-        __syncthreads();
-        if (scheme == LSS_ADI_HUNDSDORFER_VERWER)
-            v_stage<T>(v, Y2, Y3, sb0, Vn, l0, BS);
+        v_stage<T>(v, U, Y1, sb0, Y2, l0, ls);
+        g.sync();
+        s_stage<T, 2, SCH>(v, U, Y1, Y2, Y3, l0, ls);
+        g.sync();
+        if constexpr (SCH == LSS_ADI_HUNDSDORFER_VERWER)
+            v_stage<T>(v, Y2, Y3, sb0, Vn, l0, ls);
         else
-            v_stage<T>(v, U, Y3, sb0, Vn, l0, BS);
+            v_stage<T>(v, U, Y3, sb0, Vn, l0, ls);
     }
-    __syncthreads();
-    b2_stage<T>(v, Vn, l0, BS);
-    __syncthreads();
+    g.sync();
+    b2_stage<T>(v, Vn, l0, ls);
+    g.sync();
 }
 
-// Register budget: 64 per thread (1024 / BS resident threads' worth of CTAs per SM).  The time
-// loop waits on streamed table loads; twice the resident warps of the unconstrained build
-// (96 registers) outweigh the few spills (+18 % on the 4096-instance batch, measured).
-template <typename T, int BS> __global__ void __launch_bounds__(BS, 1024 / BS) k_batch_forward(const __grid_constant__ bparams<T> p)
+// Persistent forward kernel of the instances of scheme SCH: CTAs of 4 warps split into groups
+// (the layout word of the CTA), each group pulling instances of its class (warps per instance)
+// from the class counter.  Register budget 64 per thread (8 CTAs per SM).
+constexpr int BATCH_CTA = 32 * MAX_GROUP_WARPS;
+
+template <typename T, int SCH>
+__global__ void __launch_bounds__(BATCH_CTA, 8) k_batch_forward(const __grid_constant__ bparams<T> p)
 {
-    __shared__ int s_idx;
-    __shared__ int s_bad;
-    __shared__ T sb0[256];
+    __shared__ int s_idx[MAX_GROUP_WARPS];
+    __shared__ int s_bad[MAX_GROUP_WARPS];
+    const grp g = make_grp(p.layout[blockIdx.x]);
+    int cls = g.n / 32;
     while (true) {
-        if (threadIdx.x == 0) s_idx = atomicAdd(p.counter, 1);
-        __syncthreads();
-        const int k = s_idx;
-        __syncthreads();
-        if (k >= p.count) break;
-        const int inst = p.order[k];
+        if (g.t == 0) s_idx[g.gi] = next_instance(p, cls, -1);
+        g.sync();
+        const int inst = s_idx[g.gi];
+        g.sync();
+        if (inst < 0) break;
         const bdesc d = p.desc[inst];
         const inst_view<T> v = make_view(p, d);
         T *U = p.U + d.o2, *Vn = p.V + d.o2, *Y1 = p.Y1 + d.o2, *Y2 = p.Y2 + d.o2, *Y3 = p.Y3 + d.o2;
+        T *sb0 = p.B0 + d.ox;
         for (int step = 0; step < d.steps; ++step) {
-            fwd_step<T, BS>(v, d.scheme, U, Y1, Y2, Y3, Vn, sb0, d.bnc);
+            fwd_step<T, SCH>(v, U, Y1, Y2, Y3, Vn, sb0, d.bnc, g);
             T *tmp = U;
             U = Vn;
             Vn = tmp;
         }
         // value at (eval_s, eval_v) and a finiteness check of the final surface
-        if (threadIdx.x == 0) s_bad = 0;
-        __syncthreads();
+        if (g.t == 0) s_bad[g.gi] = 0;
+        g.sync();
         const long long n = (long long)d.nx * d.ny;
         int bad = 0;
-        for (long long q = threadIdx.x; q < n; q += BS) bad |= !isfinite(static_cast<double>(U[q]));
-        if (bad) atomicOr(&s_bad, 1);
-        __syncthreads();
-        if (threadIdx.x == 0) {
+        for (long long q = g.t; q < n; q += g.n) bad |= !isfinite(static_cast<double>(U[q]));
+        if (bad) atomicOr(&s_bad[g.gi], 1);
+        g.sync();
+        if (g.t == 0) {
             const long long o = (long long)d.i0 * d.ny + d.j0;
             p.values[inst] = d.w00 * static_cast<double>(U[o]) + d.w10 * static_cast<double>(U[o + d.ny]) +
                              d.w01 * static_cast<double>(U[o + 1]) + d.w11 * static_cast<double>(U[o + d.ny + 1]);
-            p.status[inst] = s_bad;
+            p.status[inst] = s_bad[g.gi];
             p.final_in_v[inst] = d.steps & 1;
         }
-        __syncthreads();
+        g.sync();
     }
 }
 
 #include "adi_adjoint.cuh"
 
-// Forward + adjoint of each instance by one CTA: forward pass keeping a checkpoint every
+// Forward + adjoint of each instance of scheme SCH by one warp group: forward pass keeping a checkpoint every
 // d.ck steps (and the stage values of every step of the last segment), then per segment (last
 // first) a forward recomputation that keeps the stage values of every step (not needed for the
 // last segment), followed by the adjoint steps of the segment in reverse order.
 // Results: value, the 5 parameter sensitivities, the final surface (state U arena) and
-// dV/d(initial condition) (state V arena).
-// Register budget ~80 per thread (768 / BS CTAs per SM).  Measured on the 4096-instance batch
-// with the planned checkpoints (fewer resident CTAs also means more workspace per CTA, so
-// longer checkpoint segments): 1024 / 896 / 768 / 640 / 512 over BS CTAs per SM (64 / 72 / 80 /
-// ~100 / 128 registers) gave 2.28e9 / 2.18e9 / 2.54e9 / 2.54e9 / 2.38e9 grid-point-steps/s.
-template <int BS> __global__ void __launch_bounds__(BS, 768 / BS) k_batch_fwdadj(const __grid_constant__ bparams<double> p)
+// dV/d(initial condition) (state V arena).  A group of w warps works in w consecutive workspace
+// slices.  Register budget ~80 per thread (6 CTAs of 4 warps per SM).
+#ifndef LSS_FWDADJ_MIN_CTAS
+#define LSS_FWDADJ_MIN_CTAS 6
+#endif
+template <int SCH>
+__global__ void __launch_bounds__(BATCH_CTA, LSS_FWDADJ_MIN_CTAS) k_batch_fwdadj(const __grid_constant__ bparams<double> p)
 {
-    __shared__ int s_idx;
-    __shared__ int s_bad;
-    __shared__ double sb0[256];
-    __shared__ double red[5][BS];
-    double *ws = p.ws + (long long)blockIdx.x * p.ws_stride;
+    __shared__ int s_idx[MAX_GROUP_WARPS];
+    __shared__ int s_bad[MAX_GROUP_WARPS];
+    __shared__ double red[MAX_GROUP_WARPS][5];
+    const grp g = make_grp(p.layout[blockIdx.x]);
+    const int gw = g.n / 32;
+    double *ws = p.ws + (long long)(blockIdx.x * MAX_GROUP_WARPS + g.warp0) * p.ws_per_warp;
+    int cls = gw;
     while (true) {
-        if (threadIdx.x == 0) s_idx = atomicAdd(p.counter, 1);
-        __syncthreads();
-        const int k = s_idx;
-        __syncthreads();
-        if (k >= p.count) break;
-        const int inst = p.order[k];
+        if (g.t == 0) s_idx[g.gi] = next_instance(p, cls, gw * p.ws_per_warp);
+        g.sync();
+        const int inst = s_idx[g.gi];
+        g.sync();
+        if (inst < 0) break;
         const bdesc d = p.desc[inst];
         const inst_view<double> v = make_view(p, d);
         const int nx = d.nx, ny = d.ny;
         const long long n = (long long)nx * ny;
         const int c = d.ck;
         const int nseg = (d.steps + c - 1) / c;
+        double *sb0 = p.B0 + d.ox;
         // workspace carve-up
         double *CK = ws;                                  // nseg * n
         double *SEG = CK + (long long)nseg * n;           // (c + 1) * 4 * n
@@ -525,7 +619,7 @@ template <int BS> __global__ void __launch_bounds__(BS, 768 / BS) k_batch_fwdadj
         auto slot = [&](int m, int a) -> double * { return SEG + ((long long)m * 4 + a) * n; };
 
         // clear what must start at zero for this instance's shape
-        for (long long q = threadIdx.x; q < n; q += BS) {
+        for (long long q = g.t; q < n; q += g.n) {
             FB[q] = 0.0;
             Y1B[q] = 0.0;
             Y3B[q] = 0.0;
@@ -533,12 +627,12 @@ template <int BS> __global__ void __launch_bounds__(BS, 768 / BS) k_batch_fwdadj
         }
         for (int m = 0; m < c; ++m) {
             double *y2 = slot(m, 2);
-            for (int q = threadIdx.x; q < ny; q += BS) {
+            for (int q = g.t; q < ny; q += g.n) {
                 y2[q] = 0.0;
                 y2[(long long)(nx - 1) * ny + q] = 0.0;
             }
         }
-        __syncthreads();
+        g.sync();
         // forward pass with checkpoints; the steps of the last segment keep their stage values in
         // the segment slots, so the reverse sweep starts without recomputing that segment
         const double *cur = CK;
@@ -546,39 +640,39 @@ template <int BS> __global__ void __launch_bounds__(BS, 768 / BS) k_batch_fwdadj
         for (int step = 0; step < d.steps; ++step) {
             if (step >= n0_last) {
                 const int m = step - n0_last;
-                fwd_step<double, BS>(v, d.scheme, cur, slot(m, 1), slot(m, 2), slot(m, 3), slot(m + 1, 0), sb0, d.bnc);
+                fwd_step<double, SCH>(v, cur, slot(m, 1), slot(m, 2), slot(m, 3), slot(m + 1, 0), sb0, d.bnc, g);
                 cur = slot(m + 1, 0);
                 continue;
             }
             double *next = ((step + 1) % c == 0 && step + 1 < d.steps) ? CK + (long long)((step + 1) / c) * n
                                                                         : ((step & 1) ? W1 : W0);
-            fwd_step<double, BS>(v, d.scheme, cur, slot(0, 1), slot(0, 2), slot(0, 3), next, sb0, d.bnc);
+            fwd_step<double, SCH>(v, cur, slot(0, 1), slot(0, 2), slot(0, 3), next, sb0, d.bnc, g);
             cur = next;
         }
         // value, finiteness, final surface
-        if (threadIdx.x == 0) s_bad = 0;
-        __syncthreads();
+        if (g.t == 0) s_bad[g.gi] = 0;
+        g.sync();
         int bad = 0;
         double *outU = p.U + d.o2;
-        for (long long q = threadIdx.x; q < n; q += BS) {
+        for (long long q = g.t; q < n; q += g.n) {
             const double val = cur[q];
             bad |= !isfinite(val);
             outU[q] = val;
             VB[q] = 0.0;
         }
-        if (bad) atomicOr(&s_bad, 1);
-        __syncthreads();
-        if (threadIdx.x == 0) {
+        if (bad) atomicOr(&s_bad[g.gi], 1);
+        g.sync();
+        if (g.t == 0) {
             const long long o = (long long)d.i0 * ny + d.j0;
             p.values[inst] = d.w00 * cur[o] + d.w10 * cur[o + ny] + d.w01 * cur[o + 1] + d.w11 * cur[o + ny + 1];
-            p.status[inst] = s_bad;
+            p.status[inst] = s_bad[g.gi];
             p.final_in_v[inst] = 0;
             VB[o] = d.w00;
             VB[o + ny] = d.w10;
             VB[o + 1] = d.w01;
             VB[o + ny + 1] = d.w11;
         }
-        __syncthreads();
+        g.sync();
         // reverse sweep over the segments
         adj_acc acc;
         for (int q = 0; q < 5; ++q) acc.s[q] = 0.0;
@@ -590,12 +684,12 @@ template <int BS> __global__ void __launch_bounds__(BS, 768 / BS) k_batch_fwdadj
             const double *u0 = CK + (long long)sgi * n;
             for (int m = 0; m < L && sgi < nseg - 1; ++m) {
                 const double *um = (m == 0) ? u0 : slot(m, 0);
-                fwd_step<double, BS>(v, d.scheme, um, slot(m, 1), slot(m, 2), slot(m, 3), slot(m + 1, 0), sb0, d.bnc);
+                fwd_step<double, SCH>(v, um, slot(m, 1), slot(m, 2), slot(m, 3), slot(m + 1, 0), sb0, d.bnc, g);
             }
             for (int m = L - 1; m >= 0; --m) {
                 const double *um = (m == 0) ? u0 : slot(m, 0);
-                adj_step<BS>(v, d, um, slot(m, 1), slot(m, 2), slot(m, 3), slot(m + 1, 0), vb, ub, Y1B, Y2B, Y3B, FB,
-                             TMP, LV, LS, HS, acc, d.a_tau0 + d.a_dtau * (n0 + m));
+                adj_step<SCH>(v, d, um, slot(m, 1), slot(m, 2), slot(m, 3), slot(m + 1, 0), vb, ub, Y1B, Y2B, Y3B, FB,
+                              TMP, LV, LS, HS, acc, d.a_tau0 + d.a_dtau * (n0 + m), g);
                 double *t = ub;
                 ub = vb;
                 vb = t;
@@ -603,28 +697,25 @@ template <int BS> __global__ void __launch_bounds__(BS, 768 / BS) k_batch_fwdadj
         }
         // vb = adjoint of the initial condition
         double *outL = p.V + d.o2;
-        for (long long q = threadIdx.x; q < n; q += BS) outL[q] = vb[q];
+        for (long long q = g.t; q < n; q += g.n) outL[q] = vb[q];
         const double th = d.a_theta, ni = d.a_ni;
-        double g[5];
-        g[0] = acc.s[0] + d.a_halfk * th * acc.vb;
-        g[1] = acc.s[1] + ni * th * acc.vk;
-        g[2] = acc.s[2] + ni * th * acc.vt;
-        g[3] = acc.s[3] + ni * th * acc.vs1 + d.a_betat * th * acc.vs2;
-        g[4] = acc.s[4];
+        double gr[5];
         // order in the output: kappa, theta, sigma, rho, r
-        red[0][threadIdx.x] = g[1];
-        red[1][threadIdx.x] = g[2];
-        red[2][threadIdx.x] = g[3];
-        red[3][threadIdx.x] = g[4];
-        red[4][threadIdx.x] = g[0];
-        __syncthreads();
-        for (int h = BS / 2; h > 0; h >>= 1) {
-            if (threadIdx.x < h)
-                for (int q = 0; q < 5; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + h];
-            __syncthreads();
+        gr[0] = acc.s[1] + ni * th * acc.vk;
+        gr[1] = acc.s[2] + ni * th * acc.vt;
+        gr[2] = acc.s[3] + ni * th * acc.vs1 + d.a_betat * th * acc.vs2;
+        gr[3] = acc.s[4];
+        gr[4] = acc.s[0] + d.a_halfk * th * acc.vb;
+        // sum over the group: within each warp by shuffles, then the warps in order
+        for (int q = 0; q < 5; ++q)
+            for (int off = 16; off > 0; off >>= 1) gr[q] += __shfl_down_sync(0xffffffffu, gr[q], off);
+        for (int w = 0; w < gw; ++w) {
+            if (g.t == 32 * w)
+                for (int q = 0; q < 5; ++q) red[g.gi][q] = (w == 0 ? 0.0 : red[g.gi][q]) + gr[q];
+            g.sync();
         }
-        if (threadIdx.x < 5) p.grads[5LL * inst + threadIdx.x] = red[threadIdx.x][0];
-        __syncthreads();
+        if (g.t < 5) p.grads[5LL * inst + g.t] = red[g.gi][g.t];
+        g.sync();
     }
 }
 
@@ -646,7 +737,7 @@ __global__ void k_wide_s(const __grid_constant__ bparams<T> p, const T *U, const
 {
     const bdesc d = p.desc[0];
     const inst_view<T> v = make_view(p, d);
-    s_stage<T, KIND>(v, d.scheme, U, Y1, Y2, Y, gtid(), gstride());
+    with_scheme(d.scheme, [&](auto sch) { s_stage<T, KIND, decltype(sch)::value>(v, U, Y1, Y2, Y, gtid(), gstride()); });
 }
 template <typename T> __global__ void k_wide_v(const __grid_constant__ bparams<T> p, const T *in, const T *inh, const T *b0, T *out)
 {
@@ -718,7 +809,9 @@ __global__ void __launch_bounds__(1024) k_wide_s_chunk(const __grid_constant__ b
         const int jj = ldg(v.jmap() + j);
         lo = U[jj];
         hi = U[(long long)(nx - 1) * ny + jj];
-        sb[c][lane] = s_line_fwd<T, KIND>(v, d.scheme, U, Y1, Y2, Y, j, t0, t1, c == 0 ? lo : T(0), hi);
+        with_scheme(d.scheme, [&](auto sch) {
+            sb[c][lane] = s_line_fwd<T, KIND, decltype(sch)::value>(v, U, Y1, Y2, Y, j, t0, t1, c == 0 ? lo : T(0), hi);
+        });
         sa[c][lane] = hf[(long long)t1 * ny + j];
     }
     __syncthreads();
@@ -865,7 +958,9 @@ __global__ void k_wadj_s(const __grid_constant__ bparams<double> p, const double
     const long long t = gtid();
     adj_acc acc;
     acc_load(acc, acc_a, nacc, t);
-    adj_s<KIND>(v, d, U, Y1, Y2, Yo, XB, FB, TMP, LS, HS, UB, Y1B, acc, tau, gtid(), gstride());
+    with_scheme(d.scheme, [&](auto sch) {
+        adj_s<KIND, decltype(sch)::value>(v, d, U, Y1, Y2, Yo, XB, FB, TMP, LS, HS, UB, Y1B, acc, tau, gtid(), gstride());
+    });
     acc_store(acc, acc_a, nacc, t);
 }
 
@@ -1007,55 +1102,60 @@ __global__ void __launch_bounds__(1024) k_wadj_s_chunk(const __grid_constant__ b
     chunk_range(e, P, c, t0, t1);
     adj_chunk_solve(TMP, j, ny, XB, v.S(SL_G), v.S(SL_LA), hz, hw, j, ny, e, t0, t1, c, P, lane, act, sa, sb);
     if (!act) return;
-    const bool sabr = d.model == LSS_ADI_SABR, hv = d.scheme == LSS_ADI_HUNDSDORFER_VERWER;
-    const double th = d.a_theta;
-    const double zt = (d.scheme == LSS_ADI_MODIFIED_CRAIG_SNEYD) ? (d.a_zeta - th) : hv ? d.a_zeta : 0.0;
+    const bool sabr = d.model == LSS_ADI_SABR;
+    const double th = d.a_theta, omth = 1.0 - d.a_theta;
     adj_acc acc;
     acc_load(acc, acc_a, nacc, tid);
     const double *LA = v.S(SL_LA), *IB = v.S(SL_IB);
-    s_sums ps = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    // three-row window over the chunk's rows (adj_s_row / adj_s_sum_w)
-    s_row rh = adj_s_row<KIND>(U, Y1, Y2, Yo, (long long)(t1 + 1) * ny + j, th, hv);
-    s_row rc = adj_s_row<KIND>(U, Y1, Y2, Yo, (long long)t1 * ny + j, th, hv);
-    for (int t = t1; t >= t0; --t) {
-        const long long o = (long long)t * ny + j;
-        const s_row rl = adj_s_row<KIND>(U, Y1, Y2, Yo, o - ny, th, hv);
-        const double w0 = TMP[o];
-        FB[o] = w0;
-        const double mu = __ldg(IB + o) * w0;
-        if constexpr (KIND == 2) {
-            const double w1 = (t + 1 <= e) ? TMP[o + ny] : 0.0, w2 = (t + 2 <= e) ? TMP[o + 2LL * ny] : 0.0;
-            const double la2 = (t + 2 <= e) ? __ldg(LA + o + 2LL * ny) : 0.0;
-            const double sc1 = (t + 1 <= e) ? __ldg(v.S(SL_S2SC) + o + ny) : 0.0;
-            const double fin = la2 * w2 + sc1 * w1 + __ldg(v.S(SL_S2SE) + o) * w0;
-            if (hv) {
-                Y1B[o + ny] = fin;
-            } else {
-                UB[o + ny] += fin;
-                Y1B[o] = mu;
+    with_scheme(d.scheme, [&](auto sch) {
+        constexpr int SCH = decltype(sch)::value;
+        constexpr bool hv = SCH == LSS_ADI_HUNDSDORFER_VERWER;
+        s_sums ps = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        // three-row window over the chunk's rows (adj_s_row / adj_s_point)
+        s_row rh = adj_s_row<KIND, SCH>(U, Y1, Y2, Yo, (long long)(t1 + 1) * ny + j, th, omth);
+        s_row rc = adj_s_row<KIND, SCH>(U, Y1, Y2, Yo, (long long)t1 * ny + j, th, omth);
+        for (int t = t1; t >= t0; --t) {
+            const long long o = (long long)t * ny + j;
+            const s_row rl = adj_s_row<KIND, SCH>(U, Y1, Y2, Yo, o - ny, th, omth);
+            const double w0 = TMP[o];
+            FB[o] = w0;
+            const double mu = __ldg(IB + o) * w0;
+            if constexpr (KIND == 2) {
+                const double w1 = (t + 1 <= e) ? TMP[o + ny] : 0.0, w2 = (t + 2 <= e) ? TMP[o + 2LL * ny] : 0.0;
+                const double la2 = (t + 2 <= e) ? __ldg(LA + o + 2LL * ny) : 0.0;
+                const double sc1 = (t + 1 <= e) ? __ldg(v.S(SL_S2SC) + o + ny) : 0.0;
+                const double fin = la2 * w2 + sc1 * w1 + __ldg(v.S(SL_S2SE) + o) * w0;
+                if constexpr (hv) {
+                    Y1B[o + ny] = fin;
+                } else {
+                    UB[o + ny] += fin;
+                    Y1B[o] = mu;
+                }
+            }
+            const double muX = mu * __ldg(v.X(X_HX) + t);
+            const double muC = sabr ? mu * __ldg(v.X(X_HC) + t) : muX;
+            adj_s_point<KIND, SCH>(v, ps, rh, rc, rl, mu, muX, muC, t, sabr);
+            rh = rc;
+            rc = rl;
+        }
+        if (c == 0) {
+            const double w1 = TMP[(long long)ny + j], la1 = __ldg(LA + ny + j);
+            LS[j] = -la1 * w1 + XB[j];
+            if constexpr (KIND == 2) {
+                const double w2 = (2 <= e) ? TMP[2LL * ny + j] : 0.0, la2 = (2 <= e) ? __ldg(LA + 2LL * ny + j) : 0.0;
+                const double a1 = la2 * w2 + __ldg(v.S(SL_S2SC) + ny + j) * w1, a0 = la1 * w1;
+                if constexpr (hv) {
+                    Y1B[(long long)ny + j] = a1;
+                    Y1B[j] = a0;
+                } else {
+                    UB[(long long)ny + j] += a1;
+                    UB[j] += a0;
+                }
             }
         }
-        adj_s_sum_w<KIND>(v, d, ps, rh, rc, rl, th, zt, hv, mu, t, KIND == 1 || zt != 0.0, sabr);
-        rh = rc;
-        rc = rl;
-    }
-    if (c == 0) {
-        const double w1 = TMP[(long long)ny + j], la1 = __ldg(LA + ny + j);
-        LS[j] = -la1 * w1 + XB[j];
-        if constexpr (KIND == 2) {
-            const double w2 = (2 <= e) ? TMP[2LL * ny + j] : 0.0, la2 = (2 <= e) ? __ldg(LA + 2LL * ny + j) : 0.0;
-            const double a1 = la2 * w2 + __ldg(v.S(SL_S2SC) + ny + j) * w1, a0 = la1 * w1;
-            if (hv) {
-                Y1B[(long long)ny + j] = a1;
-                Y1B[j] = a0;
-            } else {
-                UB[(long long)ny + j] += a1;
-                UB[j] += a0;
-            }
-        }
-    }
-    if (c == P - 1) HS[j] = -__ldg(v.Yv(Y_CHS) + j) * TMP[(long long)e * ny + j] + XB[(long long)(nx - 1) * ny + j];
-    adj_s_line(v, d, j, ps, tau, sabr, acc);
+        if (c == P - 1) HS[j] = -__ldg(v.Yv(Y_CHS) + j) * TMP[(long long)e * ny + j] + XB[(long long)(nx - 1) * ny + j];
+        adj_s_line<KIND, SCH>(v, d, j, ps, tau, sabr, acc);
+    });
     acc_store(acc, acc_a, nacc, tid);
 }
 
@@ -1175,16 +1275,32 @@ template <typename T> struct batch_typed {
     dbuf<T> state, stab, vtab, xarena, yarena;
     std::vector<std::vector<T>> payoff_host;
     dbuf<T> d_payoff; // concatenated initial conditions (sum n)
-    int grid_blocks = 0;
     long long launches = 0;
     // forward + adjoint
     bool adjoint_ok = false;      // FP64, Heston and SABR with r = 0
     std::string adjoint_why;
-    int ck_override = 0;          // checkpoint interval (0 = planned by plan_checkpoints)
+    int ck_override = 0;          // checkpoint interval (0 = planned from the workspace cap)
     double ws_cap = 0.0;          // adjoint workspace cap in bytes (0 = a quarter of the device memory)
-    int grid_adj = 0;                 // CTAs the workspace has slices for
-    long long ws_stride = 0, ws_need = 0;
     dbuf<double> d_grads, d_ws;
+    dbuf<T> b0arena;              // nx arena: boundary column of the step (persistent kernels)
+    // warp-group plan of a persistent kernel (per mode): instance classes, class queues, CTA
+    // layouts and, for mode 1, the workspace slices and checkpoint intervals
+    // (one launch per scheme present: each specialisation gets its own register allocation)
+    struct group_plan {
+        int grid = 0;
+        int start[MAX_GROUP_WARPS + 1] = {}, cnt[MAX_GROUP_WARPS + 1] = {};
+        long long need[MAX_GROUP_WARPS + 1] = {};
+        std::vector<int> order, layout;
+        dbuf<int> d_order, d_layout;
+    };
+    static constexpr int NSCHEMES = 4; // LSS_ADI_DOUGLAS_RACHFORD .. LSS_ADI_HUNDSDORFER_VERWER
+    struct mode_plan {
+        bool valid = false;
+        int gcap = 0, override_ck = -1;
+        double cap = -1.0;
+        long long per_warp = 0;
+        group_plan sch[NSCHEMES];
+    } plan[2];
     int sms = 0;
     cudaGraphExec_t graph = nullptr;
     int graph_mode = -1;
@@ -1202,6 +1318,7 @@ template <typename T> struct batch_typed {
         p.order = d_order.p;
         p.count = count;
         p.counter = d_counter.p;
+        p.B0 = b0arena.p;
         p.U = state.p;
         p.V = state.p + total_n;
         p.Y1 = state.p + 2 * total_n;
@@ -1218,22 +1335,35 @@ template <typename T> struct batch_typed {
         p.final_in_v = d_final.p;
         p.grads = d_grads.p;
         p.ws = d_ws.p;
-        p.ws_stride = ws_stride;
         p.payoff = d_payoff.p;
+        return p;
+    }
+    // params() with the class queues and layouts of mode m's plan for scheme sc
+    bparams<T> params_for(int m, int sc)
+    {
+        bparams<T> p = params();
+        const group_plan &g = plan[m].sch[sc];
+        p.order = g.d_order.p;
+        p.layout = g.d_layout.p;
+        p.counter = d_counter.p + sc * (MAX_GROUP_WARPS + 1);
+        for (int c = 0; c <= MAX_GROUP_WARPS; ++c) {
+            p.cls_start[c] = g.start[c];
+            p.cls_count[c] = g.cnt[c];
+            p.cls_need[c] = g.need[c];
+        }
+        p.ws_per_warp = plan[m].per_warp;
         return p;
     }
 
     int create(const lss_adi_problem *ps, int n);
     int prepare_adjoint(cudaStream_t s);
-    int ensure_ws(int bs); // workspace (and checkpoint plan) for CTA size `bs`
-    int plan_checkpoints(int slices);
-    int plan_slices = 0, plan_override = -1;    // what the current plan was made for
-    double plan_cap = -1.0;
     double ws_bytes_allowed();
-    // threads per instance (CTA size) of the persistent kernels, per mode; chosen by autotune()
-    int bs_mode[2] = {64, 64};
-    template <int BS> int launch_forward(cudaStream_t s);
-    template <int BS> int launch_fwdadj(cudaStream_t s);
+    // most threads per instance (32 x warps of a group) of the persistent kernels, per mode;
+    // chosen by autotune()
+    int bs_mode[2] = {BATCH_CTA, BATCH_CTA};
+    int make_plan(int mode); // (re)plans mode's groups when its inputs changed
+    int launch_forward(cudaStream_t s);
+    int launch_fwdadj(cudaStream_t s);
     int autotune(int mode, int *chosen, cudaStream_t s);
     // wide path (count == 1)
     dbuf<T> d_b0;
@@ -1401,7 +1531,8 @@ template <typename T> int batch_typed<T>::create(const lss_adi_problem *ps, int 
     LSS_CUDA_TRY(d_desc.upload(desc.data(), n), "batch: uploading descriptors");
     LSS_CUDA_TRY(d_order.alloc(n), "batch: allocating order");
     LSS_CUDA_TRY(d_order.upload(order.data(), n), "batch: uploading order");
-    LSS_CUDA_TRY(d_counter.alloc(1), "batch: allocating counter");
+    LSS_CUDA_TRY(d_counter.alloc(4 * (MAX_GROUP_WARPS + 1)), "batch: allocating counters");
+    LSS_CUDA_TRY(b0arena.alloc(total_x), "batch: allocating boundary columns");
     LSS_CUDA_TRY(d_status.alloc(n), "batch: allocating status");
     LSS_CUDA_TRY(d_final.alloc(n), "batch: allocating flags");
     LSS_CUDA_TRY(d_values.alloc(n), "batch: allocating values");
@@ -1465,11 +1596,9 @@ template <typename T> int batch_typed<T>::create(const lss_adi_problem *ps, int 
         LSS_CUDA_TRY(cudaGetLastError(), "batch: launching v-line set-up");
         LSS_CUDA_TRY(cudaDeviceSynchronize(), "batch: v-line set-up");
     }
-    int dev = 0, sms = 0, per_sm = 0; // local
+    int dev = 0, sms = 0; // local
     LSS_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
     LSS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
-    LSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_forward<T, 64>, 64, 0), "occupancy");
-    grid_blocks = std::max(1, std::min(sms * std::max(1, std::min(per_sm, 16)), n));
     this->sms = sms;
     if (n == 1) LSS_CUDA_TRY(d_b0.alloc(desc[0].nx), "batch: allocating the boundary column");
     return LSS_ADI_OK;
@@ -1479,12 +1608,12 @@ template <typename T> int batch_typed<T>::prepare_adjoint(cudaStream_t s)
 {
     (void)s;
     if (!adjoint_ok) return set_error(LSS_ADI_EUNSUPPORTED, "batch: " + adjoint_why);
-    return ensure_ws(bs_mode[1]);
+    return make_plan(1);
 }
 
-// Workspace (doubles) of one CTA slice for an instance checkpointed every c steps: nseg
-// checkpoints, the stage values of one segment (4 arrays per step plus the segment's end), two
-// scratch states, seven adjoint arrays and three line-end vectors.
+// Workspace (doubles) of one instance checkpointed every c steps: nseg checkpoints, the stage
+// values of one segment (4 arrays per step plus the segment's end), two scratch states, seven
+// adjoint arrays and three line-end vectors.
 static long long adj_ws_need(const bdesc &d, int c)
 {
     const long long nn = static_cast<long long>(d.nx) * d.ny;
@@ -1507,114 +1636,211 @@ template <typename T> double batch_typed<T>::ws_bytes_allowed()
     return std::min(cap, 0.5 * (static_cast<double>(free_b) + held));
 }
 
-// Checkpoint interval of every instance for `slices` CTA slices.  The forward pass keeps the
-// stage values of the last segment, so an instance recomputes all its segments but one: the
-// longer the segments, the less it recomputes (none when one segment holds the whole loop).
-// Each slice gets at least the sqrt(steps) need of the largest instance and, when the device has
-// room, up to half of the free memory over the slices; every instance then takes the longest
-// interval whose workspace fits the slice.  checkpoint_every (ck_override) fixes the interval.
-template <typename T> int batch_typed<T>::plan_checkpoints(int slices)
+// CTA layouts (warp-group sizes, one hex digit per group) for `grid` CTAs of MAX_GROUP_WARPS
+// warps: each CTA in turn takes the layout that covers the most of the classes' remaining
+// shares of the warps (class c's share: its grid-point-steps over all, times the warps); the
+// groups' stealing of smaller instances evens out what the rounding leaves.
+static std::vector<int> plan_layouts(int grid, const double work[MAX_GROUP_WARPS + 1], int gcap)
 {
-    long long base = 0, full = 0;
-    std::vector<int> c0(count);
-    for (int k = 0; k < count; ++k) {
-        const bdesc &d = desc[k];
-        c0[k] = ck_override > 0 ? std::min(ck_override, d.steps)
-                                : std::max(1, static_cast<int>(std::ceil(std::sqrt(static_cast<double>(d.steps)))));
-        base = std::max(base, adj_ws_need(d, c0[k]));
-        full = std::max(full, adj_ws_need(d, d.steps));
+    struct lay { int code; int w[MAX_GROUP_WARPS + 1]; };
+    const lay all[] = {{0x4, {0, 0, 0, 0, 1}}, {0x13, {0, 1, 0, 1, 0}}, {0x22, {0, 0, 2, 0, 0}},
+                       {0x112, {0, 2, 1, 0, 0}}, {0x1111, {0, 4, 0, 0, 0}}};
+    std::vector<lay> cand;
+    for (const lay &l : all) {
+        bool ok = true;
+        for (int c = gcap + 1; c <= MAX_GROUP_WARPS; ++c) ok = ok && l.w[c] == 0;
+        if (ok) cand.push_back(l);
     }
-    long long budget = base;
-    if (ck_override <= 0) {
-        const long long avail = static_cast<long long>(ws_bytes_allowed() / sizeof(double) / std::max(1, slices));
-        budget = std::max(base, std::min(full, avail));
-    }
-    bool changed = false;
-    long long need = 0;
-    for (int k = 0; k < count; ++k) {
-        bdesc &d = desc[k];
-        int c = c0[k];
-        if (ck_override <= 0)
-            for (int cc = d.steps; cc > c0[k]; --cc)
-                if (adj_ws_need(d, cc) <= budget) { c = cc; break; }
-        if (c != d.ck) {
-            d.ck = c;
-            changed = true;
+    double tot = 0.0;
+    for (int c = 1; c <= MAX_GROUP_WARPS; ++c) tot += work[c];
+    double want[MAX_GROUP_WARPS + 1] = {};
+    for (int c = 1; c <= MAX_GROUP_WARPS; ++c)
+        want[c] = tot > 0.0 ? work[c] / tot * MAX_GROUP_WARPS * grid : 0.0;
+    // the first CTA holds a group as large as the largest class that has work, so that every
+    // class has a group able to take its instances
+    int top = 0;
+    for (int c = 1; c <= MAX_GROUP_WARPS; ++c)
+        if (work[c] > 0.0) top = c;
+    std::vector<int> out(grid);
+    for (int b = 0; b < grid; ++b) {
+        int best = 0;
+        double best_score = -1.0;
+        if (b == 0 && top > 0) {
+            for (size_t q = 0; q < cand.size(); ++q) {
+                bool fits = cand[q].w[top] > 0;
+                for (int c = top + 1; c <= MAX_GROUP_WARPS; ++c) fits = fits && cand[q].w[c] == 0;
+                if (fits) { best = static_cast<int>(q); break; }
+            }
+            out[b] = cand[best].code;
+            for (int c = 1; c <= MAX_GROUP_WARPS; ++c) want[c] -= cand[best].w[c] * c;
+            continue;
         }
-        need = std::max(need, adj_ws_need(d, c));
+        for (size_t q = 0; q < cand.size(); ++q) {
+            double score = 0.0;
+            for (int c = 1; c <= MAX_GROUP_WARPS; ++c)
+                score += std::min(static_cast<double>(cand[q].w[c] * c), std::max(0.0, want[c]));
+            if (score > best_score + 1e-9) { best_score = score; best = static_cast<int>(q); }
+        }
+        out[b] = cand[best].code;
+        for (int c = 1; c <= MAX_GROUP_WARPS; ++c) want[c] -= cand[best].w[c] * c;
     }
-    if (changed) LSS_CUDA_TRY(cudaMemcpy(d_desc.p, desc.data(), count * sizeof(bdesc), cudaMemcpyHostToDevice), "batch: descriptors");
-    ws_need = (need + 31) / 32 * 32;
-    return LSS_ADI_OK;
+    return out;
 }
 
-// Adjoint workspace for every resident CTA of k_batch_fwdadj<bs> (one slice per CTA).
-template <typename T> int batch_typed<T>::ensure_ws(int bs)
+// Warp-group plan of mode `mode`: class (warps per instance) of every instance -- one warp per 32
+// S lines, at most bs_mode/32 -- and, per scheme present (one launch each), the class queues
+// longest first and the CTA layouts; for mode 1 the workspace slices (per warp, within the cap,
+// shared by the schemes' launches) and every instance's checkpoint interval: at least
+// ceil(sqrt(steps)) (or the fixed interval), else the longest whose workspace fits the slices of
+// its class's group.  A cap too small for the minimal slices of every resident CTA runs fewer CTAs.
+template <typename T> int batch_typed<T>::make_plan(int mode)
 {
-    int per_sm = 0;
-    switch (bs) {
-    case 32: LSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_fwdadj<32>, 32, 0), "occupancy"); break;
-    case 128: LSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_fwdadj<128>, 128, 0), "occupancy"); break;
-    case 256: LSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_fwdadj<256>, 256, 0), "occupancy"); break;
-    default: LSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_fwdadj<64>, 64, 0), "occupancy"); break;
-    }
-    int want = std::max(1, std::min(sms * std::max(1, per_sm), count));
-    {
-        // fewer resident CTAs when the cap does not hold one minimal slice (ceil(sqrt(steps))
-        // checkpoints, or the fixed interval) per CTA
-        long long base = 0;
-        for (int k = 0; k < count; ++k) {
-            const bdesc &d = desc[k];
-            const int c = ck_override > 0 ? std::min(ck_override, d.steps)
-                                          : std::max(1, static_cast<int>(std::ceil(std::sqrt(static_cast<double>(d.steps)))));
-            base = std::max(base, adj_ws_need(d, c));
-        }
-        const double allowed = ws_bytes_allowed();
-        const long long fit = static_cast<long long>(allowed / (static_cast<double>((base + 31) / 32 * 32) * sizeof(double)));
-        if (fit < 1)
-            return set_error(LSS_ADI_ENOMEM, "batch: the adjoint workspace cap (" + std::to_string(allowed / 1e6) +
-                                                 " MB) does not hold the checkpoints of the largest instance");
-        want = static_cast<int>(std::min<long long>(want, fit));
-    }
-    if (d_ws.p && grid_adj == want && plan_slices == want && plan_override == ck_override && plan_cap == ws_cap)
-        return LSS_ADI_OK;
-    int rc = plan_checkpoints(want);
-    if (rc) return rc;
-    if (!(d_ws.p && ws_stride == ws_need && grid_adj == want)) {
-        ws_stride = ws_need;
-        grid_adj = want;
-        d_ws.release();
-        LSS_CUDA_TRY(d_ws.alloc(static_cast<size_t>(ws_stride) * grid_adj), "batch: allocating adjoint workspace");
-    }
-    plan_slices = want;
-    plan_override = ck_override;
-    plan_cap = ws_cap;
-    if (graph) { // a captured launch holds the old workspace pointer and checkpoint plan
+    mode_plan &mp = plan[mode];
+    const int gcap = std::max(1, std::min(MAX_GROUP_WARPS, bs_mode[mode] / 32));
+    if (mp.valid && mp.gcap == gcap && (mode == 0 || (mp.override_ck == ck_override && mp.cap == ws_cap))) return LSS_ADI_OK;
+    if (graph && graph_mode == mode) { // a captured launch holds the old plan
         cudaGraphExecDestroy(graph);
         graph = nullptr;
         graph_mode = -1;
     }
-    return LSS_ADI_OK;
-}
-
-template <typename T> template <int BS> int batch_typed<T>::launch_forward(cudaStream_t s)
-{
+    mp.valid = false;
+    std::vector<int> cls(count);
+    double work[NSCHEMES][MAX_GROUP_WARPS + 1] = {};
+    int warps_wanted[NSCHEMES] = {};
+    for (int k = 0; k < count; ++k) {
+        const int nx = desc[k].nx, ny = desc[k].ny, sc = desc[k].scheme;
+        cls[k] = std::max(1, std::min(gcap, (ny - 2 + 31) / 32));
+        // the group's threads that have a line, over its threads, per S / v sweep: the class's
+        // warps are shared out by work over that efficiency
+        const int th = 32 * cls[k];
+        const double lines = static_cast<double>(nx - 2) * (ny - 2);
+        const double slots = static_cast<double>(nx - 2) * ((ny - 2 + th - 1) / th) * th +
+                             static_cast<double>(ny - 2) * ((nx - 2 + th - 1) / th) * th;
+        work[sc][cls[k]] += static_cast<double>(gps[k]) * slots / (2.0 * lines);
+        warps_wanted[sc] += cls[k];
+    }
     int per_sm = 0;
-    LSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_forward<T, BS>, BS, 0), "occupancy");
-    const int grid = std::max(1, std::min(sms * std::max(1, per_sm), count));
-    k_batch_forward<T, BS><<<grid, BS, 0, s>>>(params());
-    LSS_CUDA_TRY(cudaGetLastError(), "batch: launching k_batch_forward");
+    if constexpr (std::is_same<T, double>::value) {
+        if (mode == 1)
+            LSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_fwdadj<LSS_ADI_CRAIG_SNEYD>, BATCH_CTA, 0),
+                         "occupancy");
+    }
+    if (mode == 0)
+        LSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_forward<T, LSS_ADI_CRAIG_SNEYD>, BATCH_CTA, 0),
+                     "occupancy");
+    const int resident = sms * std::max(1, per_sm);
+    int grid[NSCHEMES];
+    for (int sc = 0; sc < NSCHEMES; ++sc)
+        grid[sc] = std::max(1, std::min(resident, (warps_wanted[sc] + MAX_GROUP_WARPS - 1) / MAX_GROUP_WARPS));
+    mp.per_warp = 0;
+    for (int sc = 0; sc < NSCHEMES; ++sc)
+        for (int c = 0; c <= MAX_GROUP_WARPS; ++c) mp.sch[sc].need[c] = 0;
+    if (mode == 1) {
+        std::vector<int> c0(count);
+        long long base_w = 1, full_w = 1; // doubles per warp: minimal and no-recomputation slices
+        for (int k = 0; k < count; ++k) {
+            const bdesc &d = desc[k];
+            c0[k] = ck_override > 0 ? std::min(ck_override, d.steps)
+                                    : std::max(1, static_cast<int>(std::ceil(std::sqrt(static_cast<double>(d.steps)))));
+            base_w = std::max(base_w, (adj_ws_need(d, c0[k]) + cls[k] - 1) / cls[k]);
+            full_w = std::max(full_w, (adj_ws_need(d, d.steps) + cls[k] - 1) / cls[k]);
+        }
+        base_w = (base_w + 31) / 32 * 32;
+        const double allowed = ws_bytes_allowed() / sizeof(double);
+        const long long fit = static_cast<long long>(allowed / (static_cast<double>(base_w) * MAX_GROUP_WARPS));
+        if (fit < 1)
+            return set_error(LSS_ADI_ENOMEM, "batch: the adjoint workspace cap (" + std::to_string(allowed * 8.0 / 1e6) +
+                                                 " MB) does not hold the checkpoints of the largest instance");
+        int gmax = 1;
+        for (int sc = 0; sc < NSCHEMES; ++sc) {
+            grid[sc] = static_cast<int>(std::min<long long>(grid[sc], fit));
+            gmax = std::max(gmax, grid[sc]);
+        }
+        long long per_warp = base_w;
+        if (ck_override <= 0)
+            per_warp = std::max(base_w, std::min((full_w + 31) / 32 * 32,
+                                                 static_cast<long long>(allowed / (static_cast<double>(gmax) * MAX_GROUP_WARPS)) / 32 * 32));
+        bool changed = false;
+        for (int k = 0; k < count; ++k) {
+            bdesc &d = desc[k];
+            int c = c0[k];
+            if (ck_override <= 0)
+                for (int cc = d.steps; cc > c0[k]; --cc)
+                    if (adj_ws_need(d, cc) <= per_warp * cls[k]) { c = cc; break; }
+            if (c != d.ck) { d.ck = c; changed = true; }
+            long long &nd = mp.sch[d.scheme].need[cls[k]];
+            nd = std::max(nd, adj_ws_need(d, c));
+        }
+        if (changed)
+            LSS_CUDA_TRY(cudaMemcpy(d_desc.p, desc.data(), count * sizeof(bdesc), cudaMemcpyHostToDevice), "batch: descriptors");
+        mp.per_warp = per_warp;
+        const size_t want = static_cast<size_t>(per_warp) * MAX_GROUP_WARPS * gmax;
+        if (d_ws.n != want) {
+            d_ws.release();
+            LSS_CUDA_TRY(d_ws.alloc(want), "batch: allocating adjoint workspace");
+        }
+    }
+    for (int sc = 0; sc < NSCHEMES; ++sc) {
+        group_plan &g = mp.sch[sc];
+        // class queues, longest first within a class
+        g.order.clear();
+        for (int c = 0; c <= MAX_GROUP_WARPS; ++c) g.start[c] = g.cnt[c] = 0;
+        for (int c = 1; c <= MAX_GROUP_WARPS; ++c) {
+            g.start[c] = static_cast<int>(g.order.size());
+            for (int k : order)
+                if (cls[k] == c && desc[k].scheme == sc) g.order.push_back(k);
+            g.cnt[c] = static_cast<int>(g.order.size()) - g.start[c];
+        }
+        g.grid = g.order.empty() ? 0 : grid[sc];
+        if (!g.grid) continue;
+        g.layout = plan_layouts(g.grid, work[sc], gcap);
+        LSS_CUDA_TRY(g.d_order.alloc(g.order.size()), "batch: allocating class queues");
+        LSS_CUDA_TRY(g.d_order.upload(g.order.data(), g.order.size()), "batch: uploading class queues");
+        LSS_CUDA_TRY(g.d_layout.alloc(g.grid), "batch: allocating CTA layouts");
+        LSS_CUDA_TRY(g.d_layout.upload(g.layout.data(), g.grid), "batch: uploading CTA layouts");
+    }
+    LSS_CUDA_TRY(cudaDeviceSynchronize(), "batch: plan upload");
+    mp.gcap = gcap;
+    mp.override_ck = ck_override;
+    mp.cap = ws_cap;
+    mp.valid = true;
     return LSS_ADI_OK;
 }
 
-template <typename T> template <int BS> int batch_typed<T>::launch_fwdadj(cudaStream_t s)
+template <typename T> int batch_typed<T>::launch_forward(cudaStream_t s)
+{
+    for (int sc = 0; sc < NSCHEMES; ++sc) {
+        const group_plan &g = plan[0].sch[sc];
+        if (!g.grid) continue;
+        const bparams<T> p = params_for(0, sc);
+        switch (sc) {
+        case LSS_ADI_DOUGLAS_RACHFORD: k_batch_forward<T, LSS_ADI_DOUGLAS_RACHFORD><<<g.grid, BATCH_CTA, 0, s>>>(p); break;
+        case LSS_ADI_CRAIG_SNEYD: k_batch_forward<T, LSS_ADI_CRAIG_SNEYD><<<g.grid, BATCH_CTA, 0, s>>>(p); break;
+        case LSS_ADI_MODIFIED_CRAIG_SNEYD: k_batch_forward<T, LSS_ADI_MODIFIED_CRAIG_SNEYD><<<g.grid, BATCH_CTA, 0, s>>>(p); break;
+        default: k_batch_forward<T, LSS_ADI_HUNDSDORFER_VERWER><<<g.grid, BATCH_CTA, 0, s>>>(p); break;
+        }
+        LSS_CUDA_TRY(cudaGetLastError(), "batch: launching k_batch_forward");
+        ++launches;
+    }
+    return LSS_ADI_OK;
+}
+
+template <typename T> int batch_typed<T>::launch_fwdadj(cudaStream_t s)
 {
     if constexpr (std::is_same<T, double>::value) {
-        int per_sm = 0;
-        LSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_fwdadj<BS>, BS, 0), "occupancy");
-        const int grid = std::max(1, std::min({sms * std::max(1, per_sm), count, grid_adj}));
-        k_batch_fwdadj<BS><<<grid, BS, 0, s>>>(params());
-        LSS_CUDA_TRY(cudaGetLastError(), "batch: launching k_batch_fwdadj");
+        for (int sc = 0; sc < NSCHEMES; ++sc) {
+            const group_plan &g = plan[1].sch[sc];
+            if (!g.grid) continue;
+            const bparams<double> p = params_for(1, sc);
+            switch (sc) {
+            case LSS_ADI_DOUGLAS_RACHFORD: k_batch_fwdadj<LSS_ADI_DOUGLAS_RACHFORD><<<g.grid, BATCH_CTA, 0, s>>>(p); break;
+            case LSS_ADI_CRAIG_SNEYD: k_batch_fwdadj<LSS_ADI_CRAIG_SNEYD><<<g.grid, BATCH_CTA, 0, s>>>(p); break;
+            case LSS_ADI_MODIFIED_CRAIG_SNEYD: k_batch_fwdadj<LSS_ADI_MODIFIED_CRAIG_SNEYD><<<g.grid, BATCH_CTA, 0, s>>>(p); break;
+            default: k_batch_fwdadj<LSS_ADI_HUNDSDORFER_VERWER><<<g.grid, BATCH_CTA, 0, s>>>(p); break;
+            }
+            LSS_CUDA_TRY(cudaGetLastError(), "batch: launching k_batch_fwdadj");
+            ++launches;
+        }
         return LSS_ADI_OK;
     } else {
         (void)s;
@@ -1624,43 +1850,35 @@ template <typename T> template <int BS> int batch_typed<T>::launch_fwdadj(cudaSt
 
 template <typename T> int batch_typed<T>::enqueue(int mode, cudaStream_t s)
 {
-    int rc;
-    const int bs = bs_mode[mode == 1 ? 1 : 0];
+    int rc = make_plan(mode == 1 ? 1 : 0);
+    if (rc) return rc;
+    LSS_CUDA_TRY(cudaMemsetAsync(d_counter.p, 0, d_counter.n * sizeof(int), s), "batch: counter reset");
+    launches = 0;
     if (mode == 1) {
-        LSS_CUDA_TRY(cudaMemsetAsync(d_counter.p, 0, sizeof(int), s), "batch: counter reset");
-        rc = bs == 256 ? launch_fwdadj<256>(s) : bs == 128 ? launch_fwdadj<128>(s)
-                                               : bs == 32 ? launch_fwdadj<32>(s) : launch_fwdadj<64>(s);
+        rc = launch_fwdadj(s);
     } else {
         LSS_CUDA_TRY(cudaMemcpyAsync(state.p, d_payoff.p, total_n * sizeof(T), cudaMemcpyDeviceToDevice, s),
                      "batch: initial state");
-        LSS_CUDA_TRY(cudaMemsetAsync(d_counter.p, 0, sizeof(int), s), "batch: counter reset");
-        rc = bs == 256 ? launch_forward<256>(s) : bs == 128 ? launch_forward<128>(s)
-                                                : bs == 32 ? launch_forward<32>(s) : launch_forward<64>(s);
+        rc = launch_forward(s);
     }
-    launches = 1;
     return rc;
 }
 
-// Times one run per CTA size (32, 64, 128, 256 threads per instance) and keeps the fastest
-// for `mode`; with *chosen > 0 on entry, sets that size without timing.  One warp per
-// instance trades longer instances for no cross-warp barriers and twice the resident CTAs.
+// Times one run per cap on the warps per instance (32, 64 and 128 threads: groups of at most 1,
+// 2 or 4 warps) and keeps the fastest for `mode`; with *chosen > 0 on entry (32, 64, 96 or 128),
+// sets that cap without timing.
 template <typename T> int batch_typed<T>::autotune(int mode, int *chosen, cudaStream_t s)
 {
     const int m = mode == 1 ? 1 : 0;
-    if (mode == 1) {
-        int rc = prepare_adjoint(s);
-        if (rc) return rc;
-    }
+    if (mode == 1 && !adjoint_ok) return set_error(LSS_ADI_EUNSUPPORTED, "batch: " + adjoint_why);
     if (chosen && *chosen > 0) {
-        if (*chosen != 32 && *chosen != 64 && *chosen != 128 && *chosen != 256)
-            return set_error(LSS_ADI_EINVAL, "autotune: threads per instance must be 32, 64, 128 or 256");
+        if (*chosen != 32 && *chosen != 64 && *chosen != 96 && *chosen != 128)
+            return set_error(LSS_ADI_EINVAL, "autotune: threads per instance must be 32, 64, 96 or 128");
         bs_mode[m] = *chosen;
-        if (mode == 1) {
-            int rc = ensure_ws(*chosen);
-            if (rc) return rc;
-        }
+        int rc = make_plan(m);
+        if (rc) return rc;
     } else {
-        const int cand[4] = {32, 64, 128, 256};
+        const int cand[3] = {32, 64, 128};
         float best = 1e30f;
         int best_bs = bs_mode[m];
         cudaEvent_t e0, e1;
@@ -1668,22 +1886,16 @@ template <typename T> int batch_typed<T>::autotune(int mode, int *chosen, cudaSt
         LSS_CUDA_TRY(cudaEventCreate(&e1), "autotune: event");
         for (int c : cand) {
             bs_mode[m] = c;
-            if (mode == 1) {
-                // a size whose workspace (one slice per resident CTA) does not fit is skipped
-                int rc = ensure_ws(c);
-                if (rc == LSS_ADI_ENOMEM) {
-                    clear_error();
-                    continue;
-                }
-                if (rc) {
-                    cudaEventDestroy(e0);
-                    cudaEventDestroy(e1);
-                    return rc;
-                }
+            int rc = make_plan(m);
+            if (rc == LSS_ADI_ENOMEM) { // a plan whose workspace does not fit is skipped
+                clear_error();
+                continue;
             }
-            cudaEventRecord(e0, s);
-            int rc = enqueue(mode, s);
-            cudaEventRecord(e1, s);
+            if (!rc) {
+                cudaEventRecord(e0, s);
+                rc = enqueue(mode, s);
+                cudaEventRecord(e1, s);
+            }
             if (rc) {
                 cudaEventDestroy(e0);
                 cudaEventDestroy(e1);
@@ -1700,15 +1912,8 @@ template <typename T> int batch_typed<T>::autotune(int mode, int *chosen, cudaSt
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         bs_mode[m] = best_bs;
-        if (mode == 1) { // the workspace and checkpoint plan of the chosen size
-            int rc = ensure_ws(best_bs);
-            if (rc) return rc;
-        }
-    }
-    if (graph && graph_mode == mode) {
-        cudaGraphExecDestroy(graph);
-        graph = nullptr;
-        graph_mode = -1;
+        int rc = make_plan(m);
+        if (rc) return rc;
     }
     if (chosen) *chosen = bs_mode[m];
     return LSS_ADI_OK;
@@ -2041,8 +2246,8 @@ template <typename T> int batch_typed<T>::run_wide(cudaStream_t s, bool use_grap
 
 template <typename T> int batch_typed<T>::run(int mode, cudaStream_t s, bool use_graph)
 {
-    if (mode == 1) {
-        int rc = prepare_adjoint(s);
+    { // plans (allocations, uploads) happen here, never inside a stream capture
+        int rc = mode == 1 ? prepare_adjoint(s) : make_plan(0);
         if (rc) return rc;
     }
     if (!use_graph) return enqueue(mode, s);
@@ -2317,7 +2522,6 @@ int lss_adi_batch_create(const lss_adi_problem *problems, int count, lss_adi_bat
         int rc = validate_problem(problems[k], why);
         if (rc) return set_error(rc, "lss_adi_batch_create: instance " + std::to_string(k) + ": " + why);
         if (problems[k].precision != prec) return set_error(LSS_ADI_EINVAL, "lss_adi_batch_create: mixed precisions");
-        if (problems[k].nx > 256) return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_batch_create: nx > 256 (use lss_adi_create)");
         if (problems[k].scheme == LSS_ADI_EXPLICIT_EULER)
             return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_batch_create: instance " + std::to_string(k) +
                                                        ": the explicit Euler scheme runs on lss_adi_create");

@@ -228,3 +228,44 @@ def test_wide_adjoint_partitioned_solves_match_line_per_thread(lss, key):
         scale = max(np.abs(g0).max(), 1e-3 * abs(v0))
         assert np.max(np.abs(g - g0)) <= 1e-9 * scale, (chunks, g, g0)
         assert np.max(np.abs(lam - l0)) <= 1e-9 * np.abs(l0).max()
+
+
+def test_plain_central_difference_error_is_the_difference_own_noise(lss, oracle):
+    """A stable instance drawn as config 4 (seed 20261204): the adjoint gradient agrees with
+    Richardson-extrapolated central differences of the oracle (bumps 1e-3 / 5e-4) to 5e-7, while
+    the plain central difference at the relative bump 1e-5 sits farther from both -- by about the
+    spread between two plain differences at nearby bumps (1e-5 and 1.25e-5), i.e. its own
+    rounding noise: the oracle's value carries ~1e-13 relative rounding, divided by a bump of
+    1e-5 relative.  The 1e-6 criterion against a plain 1e-5 difference therefore measures the
+    difference, not the adjoint."""
+    from linear_system_solvers_gb300.batch import draw_batch
+
+    cands = draw_batch(64, seed=20261204)
+    p = None
+    for q in cands:
+        q.nt = 61
+        if q.nx <= 96 and q.ny <= 48:
+            surf = oracle.solve(oracle.Problem(**q.pde_fields()), "f64")
+            if not oracle_unstable(surf, q.s_hi):
+                p = q
+                break
+    assert p is not None
+    val, grads, _ = lss.ImplicitHestonSolver(p, precision="f64", arith="fast").adjoint(want_payoff_grad=False)
+
+    def central(name, rel):
+        base = getattr(p, name)
+        h = rel * abs(base)
+        up = oracle_value(oracle, lss, dataclasses.replace(p, **{name: base + h}))
+        dn = oracle_value(oracle, lss, dataclasses.replace(p, **{name: base - h}))
+        return (up - dn) / (2 * h)
+
+    worst_rich = 0.0
+    for k, name in enumerate(PARAMS):
+        rich = (4.0 * central(name, 5e-4) - central(name, 1e-3)) / 3.0
+        plain, plain2 = central(name, 1e-5), central(name, 1.25e-5)
+        den = max(abs(rich), 1e-3 * abs(val))
+        worst_rich = max(worst_rich, abs(grads[k] - rich) / den)
+        # the plain difference's distance from the adjoint is within a small multiple of its
+        # distance from the noise-free Richardson difference plus its own bump-to-bump spread
+        assert abs(grads[k] - plain) <= 2.0 * (abs(plain - rich) + abs(plain - plain2)) + 5e-7 * den, name
+    assert worst_rich < 5e-7

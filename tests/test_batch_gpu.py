@@ -161,9 +161,10 @@ def test_partition_autotuner_and_limits(lss):
 
 @pytest.mark.parametrize("mode", [0, 1])
 def test_cta_size_does_not_change_bits(lss, mode):
-    """Each line is solved by one thread whatever the CTA size, so every size the autotuner
-    may pick gives the same surfaces and values bit for bit; the parameter sensitivities are
-    sums over lines whose order follows the thread layout (rounding-level differences)."""
+    """Each line is solved by one thread whatever the number of warps on an instance, so every cap
+    the autotuner may pick gives the same surfaces and values bit for bit; the parameter
+    sensitivities are sums over lines whose order follows the thread layout (rounding-level
+    differences)."""
     from linear_system_solvers_gb300.batch import draw_batch
 
     probs = draw_batch(10, seed=77)
@@ -171,7 +172,7 @@ def test_cta_size_does_not_change_bits(lss, mode):
         p.nt = 15
     b = lss.BatchSolver(probs, precision="f64")
     ref = None
-    for threads in (32, 64, 128, 256):
+    for threads in (32, 64, 96, 128):
         assert b.autotune(mode=mode, threads=threads) == threads
         b.run(mode)
         v, g, _ = b.results()
@@ -182,4 +183,4 @@ def test_cta_size_does_not_change_bits(lss, mode):
             assert np.array_equal(v, ref[0])
             np.testing.assert_allclose(g, ref[1], rtol=1e-11, atol=1e-14)
             assert all(np.array_equal(a, c) for a, c in zip(surf, ref[2]))
-    assert b.autotune(mode=mode) in (32, 64, 128, 256)
+    assert b.autotune(mode=mode) in (32, 64, 128)
