@@ -532,9 +532,11 @@ def run_configs(args):
     if "c4" in wanted:
         run_config4()
     if "c5" in wanted:
+        # --max-time-steps caps the time loop (profiler captures of the large-grid kernels)
+        nt5 = min(1001, args.max_time_steps + 1) if args.max_time_steps else 1001
         for fp in ("f64", "f32"):
-            p = lss.HestonProblem(**dict(CONFIG1, scheme="hv", nx=4096, ny=2048, nt=1001, **NU_K100))
-            case("config5 HV 4096x2048x1000", p, fp, 1, oracle_nt=11)
+            p = lss.HestonProblem(**dict(CONFIG1, scheme="hv", nx=4096, ny=2048, nt=nt5, **NU_K100))
+            case(f"config5 HV 4096x2048x{nt5 - 1}", p, fp, 1, oracle_nt=min(11, nt5))
     if "euler" in wanted:
         # explicit Euler (explicit_solvers::general_heston_equation): 200 x 100, 8000 steps, T = 0.25
         p = lss.HestonProblem(**dict(CONFIG1, scheme="euler", nx=200, ny=100, nt=8001, maturity=0.25))

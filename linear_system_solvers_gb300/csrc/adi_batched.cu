@@ -486,6 +486,118 @@ __device__ __forceinline__ void v_stage(const inst_view<T> &v, const T *__restri
     }
 }
 
+// v-line sweep through shared-memory tiles.  The lines of a v sweep are rows of the row-major
+// state, so lane r of a warp reading its own row walks memory 8 * ny bytes away from its
+// neighbours: every load of the plain sweep touches 32 sectors.  Here the warp's 32 consecutive
+// lines (lane r owns line i0 + r) move through a per-warp tile of VT columns: the whole warp loads
+// `in` (VT + 2 columns, the window's halo included) and `inh`, and stores `out`, as a few
+// contiguous row segments per instruction; each lane then runs its line's recurrence from the
+// tile.  The per-line arithmetic is that of v_stage, operation for operation (same bits).
+constexpr int VT = 4;
+template <typename T> struct vtile {
+    T in[32][VT + 3]; // columns t-1 .. t+VT of `in` (odd row stride: conflict-free lane reads)
+    T io[32][VT + 1]; // `inh`, overwritten by the recurrence's values, stored to `out`
+};
+
+// Copies `cols` columns starting at column c0 of rows i0 .. i0+nrows-1 (row stride ny) between
+// global memory and the tile rows 0 .. nrows-1 (row stride W), all 32 lanes of the warp
+// cooperating (`lane`: this thread's lane in its warp).
+template <int W, int CMAX, bool LOAD, typename T>
+__device__ __forceinline__ void vtile_copy(T *tile, const T *src, T *dst, long long i0, int ny, int nrows, int c0,
+                                           int cols, int lane)
+{
+#pragma unroll
+    for (int q = 0; q < CMAX; ++q) {
+        const int idx = lane + 32 * q, r = idx / CMAX, c = idx % CMAX;
+        if (r < nrows && c < cols) {
+            const long long g = (i0 + r) * ny + c0 + c;
+            if constexpr (LOAD) tile[r * W + c] = src[g];
+            else dst[g] = tile[r * W + c];
+        }
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void v_lines_tiled(const inst_view<T> &v, const T *__restrict__ in, const T *__restrict__ inh,
+                                              const T *__restrict__ sb0, T *__restrict__ out, int i0, vtile<T> &tl)
+{
+    const int lane = threadIdx.x & 31; // one-dimensional blocks of whole warps
+    const int nx = v.nx, ny = v.ny, e = v.e_v;
+    const int i = i0 + lane;
+    const bool act = i <= nx - 2;
+    const int nrows = min(32, nx - 1 - i0);
+    T lo = T(0), hi = T(0), y = T(0);
+    if (act) {
+        const int ii = ldg(v.imap() + i);
+        lo = sb0[ii];
+        hi = ldg(v.X(X_VHI) + ii);
+        y = lo;
+    }
+    const T chv = act ? ldg(v.X(X_CHV) + i) : T(0);
+    // forward recurrence y_t = f_t - la_t y_{t-1}, tiles left to right
+    for (int tb = 1; tb <= e; tb += VT) {
+        const int kk = min(VT, e - tb + 1);
+        vtile_copy<VT + 3, VT + 2, true>(&tl.in[0][0], in, (T *)nullptr, i0, ny, nrows, tb - 1, kk + 2, lane);
+        vtile_copy<VT + 1, VT, true>(&tl.io[0][0], inh, (T *)nullptr, i0, ny, nrows, tb, kk, lane);
+        __syncwarp();
+        if (act) {
+#pragma unroll
+            for (int k = 0; k < VT; ++k) {
+                if (k < kk) {
+                    const int t = tb + k;
+                    const long long ot = (long long)t * nx + i;
+                    T f = ldg(v.Vt(VL_LA) + ot) * tl.in[lane][k];
+                    f += ldg(v.Vt(VL_VC) + ot) * tl.in[lane][k + 1];
+                    f += ldg(v.Vt(VL_VN) + ot) * tl.in[lane][k + 2];
+                    f += ldg(v.Vt(VL_IB) + ot) * tl.io[lane][k];
+                    y = f - ldg(v.Vt(VL_LA) + ot) * y;
+                    if (t == e) y -= chv * hi;
+                    tl.io[lane][k] = y;
+                }
+            }
+        }
+        __syncwarp();
+        vtile_copy<VT + 1, VT, false>(&tl.io[0][0], (const T *)nullptr, out, i0, ny, nrows, tb, kk, lane);
+        __syncwarp();
+    }
+    // back substitution x_t = y_t - g_t x_{t+1} (x_e = y_e), tiles right to left
+    T x = y;
+    for (int te = e - 1; te >= 1; te -= VT) {
+        const int kk = min(VT, te), ts = te - kk + 1;
+        vtile_copy<VT + 1, VT, true>(&tl.io[0][0], out, (T *)nullptr, i0, ny, nrows, ts, kk, lane);
+        __syncwarp();
+        if (act) {
+#pragma unroll
+            for (int k = VT - 1; k >= 0; --k) {
+                if (k < kk) {
+                    const int t = ts + k;
+                    x = tl.io[lane][k] - ldg(v.Vt(VL_G) + (long long)t * nx + i) * x;
+                    tl.io[lane][k] = x;
+                }
+            }
+        }
+        __syncwarp();
+        vtile_copy<VT + 1, VT, false>(&tl.io[0][0], (const T *)nullptr, out, i0, ny, nrows, ts, kk, lane);
+        __syncwarp();
+    }
+    if (act) {
+        const long long row = (long long)i * ny;
+        out[row] = lo;
+        out[row + ny - 1] = hi;
+    }
+}
+
+// v_stage through the warp tiles: the warp of lane (l0 mod 32) takes lines i0 = 1 + (l0 - lane),
+// i0 + ls, ... (ls a multiple of 32, all lanes of a warp in the same work split).
+template <typename T>
+__device__ __forceinline__ void v_stage_tiled(const inst_view<T> &v, const T *__restrict__ in, const T *__restrict__ inh,
+                                              const T *__restrict__ sb0, T *__restrict__ out, int l0, int ls,
+                                              vtile<T> &tl)
+{
+    const int nx = v.nx;
+    for (int i0 = 1 + (l0 & ~31); i0 <= nx - 2; i0 += ls) v_lines_tiled<T>(v, in, inh, sb0, out, i0, tl);
+}
+
 template <typename T> __device__ __forceinline__ inst_view<T> make_view(const bparams<T> &p, const bdesc &d)
 {
     inst_view<T> v;
@@ -503,23 +615,23 @@ template <typename T> __device__ __forceinline__ inst_view<T> make_view(const bp
 // One time step U -> Vn of scheme SCH with stage outputs in Y1, Y2, Y3; ends with a group barrier.
 template <typename T, int SCH>
 __device__ __forceinline__ void fwd_step(const inst_view<T> &v, const T *U, T *Y1, T *Y2, T *Y3, T *Vn, T *sb0,
-                                         double bnc, const grp &g)
+                                         double bnc, const grp &g, vtile<T> &tl)
 {
     const int l0 = g.t, ls = g.n;
     b1_stage<T>(v, U, sb0, bnc, l0, ls);
     s_stage<T, 1, SCH>(v, U, nullptr, nullptr, Y1, l0, ls);
     g.sync();
     if constexpr (SCH == LSS_ADI_DOUGLAS_RACHFORD) {
-        v_stage<T>(v, U, Y1, sb0, Vn, l0, ls);
+        v_stage_tiled<T>(v, U, Y1, sb0, Vn, l0, ls, tl);
     } else {
-        v_stage<T>(v, U, Y1, sb0, Y2, l0, ls);
+        v_stage_tiled<T>(v, U, Y1, sb0, Y2, l0, ls, tl);
         g.sync();
         s_stage<T, 2, SCH>(v, U, Y1, Y2, Y3, l0, ls);
         g.sync();
         if constexpr (SCH == LSS_ADI_HUNDSDORFER_VERWER)
-            v_stage<T>(v, Y2, Y3, sb0, Vn, l0, ls);
+            v_stage_tiled<T>(v, Y2, Y3, sb0, Vn, l0, ls, tl);
         else
-            v_stage<T>(v, U, Y3, sb0, Vn, l0, ls);
+            v_stage_tiled<T>(v, U, Y3, sb0, Vn, l0, ls, tl);
     }
     g.sync();
     b2_stage<T>(v, Vn, l0, ls);
@@ -536,7 +648,9 @@ __global__ void __launch_bounds__(BATCH_CTA, 8) k_batch_forward(const __grid_con
 {
     __shared__ int s_idx[MAX_GROUP_WARPS];
     __shared__ int s_bad[MAX_GROUP_WARPS];
+    __shared__ vtile<T> s_vt[MAX_GROUP_WARPS];
     const grp g = make_grp(p.layout[blockIdx.x]);
+    vtile<T> &tl = s_vt[threadIdx.x >> 5];
     int cls = g.n / 32;
     while (true) {
         if (g.t == 0) s_idx[g.gi] = next_instance(p, cls, -1);
@@ -549,7 +663,7 @@ __global__ void __launch_bounds__(BATCH_CTA, 8) k_batch_forward(const __grid_con
         T *U = p.U + d.o2, *Vn = p.V + d.o2, *Y1 = p.Y1 + d.o2, *Y2 = p.Y2 + d.o2, *Y3 = p.Y3 + d.o2;
         T *sb0 = p.B0 + d.ox;
         for (int step = 0; step < d.steps; ++step) {
-            fwd_step<T, SCH>(v, U, Y1, Y2, Y3, Vn, sb0, d.bnc, g);
+            fwd_step<T, SCH>(v, U, Y1, Y2, Y3, Vn, sb0, d.bnc, g, tl);
             T *tmp = U;
             U = Vn;
             Vn = tmp;
@@ -591,7 +705,9 @@ __global__ void __launch_bounds__(BATCH_CTA, LSS_FWDADJ_MIN_CTAS) k_batch_fwdadj
     __shared__ int s_idx[MAX_GROUP_WARPS];
     __shared__ int s_bad[MAX_GROUP_WARPS];
     __shared__ double red[MAX_GROUP_WARPS][5];
+    __shared__ vtile<double> s_vt[MAX_GROUP_WARPS];
     const grp g = make_grp(p.layout[blockIdx.x]);
+    vtile<double> &tl = s_vt[threadIdx.x >> 5];
     const int gw = g.n / 32;
     double *ws = p.ws + (long long)(blockIdx.x * MAX_GROUP_WARPS + g.warp0) * p.ws_per_warp;
     int cls = gw;
@@ -640,13 +756,13 @@ __global__ void __launch_bounds__(BATCH_CTA, LSS_FWDADJ_MIN_CTAS) k_batch_fwdadj
         for (int step = 0; step < d.steps; ++step) {
             if (step >= n0_last) {
                 const int m = step - n0_last;
-                fwd_step<double, SCH>(v, cur, slot(m, 1), slot(m, 2), slot(m, 3), slot(m + 1, 0), sb0, d.bnc, g);
+                fwd_step<double, SCH>(v, cur, slot(m, 1), slot(m, 2), slot(m, 3), slot(m + 1, 0), sb0, d.bnc, g, tl);
                 cur = slot(m + 1, 0);
                 continue;
             }
             double *next = ((step + 1) % c == 0 && step + 1 < d.steps) ? CK + (long long)((step + 1) / c) * n
                                                                         : ((step & 1) ? W1 : W0);
-            fwd_step<double, SCH>(v, cur, slot(0, 1), slot(0, 2), slot(0, 3), next, sb0, d.bnc, g);
+            fwd_step<double, SCH>(v, cur, slot(0, 1), slot(0, 2), slot(0, 3), next, sb0, d.bnc, g, tl);
             cur = next;
         }
         // value, finiteness, final surface
@@ -684,7 +800,7 @@ __global__ void __launch_bounds__(BATCH_CTA, LSS_FWDADJ_MIN_CTAS) k_batch_fwdadj
             const double *u0 = CK + (long long)sgi * n;
             for (int m = 0; m < L && sgi < nseg - 1; ++m) {
                 const double *um = (m == 0) ? u0 : slot(m, 0);
-                fwd_step<double, SCH>(v, um, slot(m, 1), slot(m, 2), slot(m, 3), slot(m + 1, 0), sb0, d.bnc, g);
+                fwd_step<double, SCH>(v, um, slot(m, 1), slot(m, 2), slot(m, 3), slot(m + 1, 0), sb0, d.bnc, g, tl);
             }
             for (int m = L - 1; m >= 0; --m) {
                 const double *um = (m == 0) ? u0 : slot(m, 0);
@@ -741,9 +857,10 @@ __global__ void k_wide_s(const __grid_constant__ bparams<T> p, const T *U, const
 }
 template <typename T> __global__ void k_wide_v(const __grid_constant__ bparams<T> p, const T *in, const T *inh, const T *b0, T *out)
 {
+    __shared__ vtile<T> s_vt[1]; // blocks of one warp
     const bdesc d = p.desc[0];
     const inst_view<T> v = make_view(p, d);
-    v_stage<T>(v, in, inh, b0, out, gtid(), gstride());
+    v_stage_tiled<T>(v, in, inh, b0, out, gtid(), gstride(), s_vt[0]);
 }
 template <typename T> __global__ void k_wide_b2(const __grid_constant__ bparams<T> p, T *Vn)
 {
@@ -849,42 +966,149 @@ __global__ void __launch_bounds__(1024) k_wide_s_chunk(const __grid_constant__ b
     }
 }
 
+// Copy between global memory and a warp's tile where each tile row r has its own global offset
+// and length: owner(r, off, cnt) gives them (cnt = 0 for rows without work); `lane`: this
+// thread's lane in its warp.
+template <int W, int CMAX, bool LOAD, typename T, typename F>
+__device__ __forceinline__ void vtile_copy_rows(T *tile, const T *src, T *dst, F owner, int lane)
+{
+#pragma unroll
+    for (int q = 0; q < CMAX; ++q) {
+        const int idx = lane + 32 * q, r = idx / CMAX, c = idx % CMAX;
+        long long off;
+        int cnt;
+        owner(r, off, cnt);
+        if (c < cnt) {
+            if constexpr (LOAD) tile[r * W + c] = src[off + c];
+            else dst[off + c] = tile[r * W + c];
+        }
+    }
+}
+
+// Partitioned v sweep (see k_wide_s_chunk) with the rows of `in`, `inh` and `out` moved through
+// per-warp shared-memory tiles (v_lines_tiled): the CTA's threads are (lines x chunks) with the
+// line index fastest, so a warp holds 32 / L chunks of L lines (or one chunk of 32 lines), each
+// lane its own line and chunk.  Every tile row is a contiguous segment of one state row; the
+// arithmetic per point is that of the thread-per-line recurrences, operation for operation.
+// The CTA must be whole warps (L * P a multiple of 32, set_wide_chunks).  Dynamic shared memory:
+// one vtile per warp.
 template <typename T>
 __global__ void __launch_bounds__(1024) k_wide_v_chunk(const __grid_constant__ bparams<T> p, const T *in, const T *inh,
                                                         const T *b0, T *out, const T *__restrict__ hf,
                                                         const T *__restrict__ hb)
 {
     __shared__ T sa[32][33], sb[32][33];
+    extern __shared__ unsigned char vt_raw[];
     const bdesc d = p.desc[0];
     const inst_view<T> v = make_view(p, d);
-    const int nx = d.nx, ny = d.ny, e = ny - 2, P = blockDim.y, c = threadIdx.y, lane = threadIdx.x;
-    const int i = 1 + blockIdx.x * blockDim.x + lane;
+    const int nx = d.nx, ny = d.ny, e = ny - 2, P = blockDim.y, c = threadIdx.y, lane = threadIdx.x, L = blockDim.x;
+    const int lin = c * L + lane, w = lin >> 5, wl = lin & 31;
+    vtile<T> &tl = reinterpret_cast<vtile<T> *>(vt_raw)[w];
+    const int i = 1 + blockIdx.x * L + lane;
     const bool act = i <= nx - 2;
     const long long row = (long long)i * ny;
     int t0, t1;
     chunk_range(e, P, c, t0, t1);
+    // tile row r of this warp: line and chunk of the warp's lane r
+    auto line_of = [&](int r, int &ir, int &cr) {
+        const int lr = (w << 5) + r;
+        cr = lr / L;
+        ir = 1 + blockIdx.x * L + lr % L;
+    };
+    const int steps = (t1 - t0 + VT) / VT; // tiles of this lane's chunk
+    int steps_max = steps;
+    for (int off = 16; off > 0; off >>= 1) steps_max = max(steps_max, __shfl_xor_sync(0xffffffffu, steps_max, off));
     T lo = T(0), hi = T(0);
     if (act) {
         const int ii = ldg(v.imap() + i);
         lo = b0[ii];
         hi = ldg(v.X(X_VHI) + ii);
-        sb[c][lane] = v_line_fwd<T>(v, in, inh, out, i, t0, t1, c == 0 ? lo : T(0), hi);
+    }
+    const T chv = act ? ldg(v.X(X_CHV) + i) : T(0);
+    // pass 1: local forward recurrence of the chunk (from lo on chunk 0, from 0 on the others)
+    T y = c == 0 ? lo : T(0);
+    for (int jt = 0; jt < steps_max; ++jt) {
+        auto own_in = [&](int r, long long &off, int &cnt) {
+            int ir, cr, a, b;
+            line_of(r, ir, cr);
+            chunk_range(e, P, cr, a, b);
+            const int tb = a + jt * VT, kk = min(VT, b - tb + 1);
+            cnt = (ir <= nx - 2 && kk > 0) ? kk + 2 : 0;
+            off = (long long)ir * ny + tb - 1;
+        };
+        auto own_h = [&](int r, long long &off, int &cnt) {
+            int ir, cr, a, b;
+            line_of(r, ir, cr);
+            chunk_range(e, P, cr, a, b);
+            const int tb = a + jt * VT, kk = min(VT, b - tb + 1);
+            cnt = (ir <= nx - 2 && kk > 0) ? kk : 0;
+            off = (long long)ir * ny + tb;
+        };
+        vtile_copy_rows<VT + 3, VT + 2, true>(&tl.in[0][0], in, (T *)nullptr, own_in, wl);
+        vtile_copy_rows<VT + 1, VT, true>(&tl.io[0][0], inh, (T *)nullptr, own_h, wl);
+        __syncwarp();
+        const int tb = t0 + jt * VT, kk = min(VT, t1 - tb + 1);
+        if (act) {
+#pragma unroll
+            for (int k = 0; k < VT; ++k) {
+                if (k < kk) {
+                    const int t = tb + k;
+                    const long long ot = (long long)t * nx + i;
+                    T f = ldg(v.Vt(VL_LA) + ot) * tl.in[wl][k];
+                    f += ldg(v.Vt(VL_VC) + ot) * tl.in[wl][k + 1];
+                    f += ldg(v.Vt(VL_VN) + ot) * tl.in[wl][k + 2];
+                    f += ldg(v.Vt(VL_IB) + ot) * tl.io[wl][k];
+                    y = f - ldg(v.Vt(VL_LA) + ot) * y;
+                    if (t == e) y -= chv * hi;
+                    tl.io[wl][k] = y;
+                }
+            }
+        }
+        __syncwarp();
+        vtile_copy_rows<VT + 1, VT, false>(&tl.io[0][0], (const T *)nullptr, out, own_h, wl);
+        __syncwarp();
+    }
+    if (act) {
+        sb[c][lane] = y;
         sa[c][lane] = hf[(long long)t1 * nx + i];
     }
     __syncthreads();
+    // pass 2: forward fix-up y += hf yin with the incoming value composed from the chunks before,
+    // fused with the chunk's back substitution from a zero start
+    T yin = T(0);
+    if (act && c > 0) {
+        yin = sb[0][lane];
+        for (int q = 1; q < c; ++q) yin = sb[q][lane] + sa[q][lane] * yin;
+    }
     T xh = T(0);
-    if (act) {
-        T yin = T(0);
-        if (c > 0) {
-            yin = sb[0][lane];
-            for (int q = 1; q < c; ++q) yin = sb[q][lane] + sa[q][lane] * yin;
+    for (int jt = 0; jt < steps_max; ++jt) {
+        // tiles from the chunk's end: columns [b - (jt+1) VT + 1, b - jt VT] clipped to the chunk
+        auto own_b = [&](int r, long long &off, int &cnt) {
+            int ir, cr, a, b;
+            line_of(r, ir, cr);
+            chunk_range(e, P, cr, a, b);
+            const int te = b - jt * VT, ts = max(a, te - VT + 1);
+            cnt = (ir <= nx - 2 && te >= a) ? te - ts + 1 : 0;
+            off = (long long)ir * ny + ts;
+        };
+        vtile_copy_rows<VT + 1, VT, true>(&tl.io[0][0], out, (T *)nullptr, own_b, wl);
+        __syncwarp();
+        const int te = t1 - jt * VT, ts = max(t0, te - VT + 1);
+        if (act && te >= t0) {
+#pragma unroll
+            for (int k = VT - 1; k >= 0; --k) {
+                if (k <= te - ts) {
+                    const int t = ts + k;
+                    const long long ot = (long long)t * nx + i;
+                    const T yv = (c > 0) ? tl.io[wl][k] + hf[ot] * yin : tl.io[wl][k];
+                    xh = yv - ldg(v.Vt(VL_G) + ot) * xh;
+                    tl.io[wl][k] = xh;
+                }
+            }
         }
-        for (int t = t1; t >= t0; --t) {
-            const long long ot = (long long)t * nx + i;
-            const T y = (c > 0) ? out[row + t] + hf[ot] * yin : out[row + t];
-            xh = y - ldg(v.Vt(VL_G) + ot) * xh;
-            out[row + t] = xh;
-        }
+        __syncwarp();
+        vtile_copy_rows<VT + 1, VT, false>(&tl.io[0][0], (const T *)nullptr, out, own_b, wl);
+        __syncwarp();
     }
     __syncthreads();
     if (act) {
@@ -892,12 +1116,34 @@ __global__ void __launch_bounds__(1024) k_wide_v_chunk(const __grid_constant__ b
         sa[c][lane] = hb[(long long)t0 * nx + i];
     }
     __syncthreads();
-    if (act) {
-        if (c < P - 1) {
-            T xin = sb[P - 1][lane];
-            for (int q = P - 2; q > c; --q) xin = sb[q][lane] + sa[q][lane] * xin;
-            for (int t = t0; t <= t1; ++t) out[row + t] += hb[(long long)t * nx + i] * xin;
+    // pass 3: backward fix-up x += hb xin (all chunks but the last)
+    T xin = T(0);
+    if (act && c < P - 1) {
+        xin = sb[P - 1][lane];
+        for (int q = P - 2; q > c; --q) xin = sb[q][lane] + sa[q][lane] * xin;
+    }
+    for (int jt = 0; jt < steps_max; ++jt) {
+        auto own_f = [&](int r, long long &off, int &cnt) {
+            int ir, cr, a, b;
+            line_of(r, ir, cr);
+            chunk_range(e, P, cr, a, b);
+            const int tb = a + jt * VT, kk = min(VT, b - tb + 1);
+            cnt = (ir <= nx - 2 && kk > 0 && cr < P - 1) ? kk : 0;
+            off = (long long)ir * ny + tb;
+        };
+        vtile_copy_rows<VT + 1, VT, true>(&tl.io[0][0], out, (T *)nullptr, own_f, wl);
+        __syncwarp();
+        const int tb = t0 + jt * VT, kk = min(VT, t1 - tb + 1);
+        if (act && c < P - 1) {
+#pragma unroll
+            for (int k = 0; k < VT; ++k)
+                if (k < kk) tl.io[wl][k] += hb[(long long)(tb + k) * nx + i] * xin;
         }
+        __syncwarp();
+        vtile_copy_rows<VT + 1, VT, false>(&tl.io[0][0], (const T *)nullptr, out, own_f, wl);
+        __syncwarp();
+    }
+    if (act) {
         if (c == 0) out[row] = lo;
         if (c == P - 1) out[row + ny - 1] = hi;
     }
@@ -1943,8 +2189,9 @@ void batch_typed<T>::launch_wide_v(cudaStream_t s, const bparams<T> &p, const T 
         k_wide_v<T><<<grid_for(d.nx - 2, 32), 32, 0, s>>>(p, in, inh, b0, out);
     } else {
         const long long n = total_n;
-        k_wide_v_chunk<T><<<grid_for(d.nx - 2, wide_lv), dim3(wide_lv, wide_pv), 0, s>>>(p, in, inh, b0, out, d_spk.p + 2 * n,
-                                                                               d_spk.p + 3 * n);
+        const size_t smem = sizeof(vtile<T>) * ((wide_lv * wide_pv) / 32);
+        k_wide_v_chunk<T><<<grid_for(d.nx - 2, wide_lv), dim3(wide_lv, wide_pv), smem, s>>>(p, in, inh, b0, out,
+                                                                                  d_spk.p + 2 * n, d_spk.p + 3 * n);
     }
 }
 
@@ -1974,6 +2221,14 @@ template <typename T> int batch_typed<T>::set_wide_chunks(int ps, int pv, cudaSt
     };
     wide_ls = (ls == 8 || ls == 16 || ls == 32) ? ls : lines_per_cta(d.ny - 2);
     wide_lv = (lv == 8 || lv == 16 || lv == 32) ? lv : lines_per_cta(d.nx - 2);
+    // the partitioned v sweep works in whole warps (shared-memory tiles moved by all 32 lanes):
+    // lines x chunks must be a multiple of 32, which 32 lines per CTA always are
+    if (pv > 1 && (wide_lv * pv) % 32 != 0) wide_lv = 32;
+    if (pv > 1) {
+        const int smem = static_cast<int>(sizeof(vtile<T>) * ((wide_lv * pv) / 32));
+        LSS_CUDA_TRY(cudaFuncSetAttribute(k_wide_v_chunk<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
+                     "wide: v-sweep tile memory");
+    }
     if (wide_graph) cudaGraphExecDestroy(wide_graph);
     wide_graph = nullptr;
     return LSS_ADI_OK;
