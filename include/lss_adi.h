@@ -152,8 +152,20 @@ typedef struct lss_adi_tables {
     const void *s_hi_neumann;   /* ny: transformed Neumann data dV/dzeta at S_hi (value * A(1)) */
     const void *v_hi_dirichlet; /* nx: V(S_i, v_hi) */
     const void *payoff;         /* nx*ny terminal/initial condition */
-    int options;                /* LSS_ADI_OPT_DOUBLE_SWEEP or 0 */
+    int options;                /* LSS_ADI_OPT_DOUBLE_SWEEP, LSS_ADI_OPT_STEP_TABLES or 0 */
 } lss_adi_tables;
+
+/* STEP_TABLES (options of lss_adi_tables): time-dependent coefficients and boundaries.  coef,
+ *   coef_v0, s_lo_dirichlet, s_hi_neumann and v_hi_dirichlet each hold nt - 1 consecutive blocks
+ *   of the sizes above, block s sampled at the time of step s -- the running time of
+ *   implicit_heston_time_loop::run (lss_2d_general_heston_equation_implicit_kernel.hpp:150-207):
+ *   t_hi - k, t_hi - 2k, ... backward, t_lo + k, t_lo + 2k, ... forward, each obtained from the
+ *   previous by one subtraction / addition of k in the solver type -- where the reference
+ *   evaluates its coefficient functions M(t, zeta, eta), ..., F(t, zeta, eta) and boundary values
+ *   (lss_2d_general_heston_equation_coefficients.hpp:31-40,89-98).  Runs the kernel-per-sweep
+ *   path (line systems factorised every step, as the reference does) in either arithmetic; not
+ *   for the explicit Euler scheme. */
+#define LSS_ADI_OPT_STEP_TABLES 16
 
 typedef struct lss_adi_handle lss_adi_handle;
 typedef struct lss_adi_batch lss_adi_batch;

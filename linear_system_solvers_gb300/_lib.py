@@ -22,6 +22,7 @@ OPT_FP64_TABLES = 1
 OPT_DOUBLE_SWEEP = 2
 OPT_LINE_PER_THREAD = 4
 OPT_WIDE_ADJOINT = 8
+OPT_STEP_TABLES = 16
 HESTON, SABR = 0, 1
 SCHEMES = {"dr": 0, "cs": 1, "mcs": 2, "hv": 3, "euler": 4}
 THETAS = {"euler": 0, "theta30": 1, "cn": 2, "theta80": 3}

@@ -278,7 +278,10 @@ namespace detail {
 // The user's coefficient functions transformed to the computational grid and sampled exactly as
 // the reference does (lss_heat_data_transform.hpp:174-214, coefficients.hpp:89-98), the
 // boundaries and the terminal condition on the grid, then the device time loop through
-// lss_adi_create_tabulated / lss_adi_forward.  Coefficients and boundaries must not depend on t.
+// lss_adi_create_tabulated / lss_adi_forward.  Coefficients and boundaries are sampled at every
+// step's time (the running time of implicit_heston_time_loop::run, implicit_kernel.hpp:150-207);
+// when any of them changes with t the device gets one block of tables per step
+// (LSS_ADI_OPT_STEP_TABLES), otherwise one.
 template <typename T>
 void tabulated_solve(heat_data_config_2d_ptr<T> const &data, pde_discretization_config_2d_ptr<T> const &disc,
                      lss_boundary::boundary_2d_ptr<T> const &ver, lss_boundary::boundary_2d_pair<T> const &hor,
@@ -347,24 +350,57 @@ void tabulated_solve(heat_data_config_2d_ptr<T> const &data, pde_discretization_
             }
         }
     };
-    std::vector<T> coef, v0, coef_last, v0_last;
-    fill(t_first, coef, v0);
-    fill(t_last, coef_last, v0_last);
-    if (coef != coef_last || v0 != v0_last)
-        throw std::invalid_argument("the device policy needs time-invariant coefficients");
+    (void)t_last;
     // boundaries on the computational grid (lss_heston_boundary_transform.hpp:47-65)
-    std::vector<T> slo(ny), neu(ny), vhi(nx), pay(n);
     const T A1 = Ad(one);
-    for (std::size_t j = 0; j < ny; ++j) {
-        const T y = Y(h2 * static_cast<T>(j));
-        slo[j] = hor.first->value(t_first, y);
-        neu[j] = hor.second->value(t_first, y) * A1;
-        if (slo[j] != hor.first->value(t_last, y) || hor.second->value(t_first, y) != hor.second->value(t_last, y))
-            throw std::invalid_argument("the device policy needs time-invariant boundary values");
+    auto fill_bnd = [&](T t, std::vector<T> &slo, std::vector<T> &neu, std::vector<T> &vhi) {
+        slo.resize(ny);
+        neu.resize(ny);
+        vhi.resize(nx);
+        for (std::size_t j = 0; j < ny; ++j) {
+            const T y = Y(h2 * static_cast<T>(j));
+            slo[j] = hor.first->value(t, y);
+            neu[j] = hor.second->value(t, y) * A1;
+        }
+        for (std::size_t i = 0; i < nx; ++i) vhi[i] = ver->value(t, X(h1 * static_cast<T>(i)));
+    };
+    // every step's tables; kept as one block while they all equal the first step's
+    const std::size_t steps = disc->number_of_time_points() - 1;
+    std::vector<T> coef, v0, slo, neu, vhi;
+    fill(t_first, coef, v0);
+    fill_bnd(t_first, slo, neu, vhi);
+    const std::vector<T> coef1 = coef, v01 = v0, slo1 = slo, neu1 = neu, vhi1 = vhi;
+    bool varies = false;
+    T ts = t_first;
+    std::vector<T> c2, w2, s2, n2, h2v;
+    for (std::size_t st = 1; st < steps; ++st) {
+        ts = fwd ? ts + k : ts - k;
+        fill(ts, c2, w2);
+        fill_bnd(ts, s2, n2, h2v);
+        if (!varies && (c2 != coef1 || w2 != v01 || s2 != slo1 || n2 != neu1 || h2v != vhi1)) {
+            varies = true;
+            for (std::size_t b = 1; b < st; ++b) { // the steps before were equal to the first
+                coef.insert(coef.end(), coef1.begin(), coef1.end());
+                v0.insert(v0.end(), v01.begin(), v01.end());
+                slo.insert(slo.end(), slo1.begin(), slo1.end());
+                neu.insert(neu.end(), neu1.begin(), neu1.end());
+                vhi.insert(vhi.end(), vhi1.begin(), vhi1.end());
+            }
+        }
+        if (varies) {
+            coef.insert(coef.end(), c2.begin(), c2.end());
+            v0.insert(v0.end(), w2.begin(), w2.end());
+            slo.insert(slo.end(), s2.begin(), s2.end());
+            neu.insert(neu.end(), n2.begin(), n2.end());
+            vhi.insert(vhi.end(), h2v.begin(), h2v.end());
+        }
     }
+    if (varies && scheme == LSS_ADI_EXPLICIT_EULER)
+        throw std::invalid_argument("the device explicit Euler scheme needs time-invariant coefficients and boundaries");
+    if (varies) options |= LSS_ADI_OPT_STEP_TABLES;
+    std::vector<T> pay(n);
     for (std::size_t i = 0; i < nx; ++i) {
         const T x = X(h1 * static_cast<T>(i));
-        vhi[i] = ver->value(t_first, x);
         for (std::size_t j = 0; j < ny; ++j) pay[i * ny + j] = data->initial->initial_condition(x, Y(h2 * static_cast<T>(j)));
     }
     lss_adi_tables t{};

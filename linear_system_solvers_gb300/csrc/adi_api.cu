@@ -130,7 +130,10 @@ int lss_adi_create_tabulated(const lss_adi_tables *t, lss_adi_handle **h)
     if (t->arith != LSS_ADI_ARITH_FAST && t->arith != LSS_ADI_ARITH_REFERENCE)
         return set_error(LSS_ADI_EINVAL, "lss_adi_create_tabulated: unknown arithmetic mode");
     if (!(t->t_hi > t->t_lo)) return set_error(LSS_ADI_EINVAL, "lss_adi_create_tabulated: empty time range");
-    if (t->options & ~LSS_ADI_OPT_DOUBLE_SWEEP) return set_error(LSS_ADI_EINVAL, "lss_adi_create_tabulated: unknown option bits");
+    if (t->options & ~(LSS_ADI_OPT_DOUBLE_SWEEP | LSS_ADI_OPT_STEP_TABLES))
+        return set_error(LSS_ADI_EINVAL, "lss_adi_create_tabulated: unknown option bits");
+    if ((t->options & LSS_ADI_OPT_STEP_TABLES) && t->scheme == LSS_ADI_EXPLICIT_EULER)
+        return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_create_tabulated: per-step tables are for the splitting schemes");
     std::unique_ptr<lss_adi_handle> hh(new (std::nothrow) lss_adi_handle());
     if (!hh) return set_error(LSS_ADI_ENOMEM, "host allocation failed");
     hh->precision = t->precision;

@@ -360,14 +360,20 @@ template <typename T> int plain_solver<T>::init(instance_tables<T> &&tab, int ar
     arith_ = arith;
     const int nx = tab_.nx, ny = tab_.ny;
     const size_t n = static_cast<size_t>(nx) * ny;
-    LSS_CUDA_TRY(coef_.alloc(7 * n), "allocating coefficient tables");
-    LSS_CUDA_TRY(coef_.upload(tab_.coef.data(), 7 * n), "uploading coefficient tables");
-    LSS_CUDA_TRY(small_.alloc(3 * nx + ny + ny + nx), "allocating boundary tables");
+    // one block of coefficient and boundary tables, or one per step (time-dependent tables)
+    const size_t blocks = tab_.step_tables ? static_cast<size_t>(tab_.steps) : 1;
+    const size_t sblk = 3 * static_cast<size_t>(nx) + ny + ny + nx;
+    LSS_CUDA_TRY(coef_.alloc(7 * n * blocks), "allocating coefficient tables");
+    LSS_CUDA_TRY(coef_.upload(tab_.coef.data(), 7 * n * blocks), "uploading coefficient tables");
+    LSS_CUDA_TRY(small_.alloc(sblk * blocks), "allocating boundary tables");
     std::vector<T> sm;
-    sm.insert(sm.end(), tab_.coef_v0.begin(), tab_.coef_v0.end());
-    sm.insert(sm.end(), tab_.s_lo.begin(), tab_.s_lo.end());
-    sm.insert(sm.end(), tab_.s_hi_neu.begin(), tab_.s_hi_neu.end());
-    sm.insert(sm.end(), tab_.v_hi.begin(), tab_.v_hi.end());
+    sm.reserve(sblk * blocks);
+    for (size_t b = 0; b < blocks; ++b) {
+        sm.insert(sm.end(), tab_.coef_v0.begin() + 3 * nx * b, tab_.coef_v0.begin() + 3 * nx * (b + 1));
+        sm.insert(sm.end(), tab_.s_lo.begin() + ny * b, tab_.s_lo.begin() + ny * (b + 1));
+        sm.insert(sm.end(), tab_.s_hi_neu.begin() + ny * b, tab_.s_hi_neu.begin() + ny * (b + 1));
+        sm.insert(sm.end(), tab_.v_hi.begin() + nx * b, tab_.v_hi.begin() + nx * (b + 1));
+    }
     LSS_CUDA_TRY(small_.upload(sm.data(), sm.size()), "uploading boundary tables");
     LSS_CUDA_TRY(maps_.alloc(nx + ny), "allocating index maps");
     std::vector<int> mp(tab_.imap);
@@ -447,7 +453,15 @@ template <typename T> template <bool X> void plain_solver<T>::enqueue_steps(cuda
         tt.half_rho_f = tab_.half_rho_f;
     }
     const int gref = grid_for(static_cast<long long>(nx) * ny, 256);
+    const size_t sblk = 3 * static_cast<size_t>(nx) + ny + ny + nx;
     for (int step = 0; step < tab_.steps; ++step) {
+        // the tables of this step (time-dependent tables: block `step`)
+        dev_instance<T> d_ = this->d_;
+        if (tab_.step_tables) {
+            const size_t oc = 7 * n * static_cast<size_t>(step), os = sblk * static_cast<size_t>(step);
+            d_.M += oc; d_.P += oc; d_.Z += oc; d_.Mt += oc; d_.Pt += oc; d_.W += oc; d_.C += oc;
+            d_.D0 += os; d_.E0 += os; d_.F0 += os; d_.s_lo += os; d_.s_hi_neu += os; d_.v_hi += os;
+        }
         if (tab_.tdep) {
             k_refresh<T, X><<<gref, 256, 0, s>>>(tt, nx, ny, tab_.step_da[step], tab_.step_dc[step]);
             launches_ += 1;

@@ -112,6 +112,9 @@ template <typename T> struct instance_tables {
     std::vector<T> payoff;         // nx*ny
     std::vector<T> x, y;           // physical grid
     T t_first{};                   // time of the first step
+    // Caller-sampled time-dependent tables (LSS_ADI_OPT_STEP_TABLES): coef, coef_v0, s_lo,
+    // s_hi_neu and v_hi hold one block per step, in step order.
+    int step_tables = 0;
     // Time-dependent coefficients (SABR with r != 0: a and c carry D(t)^(2(1-beta)) and
     // D(t)^(1-beta), D(t) = exp(-r (T - t))).  Each step re-evaluates M, P, Z, C and the
     // D line from the time-independent factors below, in the reference's operation order.
@@ -304,17 +307,19 @@ template <typename T> inline void build_tables(const lss_adi_tables &t, instance
     it.double_sweep = (t.options & LSS_ADI_OPT_DOUBLE_SWEEP) ? 1 : 0;
     it.sc = make_scalars<T>(t.nx, t.ny, t.nt, static_cast<T>(t.t_lo), static_cast<T>(t.t_hi), t.zeta, t.theta_scheme);
     const std::size_t n = static_cast<std::size_t>(t.nx) * t.ny;
+    it.step_tables = (t.options & LSS_ADI_OPT_STEP_TABLES) ? 1 : 0;
+    const std::size_t blocks = it.step_tables ? static_cast<std::size_t>(it.steps) : 1;
     const T *c = static_cast<const T *>(t.coef);
-    it.coef.assign(c, c + 7 * n);
+    it.coef.assign(c, c + 7 * n * blocks);
     const T *v0 = static_cast<const T *>(t.coef_v0);
-    it.coef_v0.assign(v0, v0 + 3 * static_cast<std::size_t>(t.nx));
+    it.coef_v0.assign(v0, v0 + 3 * static_cast<std::size_t>(t.nx) * blocks);
     const T *slo = static_cast<const T *>(t.s_lo_dirichlet);
-    it.s_lo.assign(slo, slo + t.ny);
+    it.s_lo.assign(slo, slo + static_cast<std::size_t>(t.ny) * blocks);
     const T *shi = static_cast<const T *>(t.s_hi_neumann);
-    it.s_hi_neu.assign(shi, shi + t.ny);
+    it.s_hi_neu.assign(shi, shi + static_cast<std::size_t>(t.ny) * blocks);
     it.neu = it.s_hi_neu[0];
     const T *vhi = static_cast<const T *>(t.v_hi_dirichlet);
-    it.v_hi.assign(vhi, vhi + t.nx);
+    it.v_hi.assign(vhi, vhi + static_cast<std::size_t>(t.nx) * blocks);
     const T *pay = static_cast<const T *>(t.payoff);
     it.payoff.assign(pay, pay + n);
     it.x.assign(t.nx, T(0));

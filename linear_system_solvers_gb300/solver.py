@@ -155,6 +155,9 @@ class TabulatedHestonSolver(ImplicitHestonSolver):
     coef: (7, nx, ny) M, P, Z, M~, P~, W, C; coef_v0: (3, nx) D, E, F on the v = v_lo line;
     s_lo: (ny,) Dirichlet values at S_lo; s_hi_neumann: (ny,) transformed Neumann data at S_hi;
     v_hi: (nx,) Dirichlet values at v_hi; payoff: (nx, ny).
+    Time-dependent coefficients or boundaries: coef (nt - 1, 7, nx, ny), coef_v0 (nt - 1, 3, nx),
+    s_lo / s_hi_neumann (nt - 1, ny), v_hi (nt - 1, nx), step s sampled at the time of step s
+    (t_hi - k, t_hi - 2k, ... backward; LSS_ADI_OPT_STEP_TABLES).
     """
 
     def __init__(self, nt, t_lo, t_hi, scheme, theta_scheme, coef, coef_v0, s_lo, s_hi_neumann, v_hi, payoff,
@@ -165,6 +168,9 @@ class TabulatedHestonSolver(ImplicitHestonSolver):
         arrs = [np.ascontiguousarray(a, dtype=self.dtype) for a in (coef, coef_v0, s_lo, s_hi_neumann, v_hi, payoff)]
         self._keep = arrs
         nx, ny = arrs[5].shape
+        step_tables = arrs[0].ndim == 4
+        if step_tables and arrs[0].shape[0] != nt - 1:
+            raise ValueError("per-step coefficient tables need nt - 1 blocks")
         self.problem = HestonProblem(nx=nx, ny=ny, nt=nt)
         t = L.LssAdiTables()
         t.nx, t.ny, t.nt = nx, ny, int(nt)
@@ -175,7 +181,7 @@ class TabulatedHestonSolver(ImplicitHestonSolver):
         t.precision = L.FP32 if precision == "f32" else L.FP64
         t.arith = L.ARITH_REFERENCE if arith == "reference" else L.ARITH_FAST
         t.zeta = float(zeta)
-        t.options = L.OPT_DOUBLE_SWEEP if solver == "ds" else 0
+        t.options = (L.OPT_DOUBLE_SWEEP if solver == "ds" else 0) | (L.OPT_STEP_TABLES if step_tables else 0)
         t.coef, t.coef_v0, t.s_lo_dirichlet, t.s_hi_neumann, t.v_hi_dirichlet, t.payoff = [a.ctypes.data for a in arrs]
         h = ctypes.c_void_p()
         L.check(self.lib.lss_adi_create_tabulated(ctypes.byref(t), ctypes.byref(h)))

@@ -5,11 +5,17 @@
 //
 // usage: heston_front_end_t <f32|f64> <dr|cs|mcs|hv> nx ny nt kappa theta sigma rho rate
 //        strike maturity s_lo s_hi v_lo v_hi zeta theta_scheme nonuniform acc alpha_s beta_s
-//        arith(0 fast|1 reference) builder(0|1) method(tlu|ds|euler) out.bin
+//        arith(0 fast|1 reference) builder(0|1) method(tlu|ds|euler) out.bin [sabr:<beta>]
 // method: tridiagonal_method_enum::GB300ThomasLUSolver / GB300DoubleSweepSolver, or the
 // explicit_solvers::general_heston_equation with the device explicit Euler scheme.
+// sabr:<beta>: the SABR model of unit_tests/common/lss_print_t.hpp:2039-2050 instead (sigma is nu,
+// F in place of S, alpha in place of v), whose coefficients change with t through the discount
+// factor D(t) = exp(-r (T - t)) when r != 0: the front end then hands the device one block of
+// tables per step.
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <functional>
 #include <string>
 
 #include "lss_gb300_heston.hpp"
@@ -54,12 +60,34 @@ template <typename T> static int run(int argc, char **argv)
     range<T> time_range(static_cast<T>(0.0), static_cast<T>(maturity));
     auto const discretization_ptr =
         std::make_shared<pde_discretization_config_2d<T>>(spacex_range, spacey_range, Sd, Vd, time_range, Td);
-    auto a = [=](T t, T s, T v) { return (0.5 * v * s * s); };
-    auto b = [=](T t, T s, T v) { return (0.5 * sig_sig * sig_sig * v); };
-    auto c = [=](T t, T s, T v) { return (rho * sig_sig * v * s); };
-    auto d = [=](T t, T s, T v) { return (rate * s); };
-    auto e = [=](T t, T s, T v) { return (sig_kappa * (sig_theta - v)); };
-    auto f = [=](T t, T s, T v) { return (-rate); };
+    const std::string model = argc > 27 ? argv[27] : "heston";
+    const bool sabr = model.rfind("sabr:", 0) == 0;
+    const double beta = sabr ? std::atof(model.c_str() + 5) : 0.0;
+    std::function<T(T, T, T)> a = [=](T t, T s, T v) { return (0.5 * v * s * s); };
+    std::function<T(T, T, T)> b = [=](T t, T s, T v) { return (0.5 * sig_sig * sig_sig * v); };
+    std::function<T(T, T, T)> c = [=](T t, T s, T v) { return (rho * sig_sig * v * s); };
+    std::function<T(T, T, T)> d = [=](T t, T s, T v) { return (rate * s); };
+    std::function<T(T, T, T)> e = [=](T t, T s, T v) { return (sig_kappa * (sig_theta - v)); };
+    std::function<T(T, T, T)> f = [=](T t, T s, T v) { return (-rate); };
+    if (sabr) {
+        // double arithmetic, evaluated left to right as the reference's lambdas
+        a = [=](T t, T s, T v) {
+            const double D = std::exp(-rate * (maturity - static_cast<double>(t)));
+            return static_cast<T>(0.5 * static_cast<double>(v) * static_cast<double>(v) *
+                                  std::pow(static_cast<double>(s), 2.0 * beta) * std::pow(D, 2.0 * (1.0 - beta)));
+        };
+        b = [=](T t, T s, T v) {
+            return static_cast<T>(0.5 * sig_sig * sig_sig * static_cast<double>(v) * static_cast<double>(v));
+        };
+        c = [=](T t, T s, T v) {
+            const double D = std::exp(-rate * (maturity - static_cast<double>(t)));
+            return static_cast<T>(rho * sig_sig * static_cast<double>(v) * static_cast<double>(v) *
+                                  std::pow(static_cast<double>(s), beta) * std::pow(D, (1.0 - beta)));
+        };
+        d = [=](T t, T s, T v) { return static_cast<T>(rate * static_cast<double>(s)); };
+        e = [=](T t, T s, T v) { return static_cast<T>(0.0); };
+        f = [=](T t, T s, T v) { return static_cast<T>(-rate); };
+    }
     auto const heat_coeffs_data_ptr = std::make_shared<heat_coefficient_data_config_2d<T>>(a, b, c, d, e, f);
     auto terminal_condition = [=](T s, T v) { return std::max<T>(0.0, s - strike); };
     auto const heat_init_data_ptr = std::make_shared<heat_initial_data_config_2d<T>>(terminal_condition);
@@ -124,7 +152,7 @@ template <typename T> static int run(int argc, char **argv)
 
 int main(int argc, char **argv)
 {
-    if (argc != 27) {
+    if (argc != 27 && argc != 28) {
         std::fprintf(stderr, "heston_front_end_t: expected 26 arguments, got %d\n", argc - 1);
         return 2;
     }

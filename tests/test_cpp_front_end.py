@@ -32,7 +32,7 @@ def test_front_end_compiles_against_the_c_abi(front_end_binary):
     assert res.returncode == 2 and "expected 26 arguments" in res.stderr
 
 
-def run_front_end(binary, kw, fp, arith, builder, method="tlu"):
+def run_front_end(binary, kw, fp, arith, builder, method="tlu", model=None):
     thetas = {"euler": 0, "theta30": 1, "cn": 2, "theta80": 3}
     with tempfile.TemporaryDirectory() as td:
         out = os.path.join(td, "v.bin")
@@ -43,6 +43,8 @@ def run_front_end(binary, kw, fp, arith, builder, method="tlu"):
                  str(int(kw.get("nonuniform", False))), repr(float(kw.get("acc_point", 0.0))),
                  repr(float(kw.get("alpha_scale", 3.0))), repr(float(kw.get("beta_scale", 50.0))), str(arith),
                  str(builder), method, out]
+        if model:
+            args.append(model)
         res = subprocess.run(args, capture_output=True, text=True)
         assert res.returncode == 0, res.stderr
         dt = np.float32 if fp == "f32" else np.float64
@@ -89,3 +91,26 @@ def test_front_end_explicit_euler_bitwise(front_end_binary, oracle, fp):
     got = run_front_end(front_end_binary, kw, fp, arith=1, builder=0, method="euler")
     want = oracle.solve(oracle.Problem(**kw), fp)
     assert np.array_equal(got, want, equal_nan=True)
+
+
+SABR_T = dict(model="sabr", kappa=0.0, theta_v=0.0, sigma=0.4, rho=-0.3, sabr_beta=0.5, rate=0.03, strike=0.05,
+              maturity=1.0, s_lo=0.0, s_hi=0.2, v_lo=0.0, v_hi=1.0, nonuniform=True, acc_point=0.05, alpha_scale=10.0,
+              beta_scale=24.0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("scheme,fp,arith", [("dr", "f64", 1), ("mcs", "f64", 1), ("hv", "f32", 1), ("cs", "f64", 0)])
+def test_front_end_time_dependent_user_lambdas(front_end_binary, oracle, scheme, fp, arith):
+    """Coefficient lambdas that change with t (SABR with r != 0: D(t) = exp(-r (T - t)) inside a and
+    c) through the reference's general_heston_equation interface: the front end samples them at
+    every step's time and the device runs one block of tables per step.  Reference arithmetic is
+    bit-identical to the oracle (the reference's own SABR path); the FMA arithmetic within 1e-10."""
+    from conftest import rel_err
+
+    kw = dict(SABR_T, scheme=scheme, nx=40, ny=22, nt=26)
+    got = run_front_end(front_end_binary, kw, fp, arith=arith, builder=0, model=f"sabr:{kw['sabr_beta']}")
+    want = oracle.solve(oracle.Problem(**kw), fp)
+    if arith == 1:
+        assert np.array_equal(got, want, equal_nan=True), rel_err(got, want)
+    else:
+        assert rel_err(got, want) < 1e-10
