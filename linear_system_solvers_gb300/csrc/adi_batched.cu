@@ -2225,7 +2225,9 @@ template <typename T> int batch_typed<T>::set_wide_chunks(int ps, int pv, cudaSt
     // lines x chunks must be a multiple of 32, which 32 lines per CTA always are
     if (pv > 1 && (wide_lv * pv) % 32 != 0) wide_lv = 32;
     if (pv > 1) {
-        const int smem = static_cast<int>(sizeof(vtile<T>) * ((wide_lv * pv) / 32));
+        // the limit belongs to the kernel, shared by every solver of the process: set it to what a
+        // 1024-thread CTA needs, so that no solver lowers it under another one's launches
+        const int smem = static_cast<int>(sizeof(vtile<T>) * 32);
         LSS_CUDA_TRY(cudaFuncSetAttribute(k_wide_v_chunk<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
                      "wide: v-sweep tile memory");
     }

@@ -269,3 +269,37 @@ def test_plain_central_difference_error_is_the_difference_own_noise(lss, oracle)
         # distance from the noise-free Richardson difference plus its own bump-to-bump spread
         assert abs(grads[k] - plain) <= 2.0 * (abs(plain - rich) + abs(plain - plain2)) + 5e-7 * den, name
     assert worst_rich < 5e-7
+
+
+def test_workspace_cap_is_honoured_and_results_do_not_depend_on_it(lss):
+    """lss_adi_batch_set_workspace bounds the forward + adjoint workspace: a tight cap holds less
+    memory and recomputes more (shorter checkpoint intervals), the results stay the same --
+    values and dV/d(initial condition) bit for bit, the parameter sums at rounding level (their
+    order follows the warp groups)."""
+    from linear_system_solvers_gb300.batch import draw_batch
+
+    probs = draw_batch(20, seed=11)
+    for p in probs:
+        p.nt = 41
+    b = lss.BatchSolver(probs, precision="f64")
+    b.set_workspace(0.0)  # default: a quarter of the device memory
+    b.run(1)
+    v_big, g_big, _ = b.results()
+    ck_big = b.checkpoints()
+    lam_big = [b.payoff_gradient(k) for k in (0, 7)]
+    cap = 64e6
+    b.set_workspace(cap)
+    b.run(1)
+    assert 0 < b.workspace_bytes() <= cap
+    v_small, g_small, _ = b.results()
+    ck_small = b.checkpoints()
+    assert (ck_small <= ck_big).all() and (ck_small < ck_big).any()
+    assert np.array_equal(v_small, v_big)
+    np.testing.assert_allclose(g_small, g_big, rtol=1e-12, atol=1e-14)
+    for k, lam in zip((0, 7), lam_big):
+        assert np.array_equal(b.payoff_gradient(k), lam)
+    from linear_system_solvers_gb300 import _lib as L
+
+    b.set_workspace(1e3)  # cannot hold the checkpoints of one instance
+    with pytest.raises(L.LssError):
+        b.run(1)

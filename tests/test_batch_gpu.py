@@ -184,3 +184,22 @@ def test_cta_size_does_not_change_bits(lss, mode):
             np.testing.assert_allclose(g, ref[1], rtol=1e-11, atol=1e-14)
             assert all(np.array_equal(a, c) for a, c in zip(surf, ref[2]))
     assert b.autotune(mode=mode) in (32, 64, 128)
+
+
+def test_batch_with_a_member_larger_than_256_rows(lss, oracle):
+    """A batch may mix small instances with one of more than 256 S points (no fixed per-instance
+    shared array): every member matches the single-instance fast path and the oracle."""
+    from linear_system_solvers_gb300.batch import draw_batch
+
+    probs = draw_batch(5, seed=21)
+    for p in probs:
+        p.nt = 13
+    probs[2].nx, probs[2].ny = 300, 40
+    b = lss.BatchSolver(probs, precision="f64")
+    b.run(0)
+    vals, _, status = b.results()
+    for k, p in enumerate(probs):
+        want = oracle.solve(oracle_of(oracle, p), "f64")
+        got = b.surface(k)
+        assert status[k] == 0
+        assert rel_err(got, want) < fp64_tol(want, p.s_hi)
