@@ -277,6 +277,15 @@ template <typename T> struct inst_view {
 
 template <typename T> __device__ __forceinline__ T ldg(const T *p) { return __ldg(p); }
 
+// Rows ahead that the line sweeps prefetch into L2 (0: none, the default).  Every access of a
+// sweep is known in advance (row t + PF of each table and state array), so a prefetch turns a
+// DRAM-latency load into an L2 hit without holding registers.  Addresses stay inside the
+// instance's arrays.
+#ifndef LSS_PREFETCH_ROWS
+#define LSS_PREFETCH_ROWS 0
+#endif
+__device__ __forceinline__ void pf_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
 // boundary#1: the v = v_lo column, explicit (explicit_boundary.hpp:39-84); result in smem
 // Work distribution of every stage: items l0, l0 + ls, ... (threads of one CTA in the
 // batched kernel; all threads of a grid in the per-stage kernels of the wide path).
@@ -335,6 +344,12 @@ __device__ __forceinline__ T s_line_fwd(const inst_view<T> &v, const T *__restri
 #pragma unroll 4
         for (int t = t0; t <= t1; ++t) {
             const long long o = (long long)t * ny + j;
+            if constexpr (LSS_PREFETCH_ROWS > 0) {
+                const long long of = (long long)min(t + LSS_PREFETCH_ROWS, e) * ny + j;
+                pf_l2(U + of + ny);
+                pf_l2(v.S(SL_WG) + of); pf_l2(v.S(SL_WW) + of); pf_l2(v.S(SL_WS) + of); pf_l2(v.S(SL_WC) + of);
+                pf_l2(v.S(SL_WN) + of); pf_l2(v.S(SL_WE) + of); pf_l2(v.S(SL_LA) + of);
+            }
             const T u2m = U[o + ny - 1], u2c = U[o + ny], u2p = U[o + ny + 1];
             const T q2 = u2m - u2p;
             const T mix = q0 - q2;
@@ -364,6 +379,16 @@ __device__ __forceinline__ T s_line_fwd(const inst_view<T> &v, const T *__restri
 #pragma unroll 4
         for (int t = t0; t <= t1; ++t) {
             const long long o = (long long)t * ny + j;
+            if constexpr (LSS_PREFETCH_ROWS > 0) {
+                const long long of = (long long)min(t + LSS_PREFETCH_ROWS, e) * ny + j;
+                pf_l2(U + of + ny); pf_l2(Y1 + of + ny); pf_l2(Y2 + of + ny);
+                pf_l2(v.S(SL_LA) + of); pf_l2(v.S(SL_S2SC) + of); pf_l2(v.S(SL_S2SE) + of); pf_l2(v.S(SL_S2MZ) + of);
+                if constexpr (hv || !xt) pf_l2(v.S(SL_S2IB) + of);
+                if constexpr (xt) {
+                    pf_l2(v.S(SL_X1) + of); pf_l2(v.S(SL_X2) + of); pf_l2(v.S(SL_X3) + of);
+                    pf_l2(v.S(SL_X4) + of); pf_l2(v.S(SL_X5) + of);
+                }
+            }
             const T uc2 = U[o + ny];
             const T d2m = Y2[o + ny - 1] - U[o + ny - 1];
             const T d2p = Y2[o + ny + 1] - U[o + ny + 1];
@@ -421,6 +446,7 @@ __device__ __forceinline__ void s_stage(const inst_view<T> &v, const T *__restri
 #pragma unroll 4
         for (int t = e - 1; t >= 1; --t) {
             const long long o = (long long)t * ny + j;
+            if constexpr (LSS_PREFETCH_ROWS > 0) pf_l2(v.S(SL_G) + (long long)max(t - LSS_PREFETCH_ROWS, 1) * ny + j);
             x = Y[o] - ldg(v.S(SL_G) + o) * x;
             Y[o] = x;
         }
@@ -541,6 +567,10 @@ __device__ __forceinline__ void v_lines_tiled(const inst_view<T> &v, const T *__
         vtile_copy<VT + 1, VT, true>(&tl.io[0][0], inh, (T *)nullptr, i0, ny, nrows, tb, kk, lane);
         __syncwarp();
         if (act) {
+            if constexpr (LSS_PREFETCH_ROWS > 0) {
+                const long long of = (long long)min(tb + VT + LSS_PREFETCH_ROWS, e) * nx + i;
+                pf_l2(v.Vt(VL_LA) + of); pf_l2(v.Vt(VL_VC) + of); pf_l2(v.Vt(VL_VN) + of); pf_l2(v.Vt(VL_IB) + of);
+            }
 #pragma unroll
             for (int k = 0; k < VT; ++k) {
                 if (k < kk) {
