@@ -29,22 +29,22 @@ sys.path.insert(0, ROOT)
 SEED = 20261203
 METRIC = "grid-point-steps/s, batched fwd+adjoint vs plain path, FP64 \u22641e-10 rel err"
 BYTES_PER_GPS_FWD = {"dr": 40, "cs": 96, "mcs": 96, "hv": 96}  # algorithmic bytes per grid-point-step (FP64)
-# DRAM bytes (read + write) per grid-point-step of the batched kernels from one ncu capture of
-# the 512-instance, 20-step case (--count 512 --max-time-steps 20), scaled to a launch by the
-# grid-point-steps it processes: mode 0 = k_batch_forward, mode 1 = k_batch_fwdadj (that capture
-# recomputes nothing: its 20-step loops fit one checkpoint segment)
-DRAM_BYTES_PER_GPS = {0: 303.0, 1: 821.0}
-# FP64 instructions (DFMA + DADD + DMUL, thread level) per grid-point-step from an ncu capture of
-# the same 512-instance, 20-step case taken while the checkpoint interval was still
-# ceil(sqrt(steps)) (smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum), and the
-# FP64 pipe's rate:
-# 1.196 TFLOP/s of DFMA measured on this GPU model = 5.98e11 FP64 instructions/s.
-# Forward + adjoint = one forward pass, the recomputation of every checkpoint segment but the
-# last (a fraction rf of the steps, from the workload) and the adjoint steps:
-# FP64_FWD * (1 + rf) + FP64_ADJ; the capture (20 steps, 4 segments of 5: rf = 0.75) counted
-# 169.1, so FP64_ADJ = 169.1 - 34.7 * 1.75.
-FP64_INSTR_FWD = 34.7
-FP64_INSTR_ADJ = 169.1 - 34.7 * 1.75
+# Figures of one ncu capture each of the batched kernels on the 1024-instance, 40-step case
+# (--count 1024 --max-time-steps 40; forward: --mode fwd; forward + adjoint: --mode fwdadj
+# --workspace-gb 12, whose plan recomputes a fraction CAPTURE_RF = 0.4898 of the steps), per
+# grid-point-step, scaled to a launch by the grid-point-steps it processes:
+# DRAM bytes read + written (dram__bytes_read.sum + dram__bytes_write.sum), mode 0 =
+# k_batch_forward, mode 1 = k_batch_fwdadj
+DRAM_BYTES_PER_GPS = {0: 340.9, 1: 1036.1}
+# FP64 instructions, thread level (smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum):
+# the forward kernel counted FP64_INSTR_FWD per grid-point-step; forward + adjoint is one forward
+# pass, the recomputation of every checkpoint segment but the last (a fraction rf of the steps)
+# and the adjoint steps, FP64_INSTR_FWD * (1 + rf) + FP64_INSTR_ADJ, and its capture counted
+# CAPTURE_FWDADJ at rf = CAPTURE_RF.
+FP64_INSTR_FWD = 34.0
+CAPTURE_RF = 0.4898
+CAPTURE_FWDADJ = 142.17
+FP64_INSTR_ADJ = CAPTURE_FWDADJ - FP64_INSTR_FWD * (1.0 + CAPTURE_RF)
 FP64_INSTR_PEAK = 5.98e11  # used only where the live probe below cannot run
 
 
@@ -417,7 +417,7 @@ def main():
                                    if world > 1 else "single GPU")},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": DRAM_BYTES_PER_GPS[mode] * gps, "traffic_unit": "bytes per launch",
-                     "traffic_source": "ncu dram__bytes_read+write of the 512-instance 20-step capture, per "
+                     "traffic_source": "ncu dram__bytes_read+write of the 1024-instance 40-step capture, per "
                                        "grid-point-step, times this launch's grid-point-steps", "peak_source": peak_kind,
                      "algorithmic_bytes_per_grid_point_step": bpg,
                      "note": "FP64 pipe (1.196 TFLOP/s measured) binds before HBM on GB300"},

@@ -645,23 +645,23 @@ template <typename T> __device__ __forceinline__ inst_view<T> make_view(const bp
 // One time step U -> Vn of scheme SCH with stage outputs in Y1, Y2, Y3; ends with a group barrier.
 template <typename T, int SCH>
 __device__ __forceinline__ void fwd_step(const inst_view<T> &v, const T *U, T *Y1, T *Y2, T *Y3, T *Vn, T *sb0,
-                                         double bnc, const grp &g, vtile<T> &tl)
+                                         double bnc, const grp &g)
 {
     const int l0 = g.t, ls = g.n;
     b1_stage<T>(v, U, sb0, bnc, l0, ls);
     s_stage<T, 1, SCH>(v, U, nullptr, nullptr, Y1, l0, ls);
     g.sync();
     if constexpr (SCH == LSS_ADI_DOUGLAS_RACHFORD) {
-        v_stage_tiled<T>(v, U, Y1, sb0, Vn, l0, ls, tl);
+        v_stage<T>(v, U, Y1, sb0, Vn, l0, ls);
     } else {
-        v_stage_tiled<T>(v, U, Y1, sb0, Y2, l0, ls, tl);
+        v_stage<T>(v, U, Y1, sb0, Y2, l0, ls);
         g.sync();
         s_stage<T, 2, SCH>(v, U, Y1, Y2, Y3, l0, ls);
         g.sync();
         if constexpr (SCH == LSS_ADI_HUNDSDORFER_VERWER)
-            v_stage_tiled<T>(v, Y2, Y3, sb0, Vn, l0, ls, tl);
+            v_stage<T>(v, Y2, Y3, sb0, Vn, l0, ls);
         else
-            v_stage_tiled<T>(v, U, Y3, sb0, Vn, l0, ls, tl);
+            v_stage<T>(v, U, Y3, sb0, Vn, l0, ls);
     }
     g.sync();
     b2_stage<T>(v, Vn, l0, ls);
@@ -678,9 +678,7 @@ __global__ void __launch_bounds__(BATCH_CTA, 8) k_batch_forward(const __grid_con
 {
     __shared__ int s_idx[MAX_GROUP_WARPS];
     __shared__ int s_bad[MAX_GROUP_WARPS];
-    __shared__ vtile<T> s_vt[MAX_GROUP_WARPS];
     const grp g = make_grp(p.layout[blockIdx.x]);
-    vtile<T> &tl = s_vt[threadIdx.x >> 5];
     int cls = g.n / 32;
     while (true) {
         if (g.t == 0) s_idx[g.gi] = next_instance(p, cls, -1);
@@ -693,7 +691,7 @@ __global__ void __launch_bounds__(BATCH_CTA, 8) k_batch_forward(const __grid_con
         T *U = p.U + d.o2, *Vn = p.V + d.o2, *Y1 = p.Y1 + d.o2, *Y2 = p.Y2 + d.o2, *Y3 = p.Y3 + d.o2;
         T *sb0 = p.B0 + d.ox;
         for (int step = 0; step < d.steps; ++step) {
-            fwd_step<T, SCH>(v, U, Y1, Y2, Y3, Vn, sb0, d.bnc, g, tl);
+            fwd_step<T, SCH>(v, U, Y1, Y2, Y3, Vn, sb0, d.bnc, g);
             T *tmp = U;
             U = Vn;
             Vn = tmp;
@@ -735,9 +733,7 @@ __global__ void __launch_bounds__(BATCH_CTA, LSS_FWDADJ_MIN_CTAS) k_batch_fwdadj
     __shared__ int s_idx[MAX_GROUP_WARPS];
     __shared__ int s_bad[MAX_GROUP_WARPS];
     __shared__ double red[MAX_GROUP_WARPS][5];
-    __shared__ vtile<double> s_vt[MAX_GROUP_WARPS];
     const grp g = make_grp(p.layout[blockIdx.x]);
-    vtile<double> &tl = s_vt[threadIdx.x >> 5];
     const int gw = g.n / 32;
     double *ws = p.ws + (long long)(blockIdx.x * MAX_GROUP_WARPS + g.warp0) * p.ws_per_warp;
     int cls = gw;
@@ -786,13 +782,13 @@ __global__ void __launch_bounds__(BATCH_CTA, LSS_FWDADJ_MIN_CTAS) k_batch_fwdadj
         for (int step = 0; step < d.steps; ++step) {
             if (step >= n0_last) {
                 const int m = step - n0_last;
-                fwd_step<double, SCH>(v, cur, slot(m, 1), slot(m, 2), slot(m, 3), slot(m + 1, 0), sb0, d.bnc, g, tl);
+                fwd_step<double, SCH>(v, cur, slot(m, 1), slot(m, 2), slot(m, 3), slot(m + 1, 0), sb0, d.bnc, g);
                 cur = slot(m + 1, 0);
                 continue;
             }
             double *next = ((step + 1) % c == 0 && step + 1 < d.steps) ? CK + (long long)((step + 1) / c) * n
                                                                         : ((step & 1) ? W1 : W0);
-            fwd_step<double, SCH>(v, cur, slot(0, 1), slot(0, 2), slot(0, 3), next, sb0, d.bnc, g, tl);
+            fwd_step<double, SCH>(v, cur, slot(0, 1), slot(0, 2), slot(0, 3), next, sb0, d.bnc, g);
             cur = next;
         }
         // value, finiteness, final surface
@@ -830,7 +826,7 @@ __global__ void __launch_bounds__(BATCH_CTA, LSS_FWDADJ_MIN_CTAS) k_batch_fwdadj
             const double *u0 = CK + (long long)sgi * n;
             for (int m = 0; m < L && sgi < nseg - 1; ++m) {
                 const double *um = (m == 0) ? u0 : slot(m, 0);
-                fwd_step<double, SCH>(v, um, slot(m, 1), slot(m, 2), slot(m, 3), slot(m + 1, 0), sb0, d.bnc, g, tl);
+                fwd_step<double, SCH>(v, um, slot(m, 1), slot(m, 2), slot(m, 3), slot(m + 1, 0), sb0, d.bnc, g);
             }
             for (int m = L - 1; m >= 0; --m) {
                 const double *um = (m == 0) ? u0 : slot(m, 0);
@@ -885,12 +881,19 @@ __global__ void k_wide_s(const __grid_constant__ bparams<T> p, const T *U, const
     const inst_view<T> v = make_view(p, d);
     with_scheme(d.scheme, [&](auto sch) { s_stage<T, KIND, decltype(sch)::value>(v, U, Y1, Y2, Y, gtid(), gstride()); });
 }
-template <typename T> __global__ void k_wide_v(const __grid_constant__ bparams<T> p, const T *in, const T *inh, const T *b0, T *out)
+// thread-per-line v sweep of the wide path, rows through shared-memory tiles (TILED) or read in
+// place; the two give the same bits, the autotuner keeps the faster for the instance
+template <typename T, bool TILED>
+__global__ void k_wide_v(const __grid_constant__ bparams<T> p, const T *in, const T *inh, const T *b0, T *out)
 {
-    __shared__ vtile<T> s_vt[1]; // blocks of one warp
     const bdesc d = p.desc[0];
     const inst_view<T> v = make_view(p, d);
-    v_stage_tiled<T>(v, in, inh, b0, out, gtid(), gstride(), s_vt[0]);
+    if constexpr (TILED) {
+        __shared__ vtile<T> s_vt[1]; // blocks of one warp
+        v_stage_tiled<T>(v, in, inh, b0, out, gtid(), gstride(), s_vt[0]);
+    } else {
+        v_stage<T>(v, in, inh, b0, out, gtid(), gstride());
+    }
 }
 template <typename T> __global__ void k_wide_b2(const __grid_constant__ bparams<T> p, T *Vn)
 {
@@ -993,6 +996,62 @@ __global__ void __launch_bounds__(1024) k_wide_s_chunk(const __grid_constant__ b
         }
         if (c == 0) Y[j] = lo;
         if (c == P - 1) Y[(long long)(nx - 1) * ny + j] = hi;
+    }
+}
+
+// Partitioned v sweep with the rows read in place (see k_wide_s_chunk; same bits as
+// k_wide_v_chunk, whose rows go through shared-memory tiles).
+template <typename T>
+__global__ void __launch_bounds__(1024) k_wide_v_chunk_plain(const __grid_constant__ bparams<T> p, const T *in, const T *inh,
+                                                        const T *b0, T *out, const T *__restrict__ hf,
+                                                        const T *__restrict__ hb)
+{
+    __shared__ T sa[32][33], sb[32][33];
+    const bdesc d = p.desc[0];
+    const inst_view<T> v = make_view(p, d);
+    const int nx = d.nx, ny = d.ny, e = ny - 2, P = blockDim.y, c = threadIdx.y, lane = threadIdx.x;
+    const int i = 1 + blockIdx.x * blockDim.x + lane;
+    const bool act = i <= nx - 2;
+    const long long row = (long long)i * ny;
+    int t0, t1;
+    chunk_range(e, P, c, t0, t1);
+    T lo = T(0), hi = T(0);
+    if (act) {
+        const int ii = ldg(v.imap() + i);
+        lo = b0[ii];
+        hi = ldg(v.X(X_VHI) + ii);
+        sb[c][lane] = v_line_fwd<T>(v, in, inh, out, i, t0, t1, c == 0 ? lo : T(0), hi);
+        sa[c][lane] = hf[(long long)t1 * nx + i];
+    }
+    __syncthreads();
+    T xh = T(0);
+    if (act) {
+        T yin = T(0);
+        if (c > 0) {
+            yin = sb[0][lane];
+            for (int q = 1; q < c; ++q) yin = sb[q][lane] + sa[q][lane] * yin;
+        }
+        for (int t = t1; t >= t0; --t) {
+            const long long ot = (long long)t * nx + i;
+            const T y = (c > 0) ? out[row + t] + hf[ot] * yin : out[row + t];
+            xh = y - ldg(v.Vt(VL_G) + ot) * xh;
+            out[row + t] = xh;
+        }
+    }
+    __syncthreads();
+    if (act) {
+        sb[c][lane] = xh;
+        sa[c][lane] = hb[(long long)t0 * nx + i];
+    }
+    __syncthreads();
+    if (act) {
+        if (c < P - 1) {
+            T xin = sb[P - 1][lane];
+            for (int q = P - 2; q > c; --q) xin = sb[q][lane] + sa[q][lane] * xin;
+            for (int t = t0; t <= t1; ++t) out[row + t] += hb[(long long)t * nx + i] * xin;
+        }
+        if (c == 0) out[row] = lo;
+        if (c == P - 1) out[row + ny - 1] = hi;
     }
 }
 
@@ -1646,6 +1705,7 @@ template <typename T> struct batch_typed {
     cudaGraphExec_t wide_graph = nullptr;
     int wide_ps = 1, wide_pv = 1;   // chunks per S line / per v line (1: thread per line)
     int wide_ls = 32, wide_lv = 32; // lines per CTA of the partitioned kernels (CTA: lines x chunks)
+    bool wide_vtile = true;         // v sweeps move their rows through shared-memory tiles (same bits)
     dbuf<T> d_spk;                  // chunk products: S hf, S hb, v hf, v hb (n each)
     int set_wide_chunks(int ps, int pv, cudaStream_t s, int ls = 0, int lv = 0); // ls, lv 0: by SM count
     int autotune_wide(cudaStream_t s);
@@ -2216,12 +2276,20 @@ void batch_typed<T>::launch_wide_v(cudaStream_t s, const bparams<T> &p, const T 
 {
     const bdesc &d = desc[0];
     if (wide_pv <= 1) {
-        k_wide_v<T><<<grid_for(d.nx - 2, 32), 32, 0, s>>>(p, in, inh, b0, out);
+        if (wide_vtile)
+            k_wide_v<T, true><<<grid_for(d.nx - 2, 32), 32, 0, s>>>(p, in, inh, b0, out);
+        else
+            k_wide_v<T, false><<<grid_for(d.nx - 2, 32), 32, 0, s>>>(p, in, inh, b0, out);
     } else {
         const long long n = total_n;
-        const size_t smem = sizeof(vtile<T>) * ((wide_lv * wide_pv) / 32);
-        k_wide_v_chunk<T><<<grid_for(d.nx - 2, wide_lv), dim3(wide_lv, wide_pv), smem, s>>>(p, in, inh, b0, out,
-                                                                                  d_spk.p + 2 * n, d_spk.p + 3 * n);
+        if (wide_vtile) {
+            const size_t smem = sizeof(vtile<T>) * ((wide_lv * wide_pv) / 32);
+            k_wide_v_chunk<T><<<grid_for(d.nx - 2, wide_lv), dim3(wide_lv, wide_pv), smem, s>>>(
+                p, in, inh, b0, out, d_spk.p + 2 * n, d_spk.p + 3 * n);
+        } else {
+            k_wide_v_chunk_plain<T><<<grid_for(d.nx - 2, wide_lv), dim3(wide_lv, wide_pv), 0, s>>>(
+                p, in, inh, b0, out, d_spk.p + 2 * n, d_spk.p + 3 * n);
+        }
     }
 }
 
@@ -2278,6 +2346,7 @@ template <typename T> int batch_typed<T>::autotune_wide(cudaStream_t s)
     LSS_CUDA_TRY(cudaEventCreate(&e1), "wide: tuning events");
     float best_s = 1e30f, best_v = 1e30f;
     int ps = 1, pv = 1, ls = 32, lv = 32;
+    bool vt = true;
     int rc = LSS_ADI_OK;
     auto timed = [&](auto &&launch) {
         launch();
@@ -2302,8 +2371,11 @@ template <typename T> int batch_typed<T>::autotune_wide(cudaStream_t s)
             }
             if (okV) {
                 k_wide_b1<T><<<grid_for(d.nx, 128), 128, 0, s>>>(p, p.U, d_b0.p);
-                const float ms = timed([&] { launch_wide_v(s, p, p.U, p.Y1, d_b0.p, p.Y2); });
-                if (ms < best_v) { best_v = ms; pv = P; lv = L; }
+                for (bool tile : {true, false}) {
+                    wide_vtile = tile;
+                    const float ms = timed([&] { launch_wide_v(s, p, p.U, p.Y1, d_b0.p, p.Y2); });
+                    if (ms < best_v) { best_v = ms; pv = P; lv = L; vt = tile; }
+                }
             }
             const cudaError_t err = cudaGetLastError();
             if (err != cudaSuccess) {
@@ -2315,6 +2387,7 @@ template <typename T> int batch_typed<T>::autotune_wide(cudaStream_t s)
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc) return rc;
+    wide_vtile = vt;
     return set_wide_chunks(ps, pv, s, ls, lv);
 }
 

@@ -66,4 +66,6 @@ def test_recompute_fraction():
         num += wi * ((s + c - 1) // c - 1) * c
         den += wi * s
     assert bench.recompute_fraction(probs) == pytest.approx(num / den)
-    assert bench.FP64_INSTR_FWD * (1 + 0.75) + bench.FP64_INSTR_ADJ == pytest.approx(169.1)
+    # the adjoint's count is what the forward + adjoint capture leaves after its forward passes
+    assert 0.0 < bench.CAPTURE_RF < 1.0
+    assert 0.0 < bench.FP64_INSTR_ADJ < bench.CAPTURE_FWDADJ

@@ -97,17 +97,22 @@ def test_custom_payoff_and_bilinear_value(lss, oracle):
     assert abs(val - ref_val) <= 1e-12 * max(1.0, abs(ref_val))
 
 
-def test_fp64_tables_option_tracks_fp64_problem(lss, oracle):
-    # the reference's FP32 remaps differ from its FP64 ones; with FP64 tables the FP32
-    # device path follows the FP64 solution far more closely than the reference's FP32
-    kw = dict(CONFIG1)
+@pytest.mark.parametrize("kw", [dict(CONFIG1),
+                                dict(CONFIG1, scheme="hv", rho=0.0, nx=160, ny=80, nt=121, **NU),
+                                dict(CONFIG1, scheme="mcs", rho=0.0, nx=120, ny=70, nt=101, **NU)],
+                         ids=["config1_dr", "hv_rho0", "mcs_rho0"])
+def test_fp64_tables_option_tracks_fp64_problem_within_1e4(lss, oracle, kw):
+    """The reference's FP32 remaps differ from its FP64 ones (its own FP32 surface is up to ~40 %
+    off at the remapped boundary points); with the grid, remaps and tables built in double and
+    rounded once, the FP32 device path stays within the 1e-4 of the FP64 oracle that FP32 is held
+    to (config 1: 7.0e-6; the 400 x 200 x 500 stable companions of config 2: 3-4e-5)."""
     op, pp = problem_pair(kw)
     v64 = oracle.solve(op, "f64")
     ref32 = oracle.solve(op, "f32")
     pp.fp64_tables = True
     got, _ = lss.ImplicitHestonSolver(pp, precision="f32", arith="fast").solve()
     assert rel_err(got, v64) < rel_err(ref32, v64)
-    assert rel_err(got, v64) < 1e-3
+    assert rel_err(got, v64) < 1e-4
 
 
 def thomas_numpy(lo, dg, up, rhs, blo, bhi):
