@@ -194,8 +194,9 @@ int lss_adi_forward_graph(lss_adi_handle *h, const void *payoff, void *out_surfa
  * sensitivities): returns out_value = V(eval_s, eval_v), dV/d(kappa, theta, sigma, rho, r)
  * in dv_dparams[5] (host doubles; for SABR sigma is nu and kappa, theta give 0) and
  * dV/d(payoff grid) in dv_dpayoff (Nx*Ny, may be NULL).  FP64, all four splittings, Heston
- * and SABR with r = 0 (the r sensitivity includes the discount factors D(t)).  Instances
- * larger than 256 x 160 points run the adjoint as one kernel per stage over the whole GPU.
+ * and SABR (the r sensitivity includes the discount factors D(t) inside a and c).  Instances
+ * larger than 256 x 160 points, and SABR with r != 0 (whose S-line tables are rebuilt at every
+ * step's time), run the adjoint as one kernel per stage over the whole GPU.
  * Checkpoints every `checkpoint_every` steps; 0 = planned: instances of up to 256 x 160 points
  * take the longest interval the workspace allows (at least ceil(sqrt(steps))), larger ones
  * ceil(sqrt(steps)).  Results do not depend on the interval. */
@@ -226,7 +227,8 @@ int lss_adi_batch_create(const lss_adi_problem *problems, int count, lss_adi_bat
 
 /* mode 0 = forward values only, 1 = forward + adjoint (values, the 5 parameter
  * sensitivities and dV/d(initial condition) per instance; FP64, every splitting, Heston and
- * SABR with r = 0).
+ * SABR with r = 0; SABR with r != 0 has time-dependent coefficients and runs through
+ * lss_adi_adjoint, one instance at a time).
  * The adjoint keeps a checkpoint every ceil(sqrt(steps)) steps or more (lss_adi_batch_checkpoints)
  * and recomputes each segment but the last once.  Device-resident: inputs were uploaded by
  * batch_create. */

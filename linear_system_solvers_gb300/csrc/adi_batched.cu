@@ -258,6 +258,51 @@ __global__ void k_setup_v_lines(setup_params sp, T *V0, long long slot_stride, T
 }
 
 // ------------------------------------------------------------------------------------------
+// time-dependent coefficients of one instance (SABR with r != 0 on the wide kernels)
+// ------------------------------------------------------------------------------------------
+// a and c carry D(t)^(2(1-beta)) and D(t)^(1-beta), D(t) = exp(-r (T - t)); b, d, e, f do not.
+// Before each step the S-direction base tables M, P, Z, C are re-evaluated at the step's powers
+// da, dc (general_heston_equation_coefficients, coefficients.hpp:89-98, on the transformed data
+// of lss_heat_data_transform.hpp:174-214) and the S lines re-factorised (k_setup_s_lines); the
+// v-direction tables do not change.  The same kernel scales the S-factors of the adjoint's
+// D(t) terms (X_HA, X_HDD by da, X_HC by dc) and the boundary-column weights that carry d^ on
+// the v = v_lo line (XB_M, XB_P), so that the adjoint steps see this step's a^ and c^.
+struct tdep_params {
+    const double *a_static, *c_static, *ab; // n each: ((0.5 v) v) S^(2 beta), ((rho nu) v) v S^beta, A B
+    const double *per_i;                    // 5 nx: A, A^2, A^3, A'', user d
+    const double *xs;                       // 3 nx: X_HA, X_HDD, X_HC at D = 1
+    double *base;                           // 7 n: M, P, Z, Mt, Pt, W, C
+    long long n;
+    int nx, ny;
+    double alpha, delta, two_alpha, half_rho_f;
+};
+
+template <typename T>
+__global__ void k_tdep_refresh(tdep_params tp, double da, double dc, T *xarena, long long total_x)
+{
+    const long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (o >= tp.n) return;
+    const int nx = tp.nx, ny = tp.ny;
+    const int i = static_cast<int>(o / ny), j = static_cast<int>(o % ny);
+    const double aval = tp.per_i[i], aa = tp.per_i[nx + i], aaa = tp.per_i[2 * nx + i];
+    const double gc = tp.per_i[3 * nx + i], ud = tp.per_i[4 * nx + i];
+    const double A = tp.a_static[o] * da;
+    const double ah = A / aa;
+    const double dh = ud / aval - (A * gc) / aaa;
+    tp.base[o] = tp.alpha * ah - tp.delta * dh;
+    tp.base[tp.n + o] = tp.alpha * ah + tp.delta * dh;
+    tp.base[2 * tp.n + o] = tp.two_alpha * ah - tp.half_rho_f;
+    tp.base[6 * tp.n + o] = (tp.c_static[o] * dc) / tp.ab[o];
+    if (j == 0) {
+        xarena[XB_M * total_x + i] = static_cast<T>(-tp.delta * dh);
+        xarena[XB_P * total_x + i] = static_cast<T>(tp.delta * dh);
+        xarena[X_HA * total_x + i] = static_cast<T>(tp.xs[i] * da);
+        xarena[X_HDD * total_x + i] = static_cast<T>(tp.xs[nx + i] * da);
+        xarena[X_HC * total_x + i] = static_cast<T>(tp.xs[2 * nx + i] * dc);
+    }
+}
+
+// ------------------------------------------------------------------------------------------
 // the persistent time-loop kernel
 // ------------------------------------------------------------------------------------------
 // One instance's view of the arenas.  The arena base pointers stay in the kernel's parameter
@@ -276,6 +321,26 @@ template <typename T> struct inst_view {
 };
 
 template <typename T> __device__ __forceinline__ T ldg(const T *p) { return __ldg(p); }
+
+// Explicitly rounded products and fused multiply-adds.  The v-line recurrences run in several
+// kernels (rows read in place, rows through shared-memory tiles, partitioned lines), and the
+// autotuner may pick a different variant per instance; written with these, every variant rounds
+// the same way whatever the compiler would contract, so they agree bit for bit.
+__device__ __forceinline__ double mul_x(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float mul_x(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double fma_x(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float fma_x(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+
+// One point of the v-line forward recurrence: y_t = la a0 + vc a1 + vn a2 + ib h - la y_{t-1}
+// (a0, a1, a2: `in` at t-1, t, t+1; h: `inh` at t).
+template <typename T> __device__ __forceinline__ T v_point(T la, T vc, T vn, T ib, T a0, T a1, T a2, T h, T y)
+{
+    T f = mul_x(la, a0);
+    f = fma_x(vc, a1, f);
+    f = fma_x(vn, a2, f);
+    f = fma_x(ib, h, f);
+    return fma_x(-la, y, f);
+}
 
 // Rows ahead that the line sweeps prefetch into L2 (0: none, the default).  Every access of a
 // sweep is known in advance (row t + PF of each table and state array), so a prefetch turns a
@@ -479,12 +544,9 @@ __device__ __forceinline__ T v_line_fwd(const inst_view<T> &v, const T *__restri
     for (int t = t0; t <= t1; ++t) {
         const long long ot = (long long)t * nx + i;
         const T a2 = in[row + t + 1];
-        T f = ldg(v.Vt(VL_LA) + ot) * a0;
-        f += ldg(v.Vt(VL_VC) + ot) * a1;
-        f += ldg(v.Vt(VL_VN) + ot) * a2;
-        f += ldg(v.Vt(VL_IB) + ot) * inh[row + t];
-        y = f - ldg(v.Vt(VL_LA) + ot) * y;
-        if (t == e) y -= ldg(v.X(X_CHV) + i) * hi;
+        y = v_point<T>(ldg(v.Vt(VL_LA) + ot), ldg(v.Vt(VL_VC) + ot), ldg(v.Vt(VL_VN) + ot), ldg(v.Vt(VL_IB) + ot), a0,
+                       a1, a2, inh[row + t], y);
+        if (t == e) y = fma_x(-ldg(v.X(X_CHV) + i), hi, y);
         out[row + t] = y;
         a0 = a1; a1 = a2;
     }
@@ -504,7 +566,7 @@ __device__ __forceinline__ void v_stage(const inst_view<T> &v, const T *__restri
         T x = v_line_fwd<T>(v, in, inh, out, i, 1, e, lo, hi);
 #pragma unroll 4
         for (int t = e - 1; t >= 1; --t) {
-            x = out[row + t] - ldg(v.Vt(VL_G) + (long long)t * nx + i) * x;
+            x = fma_x(-ldg(v.Vt(VL_G) + (long long)t * nx + i), x, out[row + t]);
             out[row + t] = x;
         }
         out[row] = lo;
@@ -576,12 +638,10 @@ __device__ __forceinline__ void v_lines_tiled(const inst_view<T> &v, const T *__
                 if (k < kk) {
                     const int t = tb + k;
                     const long long ot = (long long)t * nx + i;
-                    T f = ldg(v.Vt(VL_LA) + ot) * tl.in[lane][k];
-                    f += ldg(v.Vt(VL_VC) + ot) * tl.in[lane][k + 1];
-                    f += ldg(v.Vt(VL_VN) + ot) * tl.in[lane][k + 2];
-                    f += ldg(v.Vt(VL_IB) + ot) * tl.io[lane][k];
-                    y = f - ldg(v.Vt(VL_LA) + ot) * y;
-                    if (t == e) y -= chv * hi;
+                    y = v_point<T>(ldg(v.Vt(VL_LA) + ot), ldg(v.Vt(VL_VC) + ot), ldg(v.Vt(VL_VN) + ot),
+                                   ldg(v.Vt(VL_IB) + ot), tl.in[lane][k], tl.in[lane][k + 1], tl.in[lane][k + 2],
+                                   tl.io[lane][k], y);
+                    if (t == e) y = fma_x(-chv, hi, y);
                     tl.io[lane][k] = y;
                 }
             }
@@ -601,7 +661,7 @@ __device__ __forceinline__ void v_lines_tiled(const inst_view<T> &v, const T *__
             for (int k = VT - 1; k >= 0; --k) {
                 if (k < kk) {
                     const int t = ts + k;
-                    x = tl.io[lane][k] - ldg(v.Vt(VL_G) + (long long)t * nx + i) * x;
+                    x = fma_x(-ldg(v.Vt(VL_G) + (long long)t * nx + i), x, tl.io[lane][k]);
                     tl.io[lane][k] = x;
                 }
             }
@@ -1029,12 +1089,12 @@ __global__ void __launch_bounds__(1024) k_wide_v_chunk_plain(const __grid_consta
         T yin = T(0);
         if (c > 0) {
             yin = sb[0][lane];
-            for (int q = 1; q < c; ++q) yin = sb[q][lane] + sa[q][lane] * yin;
+            for (int q = 1; q < c; ++q) yin = fma_x(sa[q][lane], yin, sb[q][lane]);
         }
         for (int t = t1; t >= t0; --t) {
             const long long ot = (long long)t * nx + i;
-            const T y = (c > 0) ? out[row + t] + hf[ot] * yin : out[row + t];
-            xh = y - ldg(v.Vt(VL_G) + ot) * xh;
+            const T y = (c > 0) ? fma_x(hf[ot], yin, out[row + t]) : out[row + t];
+            xh = fma_x(-ldg(v.Vt(VL_G) + ot), xh, y);
             out[row + t] = xh;
         }
     }
@@ -1047,8 +1107,8 @@ __global__ void __launch_bounds__(1024) k_wide_v_chunk_plain(const __grid_consta
     if (act) {
         if (c < P - 1) {
             T xin = sb[P - 1][lane];
-            for (int q = P - 2; q > c; --q) xin = sb[q][lane] + sa[q][lane] * xin;
-            for (int t = t0; t <= t1; ++t) out[row + t] += hb[(long long)t * nx + i] * xin;
+            for (int q = P - 2; q > c; --q) xin = fma_x(sa[q][lane], xin, sb[q][lane]);
+            for (int t = t0; t <= t1; ++t) out[row + t] = fma_x(hb[(long long)t * nx + i], xin, out[row + t]);
         }
         if (c == 0) out[row] = lo;
         if (c == P - 1) out[row + ny - 1] = hi;
@@ -1143,12 +1203,10 @@ __global__ void __launch_bounds__(1024) k_wide_v_chunk(const __grid_constant__ b
                 if (k < kk) {
                     const int t = tb + k;
                     const long long ot = (long long)t * nx + i;
-                    T f = ldg(v.Vt(VL_LA) + ot) * tl.in[wl][k];
-                    f += ldg(v.Vt(VL_VC) + ot) * tl.in[wl][k + 1];
-                    f += ldg(v.Vt(VL_VN) + ot) * tl.in[wl][k + 2];
-                    f += ldg(v.Vt(VL_IB) + ot) * tl.io[wl][k];
-                    y = f - ldg(v.Vt(VL_LA) + ot) * y;
-                    if (t == e) y -= chv * hi;
+                    y = v_point<T>(ldg(v.Vt(VL_LA) + ot), ldg(v.Vt(VL_VC) + ot), ldg(v.Vt(VL_VN) + ot),
+                                   ldg(v.Vt(VL_IB) + ot), tl.in[wl][k], tl.in[wl][k + 1], tl.in[wl][k + 2],
+                                   tl.io[wl][k], y);
+                    if (t == e) y = fma_x(-chv, hi, y);
                     tl.io[wl][k] = y;
                 }
             }
@@ -1167,7 +1225,7 @@ __global__ void __launch_bounds__(1024) k_wide_v_chunk(const __grid_constant__ b
     T yin = T(0);
     if (act && c > 0) {
         yin = sb[0][lane];
-        for (int q = 1; q < c; ++q) yin = sb[q][lane] + sa[q][lane] * yin;
+        for (int q = 1; q < c; ++q) yin = fma_x(sa[q][lane], yin, sb[q][lane]);
     }
     T xh = T(0);
     for (int jt = 0; jt < steps_max; ++jt) {
@@ -1189,8 +1247,8 @@ __global__ void __launch_bounds__(1024) k_wide_v_chunk(const __grid_constant__ b
                 if (k <= te - ts) {
                     const int t = ts + k;
                     const long long ot = (long long)t * nx + i;
-                    const T yv = (c > 0) ? tl.io[wl][k] + hf[ot] * yin : tl.io[wl][k];
-                    xh = yv - ldg(v.Vt(VL_G) + ot) * xh;
+                    const T yv = (c > 0) ? fma_x(hf[ot], yin, tl.io[wl][k]) : tl.io[wl][k];
+                    xh = fma_x(-ldg(v.Vt(VL_G) + ot), xh, yv);
                     tl.io[wl][k] = xh;
                 }
             }
@@ -1209,7 +1267,7 @@ __global__ void __launch_bounds__(1024) k_wide_v_chunk(const __grid_constant__ b
     T xin = T(0);
     if (act && c < P - 1) {
         xin = sb[P - 1][lane];
-        for (int q = P - 2; q > c; --q) xin = sb[q][lane] + sa[q][lane] * xin;
+        for (int q = P - 2; q > c; --q) xin = fma_x(sa[q][lane], xin, sb[q][lane]);
     }
     for (int jt = 0; jt < steps_max; ++jt) {
         auto own_f = [&](int r, long long &off, int &cnt) {
@@ -1226,7 +1284,7 @@ __global__ void __launch_bounds__(1024) k_wide_v_chunk(const __grid_constant__ b
         if (act && c < P - 1) {
 #pragma unroll
             for (int k = 0; k < VT; ++k)
-                if (k < kk) tl.io[wl][k] += hb[(long long)(tb + k) * nx + i] * xin;
+                if (k < kk) tl.io[wl][k] = fma_x(hb[(long long)(tb + k) * nx + i], xin, tl.io[wl][k]);
         }
         __syncwarp();
         vtile_copy_rows<VT + 1, VT, false>(&tl.io[0][0], (const T *)nullptr, out, own_f, wl);
@@ -1720,6 +1778,17 @@ template <typename T> struct batch_typed {
     dbuf<T> d_aspk;                 // adjoint chunk products: S hz, S hw, v hz, v hw (n each)
     int aspk_ps = 0, aspk_pv = 0;
     int enqueue_wide_adjoint(cudaStream_t s);
+    // time-dependent coefficients (SABR with r != 0; one FP64 instance on the wide kernels):
+    // before each step, forward or adjoint, the S-line tables are rebuilt at the step's time
+    bool tdep = false;
+    dbuf<double> td_buf;            // base tables (7 n), a_static, c_static, ab (n each), per_i (5 nx), xs (3 nx)
+    dbuf<double> td_scal;           // theta, zeta, gamma
+    dbuf<long long> td_ls;          // S-line offset of the instance (0)
+    tdep_params td{};
+    std::vector<double> td_da, td_dc; // D(t)^(2(1-beta)), D(t)^(1-beta) per step
+    int init_tdep(const lss_adi_problem &p);
+    // products: 1 = the forward chunk products of the S lines, 2 = the adjoint's
+    void refresh_step(cudaStream_t s, int step, int products);
     int enqueue(int mode, cudaStream_t s);
     int run(int mode, cudaStream_t s, bool use_graph);
 };
@@ -1892,8 +1961,11 @@ template <typename T> int batch_typed<T>::create(const lss_adi_problem *ps, int 
     adjoint_ok = std::is_same<T, double>::value;
     adjoint_why = adjoint_ok ? "" : "the adjoint is FP64 only";
     for (int k = 0; k < n && adjoint_ok; ++k) {
-        if (time_dependent(ps[k])) { adjoint_ok = false; adjoint_why = "no adjoint for SABR with r != 0"; }
-
+        // time-dependent tables are rebuilt per step by the host-sequenced wide kernels only
+        if (time_dependent(ps[k]) && n > 1) {
+            adjoint_ok = false;
+            adjoint_why = "SABR with r != 0 (time-dependent coefficients) runs as a single instance only";
+        }
     }
 
     // factorise on the device from the base tables
@@ -1937,7 +2009,88 @@ template <typename T> int batch_typed<T>::create(const lss_adi_problem *ps, int 
     LSS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
     this->sms = sms;
     if (n == 1) LSS_CUDA_TRY(d_b0.alloc(desc[0].nx), "batch: allocating the boundary column");
+    if (n == 1 && time_dependent(ps[0])) return init_tdep(ps[0]);
     return LSS_ADI_OK;
+}
+
+// Device copies of the time-independent factors of a time-dependent instance (FP64 only).
+template <typename T> int batch_typed<T>::init_tdep(const lss_adi_problem &p)
+{
+    if (!std::is_same<T, double>::value)
+        return set_error(LSS_ADI_EUNSUPPORTED, "batch: time-dependent coefficients on the wide kernels are FP64 only");
+    instance_tables<double> tt;
+    build_tables<double>(p, tt);
+    const bdesc &d = desc[0];
+    const long long n = total_n;
+    const int nx = d.nx;
+    const size_t off_stat = 7 * static_cast<size_t>(n), off_pi = off_stat + 3 * static_cast<size_t>(n),
+                 off_xs = off_pi + 5 * static_cast<size_t>(nx), total = off_xs + 3 * static_cast<size_t>(nx);
+    std::vector<double> h(total, 0.0);
+    std::copy(tt.coef.begin(), tt.coef.end(), h.begin());
+    std::copy(tt.a_static.begin(), tt.a_static.end(), h.begin() + off_stat);
+    std::copy(tt.c_static.begin(), tt.c_static.end(), h.begin() + off_stat + n);
+    std::copy(tt.ab.begin(), tt.ab.end(), h.begin() + off_stat + 2 * n);
+    std::copy(tt.per_i.begin(), tt.per_i.end(), h.begin() + off_pi);
+    // the adjoint's S-factors at D = 1 (the arena holds them as built by create)
+    std::vector<T> xa(X_COUNT * static_cast<size_t>(total_x));
+    LSS_CUDA_TRY(cudaMemcpy(xa.data(), xarena.p, xa.size() * sizeof(T), cudaMemcpyDeviceToHost), "batch: x arena");
+    for (int i = 0; i < nx; ++i) {
+        h[off_xs + i] = static_cast<double>(xa[X_HA * total_x + i]);
+        h[off_xs + nx + i] = static_cast<double>(xa[X_HDD * total_x + i]);
+        h[off_xs + 2 * nx + i] = static_cast<double>(xa[X_HC * total_x + i]);
+    }
+    LSS_CUDA_TRY(td_buf.alloc(total), "batch: allocating time-dependent tables");
+    LSS_CUDA_TRY(td_buf.upload(h.data(), total), "batch: uploading time-dependent tables");
+    const double scal[3] = {tt.sc.theta, tt.sc.zeta, tt.sc.gamma};
+    LSS_CUDA_TRY(td_scal.alloc(3), "batch: allocating scalars");
+    LSS_CUDA_TRY(td_scal.upload(scal, 3), "batch: uploading scalars");
+    const long long zero = 0;
+    LSS_CUDA_TRY(td_ls.alloc(1), "batch: allocating line offsets");
+    LSS_CUDA_TRY(td_ls.upload(&zero, 1), "batch: uploading line offsets");
+    LSS_CUDA_TRY(cudaDeviceSynchronize(), "batch: time-dependent tables");
+    td.base = td_buf.p;
+    td.a_static = td_buf.p + off_stat;
+    td.c_static = td_buf.p + off_stat + n;
+    td.ab = td_buf.p + off_stat + 2 * n;
+    td.per_i = td_buf.p + off_pi;
+    td.xs = td_buf.p + off_xs;
+    td.n = n;
+    td.nx = nx;
+    td.ny = d.ny;
+    td.alpha = tt.sc.alpha;
+    td.delta = tt.sc.delta;
+    td.two_alpha = tt.two_alpha;
+    td.half_rho_f = tt.half_rho_f;
+    td_da = tt.step_da;
+    td_dc = tt.step_dc;
+    tdep = true;
+    return LSS_ADI_OK;
+}
+
+// The S-line tables (and with `products` the chunk products of the partitioned solves) of
+// step `step` of a time-dependent instance, enqueued on s before that step's kernels.
+template <typename T> void batch_typed<T>::refresh_step(cudaStream_t s, int step, int products)
+{
+    const bdesc &d = desc[0];
+    const long long n = total_n;
+    k_tdep_refresh<T><<<grid_for(n, 256), 256, 0, s>>>(td, td_da[step], td_dc[step], xarena.p, total_x);
+    setup_params sp{};
+    sp.desc = d_desc.p;
+    sp.line_start = td_ls.p;
+    sp.count = 1;
+    sp.total_lines = d.ny - 2;
+    sp.base = td.base;
+    sp.total_n = n;
+    sp.scal = td_scal.p;
+    k_setup_s_lines<T><<<grid_for(d.ny - 2, 128), 128, 0, s>>>(sp, stab.p, n, yarena.p + Y_CHS * total_y);
+    if (wide_ps > 1) {
+        const bparams<T> p = params();
+        const int g = grid_for(static_cast<long long>(d.ny - 2) * wide_ps, 128);
+        if (products & 1)
+            k_wide_spikes<T><<<g, 128, 0, s>>>(p.S[SL_LA], p.S[SL_G], d_spk.p, d_spk.p + n, d.ny, d.ny, d.nx - 2, wide_ps);
+        if (products & 2)
+            k_wadj_spikes<T><<<g, 128, 0, s>>>(p.S[SL_LA], p.S[SL_G], d_aspk.p, d_aspk.p + n, d.ny, d.ny, d.nx - 2, wide_ps);
+    }
 }
 
 template <typename T> int batch_typed<T>::prepare_adjoint(cudaStream_t s)
@@ -2420,7 +2573,12 @@ template <typename T> int batch_typed<T>::enqueue_wide(cudaStream_t s)
     LSS_CUDA_TRY(cudaMemcpyAsync(U, d_payoff.p, total_n * sizeof(T), cudaMemcpyDeviceToDevice, s), "wide: initial state");
     LSS_CUDA_TRY(cudaMemsetAsync(d_status.p, 0, sizeof(int), s), "wide: clearing the status");
     long long nl = 0;
+    const int per_refresh = 2 + (wide_ps > 1 ? 1 : 0);
     for (int step = 0; step < d.steps; ++step) {
+        if (tdep) {
+            refresh_step(s, step, 1);
+            nl += per_refresh;
+        }
         enqueue_wide_step(s, p, U, Y1, Y2, Y3, V);
         nl += d.scheme == LSS_ADI_DOUGLAS_RACHFORD ? 4 : 6;
         std::swap(U, V);
@@ -2492,7 +2650,12 @@ template <typename T> int batch_typed<T>::enqueue_wide_adjoint(cudaStream_t s)
         const int per_step = d.scheme == LSS_ADI_DOUGLAS_RACHFORD ? 4 : 6;
         const double *cur = CK;
         const int n0_last = (nseg - 1) * c; // the last segment keeps its stage values: no recomputation
+        const int per_refresh = 2 + (ps > 1 ? 1 : 0);
         for (int step = 0; step < d.steps; ++step) {
+            if (tdep) {
+                refresh_step(s, step, 1);
+                nl += per_refresh;
+            }
             if (step >= n0_last) {
                 const int m = step - n0_last;
                 enqueue_wide_step(s, p, cur, slot(m, 1), slot(m, 2), slot(m, 3), slot(m + 1, 0));
@@ -2516,11 +2679,19 @@ template <typename T> int batch_typed<T>::enqueue_wide_adjoint(cudaStream_t s)
             const double *u0 = CK + static_cast<long long>(sgi) * n;
             for (int m = 0; m < L && sgi < nseg - 1; ++m) {
                 const double *um = (m == 0) ? u0 : slot(m, 0);
+                if (tdep) {
+                    refresh_step(s, n0 + m, 1);
+                    nl += per_refresh;
+                }
                 enqueue_wide_step(s, p, um, slot(m, 1), slot(m, 2), slot(m, 3), slot(m + 1, 0));
                 nl += per_step;
             }
             for (int m = L - 1; m >= 0; --m) {
                 const double *um = (m == 0) ? u0 : slot(m, 0);
+                if (tdep) { // this step's S-line tables and the adjoint's D(t) factors
+                    refresh_step(s, n0 + m, 2);
+                    nl += per_refresh;
+                }
                 const double *Y1 = slot(m, 1), *Y2 = slot(m, 2), *Y3 = slot(m, 3), *Vo = slot(m + 1, 0);
                 const double tau = d.a_tau0 + d.a_dtau * (n0 + m);
                 // v stages: (in, out, output adjoint, adjoint of in, adjoint of inh), first or accumulating
@@ -2743,16 +2914,17 @@ int adjoint_solver::init(const lss_adi_problem &p)
 {
     if (p.scheme == LSS_ADI_EXPLICIT_EULER)
         return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_adjoint: no adjoint for the explicit Euler scheme");
-    if (time_dependent(p))
-        return set_error(LSS_ADI_EUNSUPPORTED, "lss_adi_adjoint: SABR with r != 0 (time-dependent coefficients) not supported");
     impl.reset(new (std::nothrow) adjoint_impl());
     if (!impl) return set_error(LSS_ADI_ENOMEM, "host allocation failed");
     lss_adi_problem q = p;
     q.arith = LSS_ADI_ARITH_FAST;
     int rc = impl->b.create(&q, 1);
     if (rc) return rc;
-    // one CTA carries an instance of up to 256 x 160 points well; larger ones run wide
-    impl->wide = p.nx > 256 || static_cast<long long>(p.nx) * p.ny > 40960 || (p.options & LSS_ADI_OPT_WIDE_ADJOINT);
+    // one CTA carries an instance of up to 256 x 160 points well; larger ones run wide, and so
+    // do time-dependent coefficients (SABR with r != 0), whose S-line tables the host-sequenced
+    // wide kernels rebuild before every step
+    impl->wide = p.nx > 256 || static_cast<long long>(p.nx) * p.ny > 40960 || (p.options & LSS_ADI_OPT_WIDE_ADJOINT) ||
+                 time_dependent(p);
     if (impl->wide && !(p.options & LSS_ADI_OPT_LINE_PER_THREAD)) {
         rc = impl->b.autotune_wide(nullptr);
         if (rc) return rc;

@@ -89,6 +89,13 @@ CASES = {
     "wide_heston_mcs": dict(BASE, scheme="mcs", zeta=1.0 / 3.0, nx=264, ny=160, nt=9, rho=-0.2),
     "wide_sabr_dr": dict(SABR, scheme="dr", nx=280, ny=90, nt=17),
     "wide_heston_hv": dict(BASE, scheme="hv", nx=300, ny=70, nt=13),
+    # SABR with r != 0 (the reference's SABR problem, unit_tests/common/lss_print_t.hpp:2039-2042):
+    # a and c carry D(t)^(2(1-beta)) and D(t)^(1-beta) at every step's time, so the adjoint runs
+    # on the wide kernels with the S-line tables rebuilt before every forward and adjoint step
+    "sabr_dr_r03": dict(SABR, scheme="dr", rate=0.03, nx=48, ny=26, nt=31),
+    "sabr_mcs_r03": dict(SABR, scheme="mcs", zeta=0.8, theta_scheme="theta80", rate=0.03, nx=40, ny=22, nt=21),
+    "sabr_hv_r03": dict(SABR, scheme="hv", rate=0.05, nx=46, ny=24, nt=21),
+    "wide_sabr_cs_r03": dict(SABR, scheme="cs", rate=0.03, nx=280, ny=90, nt=17, maturity=2.0),
 }
 
 
@@ -104,7 +111,8 @@ def test_parameter_gradients_match_device_finite_differences(lss, key):
 
 
 @pytest.mark.parametrize("key", ["mcs_64x32", "dr_70x35", "mcs_z08_cn", "sabr_dr", "sabr_mcs_z08", "wide_heston_cs",
-                                 "wide_sabr_dr", "hv_60x30", "sabr_hv", "wide_heston_hv"])
+                                 "wide_sabr_dr", "hv_60x30", "sabr_hv", "wide_heston_hv", "sabr_dr_r03", "sabr_hv_r03",
+                                 "wide_sabr_cs_r03"])
 def test_parameter_gradients_match_reference_bump_and_revalue(lss, oracle, key):
     p = lss.HestonProblem(**CASES[key])
     val, grads, _ = lss.ImplicitHestonSolver(p, precision="f64", arith="fast").adjoint(want_payoff_grad=False)
@@ -114,7 +122,7 @@ def test_parameter_gradients_match_reference_bump_and_revalue(lss, oracle, key):
 
 
 @pytest.mark.parametrize("key", ["mcs_64x32", "cs_60x30", "dr_70x35", "sabr_cs", "wide_heston_mcs", "hv_60x30",
-                                 "wide_heston_hv"])
+                                 "wide_heston_hv", "sabr_mcs_r03", "wide_sabr_cs_r03"])
 def test_payoff_gradient_is_the_linear_response(lss, key):
     p = lss.HestonProblem(**CASES[key])
     s = lss.ImplicitHestonSolver(p, precision="f64", arith="fast")
@@ -129,7 +137,7 @@ def test_payoff_gradient_is_the_linear_response(lss, key):
     assert abs((v1 - v0) - pred) <= 1e-9 * max(1.0, np.sum(np.abs(lam * delta)))
 
 
-@pytest.mark.parametrize("key", ["mcs_64x32", "wide_heston_cs", "hv_60x30"])
+@pytest.mark.parametrize("key", ["mcs_64x32", "wide_heston_cs", "hv_60x30", "sabr_dr_r03"])
 def test_checkpoint_interval_does_not_change_results(lss, key):
     p = lss.HestonProblem(**CASES[key])
     s = lss.ImplicitHestonSolver(p, precision="f64", arith="fast")
