@@ -32,20 +32,31 @@ BYTES_PER_GPS_FWD = {"dr": 40, "cs": 96, "mcs": 96, "hv": 96}  # algorithmic byt
 # Figures of one ncu capture each of the batched kernels on the 1024-instance, 40-step case
 # (--count 1024 --max-time-steps 40; forward: --mode fwd; forward + adjoint: --mode fwdadj
 # --workspace-gb 12, whose plan recomputes a fraction CAPTURE_RF = 0.4898 of the steps), per
-# grid-point-step, scaled to a launch by the grid-point-steps it processes:
-# DRAM bytes read + written (dram__bytes_read.sum + dram__bytes_write.sum), mode 0 =
-# k_batch_forward, mode 1 = k_batch_fwdadj
-DRAM_BYTES_PER_GPS = {0: 340.9, 1: 1036.1}
-# FP64 instructions, thread level (smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum):
-# the forward kernel counted FP64_INSTR_FWD per grid-point-step; forward + adjoint is one forward
-# pass, the recomputation of every checkpoint segment but the last (a fraction rf of the steps)
-# and the adjoint steps, FP64_INSTR_FWD * (1 + rf) + FP64_INSTR_ADJ, and its capture counted
-# CAPTURE_FWDADJ at rf = CAPTURE_RF.
-FP64_INSTR_FWD = 34.0
+# grid-point-step, scaled to a launch by the grid-point-steps it processes.  Forward + adjoint
+# is one forward pass, the recomputation of every checkpoint segment but the last (a fraction rf
+# of the steps) and the adjoint steps, so a figure X of it is X_FWD * (1 + rf) + X_ADJ, with X_ADJ
+# what the forward + adjoint capture (at rf = CAPTURE_RF) leaves after its forward passes.
 CAPTURE_RF = 0.4898
-CAPTURE_FWDADJ = 142.17
+# DRAM bytes read + written (dram__bytes_read.sum + dram__bytes_write.sum): k_batch_forward,
+# k_batch_fwdadj
+DRAM_BYTES_FWD = 339.1
+CAPTURE_DRAM_FWDADJ = 1035.8
+DRAM_BYTES_ADJ = CAPTURE_DRAM_FWDADJ - DRAM_BYTES_FWD * (1.0 + CAPTURE_RF)
+# FP64 instructions, thread level (smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum)
+FP64_INSTR_FWD = 32.07
+CAPTURE_FWDADJ = 139.30
 FP64_INSTR_ADJ = CAPTURE_FWDADJ - FP64_INSTR_FWD * (1.0 + CAPTURE_RF)
-FP64_INSTR_PEAK = 5.98e11  # used only where the live probe below cannot run
+
+
+# Adjoint workspace cap of the timed batch, as a fraction of the device memory (the library's
+# default is a quarter; a larger cap stores more stage values and recomputes fewer steps)
+WS_FRACTION = 0.6
+
+
+def per_gps(fwd, adj, mode, rf):
+    """A per-grid-point-step figure of the run: the forward kernel's, or forward + adjoint at the
+    run's recomputed fraction rf."""
+    return fwd if mode == 0 else fwd * (1.0 + rf) + adj
 
 
 def fp64_rate(lib):
@@ -92,9 +103,9 @@ def parse():
     ap.add_argument("--strong", action="store_true",
                     help="under torchrun: split one batch over the ranks by cost (strong scaling) instead of one "
                          "batch per rank (weak scaling)")
-    ap.add_argument("--workspace-gb", type=float, default=0.0,
-                    help="cap of the forward + adjoint workspace in GB (0 = the library default, a quarter of the "
-                         "device memory)")
+    ap.add_argument("--workspace-gb", type=float, default=None,
+                    help="cap of the forward + adjoint workspace in GB (default: WS_FRACTION of the device memory; "
+                         "0 = the library default, a quarter of it)")
     ap.add_argument("--checkpoint-every", type=int, default=0,
                     help="fixed checkpoint interval of the adjoint (0 = planned from the workspace cap)")
     ap.add_argument("--max-time-steps", type=int, default=0,
@@ -332,7 +343,10 @@ def main():
     lib = L.load()
     fp64_peak = fp64_rate(lib)
     batch = lss.BatchSolver(problems, precision="f64")
-    batch.set_workspace(args.workspace_gb * 1e9, args.checkpoint_every)
+    # the batch has the GPU to itself: give the adjoint workspace most of it (fewer recomputed steps)
+    ws_cap = (WS_FRACTION * torch.cuda.get_device_properties(0).total_memory if args.workspace_gb is None
+              else args.workspace_gb * 1e9)
+    batch.set_workspace(ws_cap, args.checkpoint_every)
     mode = 0
     if args.mode in ("auto", "fwdadj"):
         try:
@@ -395,7 +409,8 @@ def main():
     value = gps_all / (t_max * 1e-3)
     bpg = BYTES_PER_GPS_FWD["mcs"] * (1 if mode == 0 else 10.0 / 3.0)
     rf = recompute_fraction(problems, batch.checkpoints()) if mode == 1 else 0.0
-    fp64_per_gps = FP64_INSTR_FWD if mode == 0 else FP64_INSTR_FWD * (1.0 + rf) + FP64_INSTR_ADJ
+    fp64_per_gps = per_gps(FP64_INSTR_FWD, FP64_INSTR_ADJ, mode, rf)
+    dram_per_gps = per_gps(DRAM_BYTES_FWD, DRAM_BYTES_ADJ, mode, rf)
     peak, peak_kind = measured_peaks()
     achieved = gps * bpg / (ms * 1e-3) / 1e9
     out = {
@@ -416,11 +431,13 @@ def main():
                    "parallelism": (f"instance sharding x{world} ({'one batch split by cost' if args.strong else 'a batch per rank'})"
                                    if world > 1 else "single GPU")},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": DRAM_BYTES_PER_GPS[mode] * gps, "traffic_unit": "bytes per launch",
-                     "traffic_source": "ncu dram__bytes_read+write of the 1024-instance 40-step capture, per "
-                                       "grid-point-step, times this launch's grid-point-steps", "peak_source": peak_kind,
+                     "traffic": dram_per_gps * gps, "traffic_unit": "bytes per launch",
+                     "traffic_source": "ncu dram__bytes_read+write of the 1024-instance 40-step captures, per "
+                                       "grid-point-step (forward + adjoint: forward x (1 + recomputed fraction) + "
+                                       "adjoint), times this launch's grid-point-steps", "peak_source": peak_kind,
                      "algorithmic_bytes_per_grid_point_step": bpg,
-                     "note": "FP64 pipe (1.196 TFLOP/s measured) binds before HBM on GB300"},
+                     "note": f"the FP64 pipe ({2 * fp64_peak / 1e12:.3f} TFLOP/s of DFMA measured in this run) "
+                             "binds before HBM on GB300"},
         "fp64_pipe": {"instructions_per_grid_point_step": fp64_per_gps, "recomputed_fraction": rf,
                       "achieved": gps * fp64_per_gps / (ms * 1e-3), "peak": fp64_peak,
                       "peak_source": "lss_diag_fp64_rate, measured in this run",
@@ -429,6 +446,10 @@ def main():
                               "forward x (1 + recomputed fraction) + adjoint), peak from a DFMA probe"},
         "e2e": {"value": gps_all / e2e_s, "unit": "grid-point-steps/s", "h2d_bytes_per_step": int(total_n * 8),
                 "d2h_bytes_per_step": int(len(problems) * 8 * (6 if mode == 1 else 1)), "matches_device_values": e2e_ok},
+        "adjoint_workspace": ({"cap_gb": ws_cap / 1e9, "held_gb": batch.workspace_bytes() / 1e9,
+                               "recomputed_fraction": rf,
+                               "how": "lss_adi_batch_set_workspace (library default: a quarter of the device memory)"}
+                              if mode == 1 else None),
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "nonfinite_instances": int(np.count_nonzero(status)),
@@ -754,8 +775,12 @@ def run_heat1d(count=65536, sample=48):
                 rec["roofline"] = {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
                                    "peak_source": peak_kind, "bytes_per_point_step": HEAT1D_BYTES_PER_PS[fp]}
                 if fp == "f64":
+                    from linear_system_solvers_gb300 import _lib as L
+
+                    fpk = fp64_rate(L.load())
                     rec["fp64_pipe"] = {"fp64_ops_per_point_step": 5, "achieved_ops_per_s": 5 * ps / secs,
-                                        "frac_of_5.98e11": 5 * ps / secs / FP64_INSTR_PEAK}
+                                        "peak": fpk, "peak_source": "lss_diag_fp64_rate, measured in this run",
+                                        "frac": 5 * ps / secs / fpk}
             else:
                 eq = [bool(np.array_equal(b.solution(i), O.solve_1d(oproblem(qs[i]), fp))) for i in idx[:16]]
                 rec["bitwise_equal_oracle_sample"] = f"{sum(eq)}/{len(eq)}"

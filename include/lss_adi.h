@@ -271,7 +271,8 @@ int lss_adi_batch_checkpoints(const lss_adi_batch *b, int *intervals);
 
 /* Bounds the forward + adjoint workspace (checkpoints and the stored stage values of one
  * checkpoint segment, one slice per resident CTA): max_bytes = 0 restores the default, a
- * quarter of the device memory (never more than half of what is free when it is planned).
+ * quarter of the device memory (never more than half of what is free when it is planned); a
+ * max_bytes > 0 is honoured up to 90 % of the free memory.
  * checkpoint_every > 0 fixes every instance's checkpoint interval (capped at its step count);
  * 0 plans it from the cap.  A cap too small for one slice per resident CTA runs fewer CTAs; one
  * too small for a single slice makes the next mode-1 run return LSS_ADI_ENOMEM.  Takes effect

@@ -342,15 +342,6 @@ template <typename T> __device__ __forceinline__ T v_point(T la, T vc, T vn, T i
     return fma_x(-la, y, f);
 }
 
-// Rows ahead that the line sweeps prefetch into L2 (0: none, the default).  Every access of a
-// sweep is known in advance (row t + PF of each table and state array), so a prefetch turns a
-// DRAM-latency load into an L2 hit without holding registers.  Addresses stay inside the
-// instance's arrays.
-#ifndef LSS_PREFETCH_ROWS
-#define LSS_PREFETCH_ROWS 0
-#endif
-__device__ __forceinline__ void pf_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
-
 // boundary#1: the v = v_lo column, explicit (explicit_boundary.hpp:39-84); result in smem
 // Work distribution of every stage: items l0, l0 + ls, ... (threads of one CTA in the
 // batched kernel; all threads of a grid in the per-stage kernels of the wide path).
@@ -409,12 +400,6 @@ __device__ __forceinline__ T s_line_fwd(const inst_view<T> &v, const T *__restri
 #pragma unroll 4
         for (int t = t0; t <= t1; ++t) {
             const long long o = (long long)t * ny + j;
-            if constexpr (LSS_PREFETCH_ROWS > 0) {
-                const long long of = (long long)min(t + LSS_PREFETCH_ROWS, e) * ny + j;
-                pf_l2(U + of + ny);
-                pf_l2(v.S(SL_WG) + of); pf_l2(v.S(SL_WW) + of); pf_l2(v.S(SL_WS) + of); pf_l2(v.S(SL_WC) + of);
-                pf_l2(v.S(SL_WN) + of); pf_l2(v.S(SL_WE) + of); pf_l2(v.S(SL_LA) + of);
-            }
             const T u2m = U[o + ny - 1], u2c = U[o + ny], u2p = U[o + ny + 1];
             const T q2 = u2m - u2p;
             const T mix = q0 - q2;
@@ -444,16 +429,6 @@ __device__ __forceinline__ T s_line_fwd(const inst_view<T> &v, const T *__restri
 #pragma unroll 4
         for (int t = t0; t <= t1; ++t) {
             const long long o = (long long)t * ny + j;
-            if constexpr (LSS_PREFETCH_ROWS > 0) {
-                const long long of = (long long)min(t + LSS_PREFETCH_ROWS, e) * ny + j;
-                pf_l2(U + of + ny); pf_l2(Y1 + of + ny); pf_l2(Y2 + of + ny);
-                pf_l2(v.S(SL_LA) + of); pf_l2(v.S(SL_S2SC) + of); pf_l2(v.S(SL_S2SE) + of); pf_l2(v.S(SL_S2MZ) + of);
-                if constexpr (hv || !xt) pf_l2(v.S(SL_S2IB) + of);
-                if constexpr (xt) {
-                    pf_l2(v.S(SL_X1) + of); pf_l2(v.S(SL_X2) + of); pf_l2(v.S(SL_X3) + of);
-                    pf_l2(v.S(SL_X4) + of); pf_l2(v.S(SL_X5) + of);
-                }
-            }
             const T uc2 = U[o + ny];
             const T d2m = Y2[o + ny - 1] - U[o + ny - 1];
             const T d2p = Y2[o + ny + 1] - U[o + ny + 1];
@@ -511,7 +486,6 @@ __device__ __forceinline__ void s_stage(const inst_view<T> &v, const T *__restri
 #pragma unroll 4
         for (int t = e - 1; t >= 1; --t) {
             const long long o = (long long)t * ny + j;
-            if constexpr (LSS_PREFETCH_ROWS > 0) pf_l2(v.S(SL_G) + (long long)max(t - LSS_PREFETCH_ROWS, 1) * ny + j);
             x = Y[o] - ldg(v.S(SL_G) + o) * x;
             Y[o] = x;
         }
@@ -629,10 +603,6 @@ __device__ __forceinline__ void v_lines_tiled(const inst_view<T> &v, const T *__
         vtile_copy<VT + 1, VT, true>(&tl.io[0][0], inh, (T *)nullptr, i0, ny, nrows, tb, kk, lane);
         __syncwarp();
         if (act) {
-            if constexpr (LSS_PREFETCH_ROWS > 0) {
-                const long long of = (long long)min(tb + VT + LSS_PREFETCH_ROWS, e) * nx + i;
-                pf_l2(v.Vt(VL_LA) + of); pf_l2(v.Vt(VL_VC) + of); pf_l2(v.Vt(VL_VN) + of); pf_l2(v.Vt(VL_IB) + of);
-            }
 #pragma unroll
             for (int k = 0; k < VT; ++k) {
                 if (k < kk) {
@@ -2120,9 +2090,12 @@ template <typename T> double batch_typed<T>::ws_bytes_allowed()
         cudaGetLastError();
         return ws_cap > 0.0 ? ws_cap : 0.0;
     }
+    // the default (a quarter of the device) leaves at least half of what is free to the caller;
+    // a cap the caller sets is honoured up to 90 % of what is free
     const double held = d_ws.p ? static_cast<double>(d_ws.n) * sizeof(double) : 0.0;
-    const double cap = ws_cap > 0.0 ? ws_cap : 0.25 * static_cast<double>(total_b);
-    return std::min(cap, 0.5 * (static_cast<double>(free_b) + held));
+    const double avail = static_cast<double>(free_b) + held;
+    if (ws_cap > 0.0) return std::min(ws_cap, 0.9 * avail);
+    return std::min(0.25 * static_cast<double>(total_b), 0.5 * avail);
 }
 
 // CTA layouts (warp-group sizes, one hex digit per group) for `grid` CTAs of MAX_GROUP_WARPS

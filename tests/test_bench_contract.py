@@ -69,3 +69,10 @@ def test_recompute_fraction():
     # the adjoint's count is what the forward + adjoint capture leaves after its forward passes
     assert 0.0 < bench.CAPTURE_RF < 1.0
     assert 0.0 < bench.FP64_INSTR_ADJ < bench.CAPTURE_FWDADJ
+    assert 0.0 < bench.DRAM_BYTES_ADJ < bench.CAPTURE_DRAM_FWDADJ
+    # at the capture's own recomputed fraction the model gives back the captured figures
+    assert bench.per_gps(bench.FP64_INSTR_FWD, bench.FP64_INSTR_ADJ, 1, bench.CAPTURE_RF) == pytest.approx(
+        bench.CAPTURE_FWDADJ)
+    assert bench.per_gps(bench.DRAM_BYTES_FWD, bench.DRAM_BYTES_ADJ, 1, bench.CAPTURE_RF) == pytest.approx(
+        bench.CAPTURE_DRAM_FWDADJ)
+    assert bench.per_gps(bench.DRAM_BYTES_FWD, bench.DRAM_BYTES_ADJ, 0, 0.7) == bench.DRAM_BYTES_FWD
