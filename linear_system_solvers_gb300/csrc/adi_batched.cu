@@ -58,6 +58,11 @@ struct bdesc {
 // order[cls_start[c] .. cls_start[c] + cls_count[c]), longest first, pulled through counter[c].
 constexpr int MAX_GROUP_WARPS = 4;
 
+// Most chunks per line of the partitioned line solves of one large instance (wide path): a CTA
+// holds L lines x P chunks (L * P <= 1024 threads) and composes the chunks' carries through
+// shared arrays of MAX_CHUNKS x 33 values.
+constexpr int MAX_CHUNKS = 64;
+
 template <typename T> struct bparams {
     const bdesc *desc;
     const int *order;
@@ -976,7 +981,7 @@ __global__ void __launch_bounds__(1024) k_wide_s_chunk(const __grid_constant__ b
                                                         const T *Y2, T *Y, const T *__restrict__ hf,
                                                         const T *__restrict__ hb)
 {
-    __shared__ T sa[32][33], sb[32][33];
+    __shared__ T sa[MAX_CHUNKS][33], sb[MAX_CHUNKS][33];
     const bdesc d = p.desc[0];
     const inst_view<T> v = make_view(p, d);
     const int nx = d.nx, ny = d.ny, e = nx - 2, P = blockDim.y, c = threadIdx.y, lane = threadIdx.x;
@@ -1036,7 +1041,7 @@ __global__ void __launch_bounds__(1024) k_wide_v_chunk_plain(const __grid_consta
                                                         const T *b0, T *out, const T *__restrict__ hf,
                                                         const T *__restrict__ hb)
 {
-    __shared__ T sa[32][33], sb[32][33];
+    __shared__ T sa[MAX_CHUNKS][33], sb[MAX_CHUNKS][33];
     const bdesc d = p.desc[0];
     const inst_view<T> v = make_view(p, d);
     const int nx = d.nx, ny = d.ny, e = ny - 2, P = blockDim.y, c = threadIdx.y, lane = threadIdx.x;
@@ -1116,7 +1121,7 @@ __global__ void __launch_bounds__(1024) k_wide_v_chunk(const __grid_constant__ b
                                                         const T *b0, T *out, const T *__restrict__ hf,
                                                         const T *__restrict__ hb)
 {
-    __shared__ T sa[32][33], sb[32][33];
+    __shared__ T sa[MAX_CHUNKS][33], sb[MAX_CHUNKS][33];
     extern __shared__ unsigned char vt_raw[];
     const bdesc d = p.desc[0];
     const inst_view<T> v = make_view(p, d);
@@ -1409,7 +1414,7 @@ __global__ void __launch_bounds__(1024) k_wadj_v_chunk(const __grid_constant__ b
                                                         double *TMP, double *LV, double *acc_a, long long nacc,
                                                         const double *__restrict__ hz, const double *__restrict__ hw)
 {
-    __shared__ double sa[32][33], sb[32][33];
+    __shared__ double sa[MAX_CHUNKS][33], sb[MAX_CHUNKS][33];
     const bdesc d = p.desc[0];
     const inst_view<double> v = make_view(p, d);
     const int nx = d.nx, ny = d.ny, e = ny - 2, P = blockDim.y, c = threadIdx.y, lane = threadIdx.x;
@@ -1454,7 +1459,7 @@ __global__ void __launch_bounds__(1024) k_wadj_s_chunk(const __grid_constant__ b
                                                         double *UB, double *Y1B, double *acc_a, long long nacc, double tau,
                                                         const double *__restrict__ hz, const double *__restrict__ hw)
 {
-    __shared__ double sa[32][33], sb[32][33];
+    __shared__ double sa[MAX_CHUNKS][33], sb[MAX_CHUNKS][33];
     const bdesc d = p.desc[0];
     const inst_view<double> v = make_view(p, d);
     const int nx = d.nx, ny = d.ny, e = nx - 2, P = blockDim.y, c = threadIdx.y, lane = threadIdx.x;
@@ -2423,7 +2428,7 @@ template <typename T> int batch_typed<T>::set_wide_chunks(int ps, int pv, cudaSt
 {
     const bdesc &d = desc[0];
     const long long n = total_n;
-    auto ok = [](int P, int e) { return P >= 1 && P <= 32 && (P == 1 || e >= 4 * P); };
+    auto ok = [](int P, int e) { return P >= 1 && P <= MAX_CHUNKS && (P == 1 || e >= 4 * P); };
     if (!ok(ps, d.nx - 2) || !ok(pv, d.ny - 2)) return set_error(LSS_ADI_EINVAL, "wide: chunk count out of range");
     if ((ps > 1 || pv > 1) && !d_spk.p) LSS_CUDA_TRY(d_spk.alloc(4 * n), "wide: allocating chunk products");
     const bparams<T> p = params();
@@ -2448,6 +2453,9 @@ template <typename T> int batch_typed<T>::set_wide_chunks(int ps, int pv, cudaSt
     // the partitioned v sweep works in whole warps (shared-memory tiles moved by all 32 lanes):
     // lines x chunks must be a multiple of 32, which 32 lines per CTA always are
     if (pv > 1 && (wide_lv * pv) % 32 != 0) wide_lv = 32;
+    // at most 1024 threads per CTA: 64 chunks take at most 16 lines
+    while (ps > 1 && wide_ls * ps > 1024) wide_ls >>= 1;
+    while (pv > 1 && wide_lv * pv > 1024) wide_lv >>= 1;
     if (pv > 1) {
         // the limit belongs to the kernel, shared by every solver of the process: set it to what a
         // 1024-thread CTA needs, so that no solver lowers it under another one's launches
@@ -2461,7 +2469,8 @@ template <typename T> int batch_typed<T>::set_wide_chunks(int ps, int pv, cudaSt
 }
 
 // Chunk counts and lines per CTA of the two sweeps, each timed on its own (first S stage,
-// first v stage) over P = 1, 2, 4, ..., 32 (at least 4 rows per chunk) and L = 8, 16, 32.
+// first v stage) over P = 1, 2, 4, ..., MAX_CHUNKS (at least 4 rows per chunk) and L = 8, 16,
+// 32 (L * P <= 1024).
 template <typename T> int batch_typed<T>::autotune_wide(cudaStream_t s)
 {
     const bdesc &d = desc[0];
@@ -2484,11 +2493,12 @@ template <typename T> int batch_typed<T>::autotune_wide(cudaStream_t s)
         cudaEventElapsedTime(&ms, e0, e1);
         return ms;
     };
-    for (int P = 1; P <= 32 && rc == LSS_ADI_OK; P *= 2) {
+    for (int P = 1; P <= MAX_CHUNKS && rc == LSS_ADI_OK; P *= 2) {
         const bool okS = (P == 1 || d.nx - 2 >= 4 * P), okV = (P == 1 || d.ny - 2 >= 4 * P);
         if (!okS && !okV) break;
         for (int L : {8, 16, 32}) {
             if (P == 1 && L != 32) continue; // thread per line: L unused
+            if (L * P > 1024) continue;
             rc = set_wide_chunks(okS ? P : 1, okV ? P : 1, s, L, L);
             if (rc) break;
             if (okS) {

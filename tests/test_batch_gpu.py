@@ -142,16 +142,42 @@ def test_partitioned_line_solves_match_line_per_thread(lss, oracle, scheme, chun
     assert rel_err(got, want) < fp64_tol(want, p.s_hi)
 
 
+@pytest.mark.parametrize("scheme", ["cs", "hv"])
+def test_sixty_four_chunks_match_line_per_thread(lss, oracle, scheme):
+    """64 chunks per line (CTAs of 16 lines x 64 chunks) on a grid with at least 4 rows per chunk
+    in both directions, against the thread-per-line solve: rounding-level differences, bounded as
+    in the test above."""
+    kw = dict(model="heston", kappa=2.0, theta_v=0.05, sigma=0.4, rho=-0.3, rate=0.02, strike=100.0, maturity=0.25,
+              s_lo=0.0, s_hi=200.0, v_lo=0.0, v_hi=1.2, nx=522, ny=300, nt=9, scheme=scheme, acc_point=100.0, **NU)
+    p = lss.HestonProblem(**kw)
+    s = lss.ImplicitHestonSolver(p, precision="f64", arith="fast")
+    assert s.line_chunks(64, 64) == (64, 64)
+    got, val = s.solve(graph=True)
+    ref, rval = lss.ImplicitHestonSolver(dataclasses.replace(p, line_per_thread=True), precision="f64",
+                                         arith="fast").solve()
+    op = oracle_of(oracle, p)
+    want = oracle.solve(op, "f64")
+    x, _ = oracle.grid(op, "f64")
+    pay = np.maximum(x[:, None] - p.strike, 0.0) * np.ones((1, p.ny))
+    noisy = pay * (1.0 + 1e-15 * np.random.default_rng(1).standard_normal(pay.shape))
+    amp = rel_err(oracle.solve(op, "f64", payoff=noisy), want)
+    tol = max(1e-13, 100.0 * amp)
+    assert rel_err(got, ref) < tol
+    assert abs(val - rval) <= tol * max(1.0, abs(rval))
+    assert rel_err(got, want) < fp64_tol(want, p.s_hi)
+
+
 def test_partition_autotuner_and_limits(lss):
     p = lss.HestonProblem(scheme="hv", nx=300, ny=100, nt=5, nonuniform=True, acc_point=100.0, alpha_scale=10.0,
                           beta_scale=24.0)
     s = lss.ImplicitHestonSolver(p, precision="f64", arith="fast")
     ps, pv = s.line_chunks(0, 0)
-    assert 1 <= ps <= 32 and 1 <= pv <= 32
+    assert 1 <= ps <= 64 and 1 <= pv <= 64
     from linear_system_solvers_gb300 import _lib as L
 
+    assert s.line_chunks(64, 1) == (64, 1)  # 298 rows: 64 chunks of at least 4
     with pytest.raises(L.LssError):
-        s.line_chunks(64, 1)  # more than 32 chunks
+        s.line_chunks(128, 1)  # more than 64 chunks
     with pytest.raises(L.LssError):
         s.line_chunks(1, 32)  # 98 rows: fewer than 4 per chunk
     ref = lss.ImplicitHestonSolver(p, precision="f64", arith="reference")
