@@ -50,7 +50,7 @@ FP64_INSTR_ADJ = CAPTURE_FWDADJ - FP64_INSTR_FWD * (1.0 + CAPTURE_RF)
 
 # Adjoint workspace cap of the timed batch, as a fraction of the device memory (the library's
 # default is a quarter; a larger cap stores more stage values and recomputes fewer steps)
-WS_FRACTION = 0.6
+WS_FRACTION = 0.8
 
 
 def per_gps(fwd, adj, mode, rf):
