@@ -19,20 +19,11 @@
 #pragma once
 // Included by adi_batched.cu inside namespace lss_gb300, after the forward stage functions.
 
-// A thread's parameter sums: the S-line sums, already scaled (r, kappa, theta, sigma, rho), and
-// the v-line raw sums (sum mu (dm-dn) ek, (dm-dn) et, (dm-dn) es, (2dc-dm-dn) bs, dc).
-enum { ACC_R = 0, ACC_KAPPA, ACC_THETA, ACC_SIGMA, ACC_RHO, ACC_VK, ACC_VT, ACC_VS1, ACC_VS2, ACC_VB, ACC_COUNT };
-// In registers: the wide kernels, which keep the sums in global memory between launches.
 struct adj_acc {
-    double a[ACC_COUNT];
-    __device__ __forceinline__ double &operator[](int k) { return a[k]; }
-    __device__ __forceinline__ double operator[](int k) const { return a[k]; }
-};
-// In shared memory, this thread's column of a [ACC_COUNT][S] array: the persistent kernel, where
-// the sums would otherwise hold 20 registers through every stage of the adjoint.
-template <int S> struct adj_acc_sh {
-    double *p;
-    __device__ __forceinline__ double &operator[](int k) const { return p[k * S]; }
+    // S-line sums, already scaled: r, kappa, theta, sigma, rho
+    double s[5];
+    // v-line raw sums: sum mu (dm-dn) ek, (dm-dn) et, (dm-dn) es, (2dc-dm-dn) bs, dc
+    double vk, vt, vs1, vs2, vb;
 };
 
 // B2^T: fold the S_max extrapolation row into rows nx-2 / nx-3; clear rows 0 and nx-1 of UB
@@ -58,26 +49,25 @@ __device__ __forceinline__ void adj_b2(const inst_view<double> &v, double *__res
 }
 
 // Parameter sums of one v-line point: mu = ib * w, dm / dc / dn = (in - out) at t-1, t, t+1.
-template <typename ACC>
 __device__ __forceinline__ void adj_v_sum(const inst_view<double> &v, int t, double mu, double dm, double dc, double dn,
-                                          ACC &acc)
+                                          adj_acc &acc)
 {
     const double q = mu * (dm - dn);
-    acc[ACC_VK] += q * __ldg(v.Yv(Y_EK) + t);
-    acc[ACC_VT] += q * __ldg(v.Yv(Y_ET) + t);
-    acc[ACC_VS1] += q * __ldg(v.Yv(Y_ES) + t);
-    acc[ACC_VS2] += mu * (2.0 * dc - dm - dn) * __ldg(v.Yv(Y_BS) + t);
-    acc[ACC_VB] += mu * dc;
+    acc.vk += q * __ldg(v.Yv(Y_EK) + t);
+    acc.vt += q * __ldg(v.Yv(Y_ET) + t);
+    acc.vs1 += q * __ldg(v.Yv(Y_ES) + t);
+    acc.vs2 += mu * (2.0 * dc - dm - dn) * __ldg(v.Yv(Y_BS) + t);
+    acc.vb += mu * dc;
 }
 
 // V-line stage adjoint.  XB: adjoint of the stage output (rows i, incl. the lo copy at t=0);
 // in/out: the stage's `in` array and its output; INB (+)= adjoint of `in`; INHB (+)= adjoint
 // of `inh`; LV (+)= adjoint of the line's lo value.
-template <bool FIRST, typename ACC>
+template <bool FIRST>
 __device__ __forceinline__ void adj_v(const inst_view<double> &v, const double *__restrict__ in,
                                       const double *__restrict__ out, const double *__restrict__ XB,
                                       double *__restrict__ INB, double *__restrict__ INHB, double *__restrict__ TMP,
-                                      double *__restrict__ LV, ACC &acc, int l0, int ls)
+                                      double *__restrict__ LV, adj_acc &acc, int l0, int ls)
 {
     const int nx = v.nx, ny = v.ny, e = ny - 2;
     for (int i = 1 + l0; i <= nx - 2; i += ls) {
@@ -201,9 +191,9 @@ __device__ __forceinline__ void adj_s_point(const inst_view<double> &v, s_sums &
     }
 }
 // The line's sums, weighed by the stage's constants and the v-direction factors of the line.
-template <int KIND, int SCH, typename ACC>
+template <int KIND, int SCH>
 __device__ __forceinline__ void adj_s_line(const inst_view<double> &v, const bdesc &d, int j, const s_sums &p,
-                                           double tau, bool sabr, ACC &acc)
+                                           double tau, bool sabr, adj_acc &acc)
 {
     double A, B, Q, D, E, Aa, Dd;
     if constexpr (KIND == 1) {
@@ -226,14 +216,14 @@ __device__ __forceinline__ void adj_s_line(const inst_view<double> &v, const bde
     }
     const double ek = __ldg(v.Yv(Y_EK) + j), et = __ldg(v.Yv(Y_ET) + j), es = __ldg(v.Yv(Y_ES) + j);
     const double bs = __ldg(v.Yv(Y_BS) + j), hy = __ldg(v.Yv(Y_HY) + j);
-    acc[0] += d.a_delta * A + d.a_halfk * B;
+    acc.s[0] += d.a_delta * A + d.a_halfk * B;
     if (sabr) // D(t) terms of a^, d^ and c^
-        acc[0] += tau * d.a_omb *
+        acc.s[0] += tau * d.a_omb *
                     (__ldg(v.Yv(Y_HV2) + j) * (2.0 * d.a_delta * Dd - 2.0 * d.a_alphat * Aa) - d.a_rho * d.a_sigma * hy * E);
-    acc[1] += d.a_ni * ek * Q;
-    acc[2] += d.a_ni * et * Q;
-    acc[3] += d.a_ni * es * Q + d.a_betat * bs * D + d.a_rho * hy * E;
-    acc[4] += d.a_sigma * hy * E;
+    acc.s[1] += d.a_ni * ek * Q;
+    acc.s[2] += d.a_ni * et * Q;
+    acc.s[3] += d.a_ni * es * Q + d.a_betat * bs * D + d.a_rho * hy * E;
+    acc.s[4] += d.a_sigma * hy * E;
 }
 
 // S-line stage adjoint.  KIND 1: S1 (explicit operator on U, output Y1).  KIND 2: second S
@@ -241,13 +231,13 @@ __device__ __forceinline__ void adj_s_line(const inst_view<double> &v, const bde
 // right-hand-side adjoint w; LS/HS the lo/hi adjoints of the line.  The along-line terms of
 // the second stage act on U for CS/MCS and on Y1 for HV, whose right-hand side is
 // (I - theta k A1) Y1 + (zeta k A - theta k A1)(Y2 - U) (hundsdorfer_verwer_method.hpp:128-194).
-template <int KIND, int SCH, typename ACC>
+template <int KIND, int SCH>
 __device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d, const double *__restrict__ U,
                                       const double *__restrict__ Y1, const double *__restrict__ Y2,
                                       const double *__restrict__ Yo, const double *__restrict__ XB,
                                       double *__restrict__ FB, double *__restrict__ TMP, double *__restrict__ LS,
                                       double *__restrict__ HS, double *__restrict__ UB, double *__restrict__ Y1B,
-                                      ACC &acc, double tau, int l0, int ls)
+                                      adj_acc &acc, double tau, int l0, int ls)
 {
     constexpr bool hv = SCH == LSS_ADI_HUNDSDORFER_VERWER;
     const int nx = v.nx, ny = v.ny, e = nx - 2;
@@ -316,9 +306,8 @@ __device__ __forceinline__ void adj_s(const inst_view<double> &v, const bdesc &d
 // B1^T at grid point (p, q <= 2): the adjoint of the explicit v = v_lo boundary column, whose
 // values are the lo ends of the v lines (bbar0(i) = sum of LV over lines i' with imap[i'] = i),
 // with its parameter sensitivities (D, E, F of the v = v_lo line) at q = 0.
-template <typename ACC>
 __device__ __forceinline__ double adj_b1_terms(const inst_view<double> &v, const bdesc &d, const double *__restrict__ U,
-                                               const double *__restrict__ LV, ACC &acc, double tau, int p, int q)
+                                               const double *__restrict__ LV, adj_acc &acc, double tau, int p, int q)
 {
     const int nx = v.nx, ny = v.ny;
     auto B0 = [&](int i) -> double {
@@ -341,10 +330,10 @@ __device__ __forceinline__ double adj_b1_terms(const inst_view<double> &v, const
             const double ee = d.a_ni * bb * (4.0 * u1 - 3.0 * u0 - u2);
             double hd = __ldg(v.X(X_HX) + p);
             if (d.model == LSS_ADI_SABR) hd += 2.0 * d.a_omb * tau * __ldg(v.Yv(Y_HV2)) * __ldg(v.X(X_HDD) + p);
-            acc[0] += bb * (d.a_delta * hd * (up - um) - d.a_k * u0);
-            acc[1] += ee * __ldg(v.Yv(Y_EK));
-            acc[2] += ee * __ldg(v.Yv(Y_ET));
-            acc[3] += ee * __ldg(v.Yv(Y_ES));
+            acc.s[0] += bb * (d.a_delta * hd * (up - um) - d.a_k * u0);
+            acc.s[1] += ee * __ldg(v.Yv(Y_EK));
+            acc.s[2] += ee * __ldg(v.Yv(Y_ET));
+            acc.s[3] += ee * __ldg(v.Yv(Y_ES));
         }
     }
     return val;
@@ -354,10 +343,10 @@ __device__ __forceinline__ double adj_b1_terms(const inst_view<double> &v, const
 // lo/hi adjoints of the S lines (lsum / hsum of column q, added on rows 0 / nx-1), and for
 // KIND 1 the adjoint of the explicit v = v_lo boundary column (B1^T) with its parameter
 // sensitivities.  One grid point (p, q) per call.
-template <int KIND, typename ACC>
+template <int KIND>
 __device__ __forceinline__ void adj_gather_point(const inst_view<double> &v, const bdesc &d, const double *__restrict__ U,
                                                  const double *__restrict__ FB, const double *__restrict__ LV,
-                                                 double *__restrict__ UB, double *__restrict__ Y2B, ACC &acc,
+                                                 double *__restrict__ UB, double *__restrict__ Y2B, adj_acc &acc,
                                                  double tau, int p, int q, double lsum, double hsum)
 {
     const int nx = v.nx, ny = v.ny;
@@ -411,11 +400,11 @@ __device__ __forceinline__ void adj_line_ends(const inst_view<double> &v, const 
 // FB and the tables are zero on the boundary rows and columns of an instance (never written), so
 // only the rows and columns outside the instance need guards.  Each row's table and FB values are
 // loaded once instead of once per neighbour.
-template <int KIND, int SCH, typename ACC>
+template <int KIND, int SCH>
 __device__ __forceinline__ void adj_gather(const inst_view<double> &v, const bdesc &d, const double *__restrict__ U,
                                            const double *__restrict__ FB, const double *__restrict__ LS,
                                            const double *__restrict__ HS, const double *__restrict__ LV,
-                                           double *__restrict__ UB, double *__restrict__ Y2B, ACC &acc, double tau,
+                                           double *__restrict__ UB, double *__restrict__ Y2B, adj_acc &acc, double tau,
                                            int l0, int ls)
 {
     const int nx = v.nx, ny = v.ny;
@@ -479,9 +468,8 @@ __device__ __forceinline__ void adj_gather(const inst_view<double> &v, const bde
 // B1^T terms of columns 0..2 (adj_b1_terms), spread over the CTA's threads by row after the
 // column walk of adj_gather<1> (which would otherwise leave the threads of columns 0..2 walking
 // their columns alone with this extra work, the rest of their warp idle).
-template <typename ACC>
 __device__ __forceinline__ void adj_b1_pass(const inst_view<double> &v, const bdesc &d, const double *__restrict__ U,
-                                            const double *__restrict__ LV, double *__restrict__ UB, ACC &acc,
+                                            const double *__restrict__ LV, double *__restrict__ UB, adj_acc &acc,
                                             double tau, int l0, int ls)
 {
     const int nx = v.nx, ny = v.ny;
@@ -493,11 +481,11 @@ __device__ __forceinline__ void adj_b1_pass(const inst_view<double> &v, const bd
 // Adjoint of one time step of scheme SCH: VB = adjoint of the step output (modified in place),
 // UB receives the adjoint of the step input.  U/Y1/Y2/Y3/Vo: the step's input, stage outputs and
 // output.  Work split over the threads of group g, group barriers between the stages.
-template <int SCH, typename ACC>
+template <int SCH>
 __device__ __forceinline__ void adj_step(const inst_view<double> &v, const bdesc &d, const double *U, const double *Y1,
                                          const double *Y2, const double *Y3, const double *Vo, double *VB, double *UB,
                                          double *Y1B, double *Y2B, double *Y3B, double *FB, double *TMP, double *LV,
-                                         double *LS, double *HS, ACC &acc, double tau, const grp &g)
+                                         double *LS, double *HS, adj_acc &acc, double tau, const grp &g)
 {
     const int l0 = g.t, ls = g.n;
     constexpr bool hv = SCH == LSS_ADI_HUNDSDORFER_VERWER;

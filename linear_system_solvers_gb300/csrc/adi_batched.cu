@@ -758,9 +758,10 @@ __global__ void __launch_bounds__(BATCH_CTA, 8) k_batch_forward(const __grid_con
 // last segment), followed by the adjoint steps of the segment in reverse order.
 // Results: value, the 5 parameter sensitivities, the final surface (state U arena) and
 // dV/d(initial condition) (state V arena).  A group of w warps works in w consecutive workspace
-// slices.  Register budget ~80 per thread (6 CTAs of 4 warps per SM).
+// slices.  Register budget 96 per thread (5 CTAs of 4 warps per SM): fewer spills than at 80, and
+// fewer resident CTAs leave each more workspace, so the plan recomputes fewer steps.
 #ifndef LSS_FWDADJ_MIN_CTAS
-#define LSS_FWDADJ_MIN_CTAS 6
+#define LSS_FWDADJ_MIN_CTAS 5
 #endif
 template <int SCH>
 __global__ void __launch_bounds__(BATCH_CTA, LSS_FWDADJ_MIN_CTAS) k_batch_fwdadj(const __grid_constant__ bparams<double> p)
@@ -768,7 +769,6 @@ __global__ void __launch_bounds__(BATCH_CTA, LSS_FWDADJ_MIN_CTAS) k_batch_fwdadj
     __shared__ int s_idx[MAX_GROUP_WARPS];
     __shared__ int s_bad[MAX_GROUP_WARPS];
     __shared__ double red[MAX_GROUP_WARPS][5];
-    __shared__ double s_acc[ACC_COUNT][BATCH_CTA]; // each thread's parameter sums
     const grp g = make_grp(p.layout[blockIdx.x]);
     const int gw = g.n / 32;
     double *ws = p.ws + (long long)(blockIdx.x * MAX_GROUP_WARPS + g.warp0) * p.ws_per_warp;
@@ -852,8 +852,9 @@ __global__ void __launch_bounds__(BATCH_CTA, LSS_FWDADJ_MIN_CTAS) k_batch_fwdadj
         }
         g.sync();
         // reverse sweep over the segments
-        const adj_acc_sh<BATCH_CTA> acc{&s_acc[0][threadIdx.x]};
-        for (int q = 0; q < ACC_COUNT; ++q) acc[q] = 0.0;
+        adj_acc acc;
+        for (int q = 0; q < 5; ++q) acc.s[q] = 0.0;
+        acc.vk = acc.vt = acc.vs1 = acc.vs2 = acc.vb = 0.0;
         double *ub = UB, *vb = VB;
         for (int sgi = nseg - 1; sgi >= 0; --sgi) {
             const int n0 = sgi * c;
@@ -878,11 +879,11 @@ __global__ void __launch_bounds__(BATCH_CTA, LSS_FWDADJ_MIN_CTAS) k_batch_fwdadj
         const double th = d.a_theta, ni = d.a_ni;
         double gr[5];
         // order in the output: kappa, theta, sigma, rho, r
-        gr[0] = acc[1] + ni * th * acc[ACC_VK];
-        gr[1] = acc[2] + ni * th * acc[ACC_VT];
-        gr[2] = acc[3] + ni * th * acc[ACC_VS1] + d.a_betat * th * acc[ACC_VS2];
-        gr[3] = acc[4];
-        gr[4] = acc[0] + d.a_halfk * th * acc[ACC_VB];
+        gr[0] = acc.s[1] + ni * th * acc.vk;
+        gr[1] = acc.s[2] + ni * th * acc.vt;
+        gr[2] = acc.s[3] + ni * th * acc.vs1 + d.a_betat * th * acc.vs2;
+        gr[3] = acc.s[4];
+        gr[4] = acc.s[0] + d.a_halfk * th * acc.vb;
         // sum over the group: within each warp by shuffles, then the warps in order
         for (int q = 0; q < 5; ++q)
             for (int off = 16; off > 0; off >>= 1) gr[q] += __shfl_down_sync(0xffffffffu, gr[q], off);
@@ -1279,21 +1280,21 @@ __global__ void __launch_bounds__(1024) k_wide_v_chunk(const __grid_constant__ b
 // ------------------------------------------------------------------------------------------
 __device__ __forceinline__ void acc_load(adj_acc &acc, const double *a, long long nthr, long long t)
 {
-    for (int q = 0; q < 5; ++q) acc[q] = a[q * nthr + t];
-    acc[ACC_VK] = a[5 * nthr + t];
-    acc[ACC_VT] = a[6 * nthr + t];
-    acc[ACC_VS1] = a[7 * nthr + t];
-    acc[ACC_VS2] = a[8 * nthr + t];
-    acc[ACC_VB] = a[9 * nthr + t];
+    for (int q = 0; q < 5; ++q) acc.s[q] = a[q * nthr + t];
+    acc.vk = a[5 * nthr + t];
+    acc.vt = a[6 * nthr + t];
+    acc.vs1 = a[7 * nthr + t];
+    acc.vs2 = a[8 * nthr + t];
+    acc.vb = a[9 * nthr + t];
 }
 __device__ __forceinline__ void acc_store(const adj_acc &acc, double *a, long long nthr, long long t)
 {
-    for (int q = 0; q < 5; ++q) a[q * nthr + t] = acc[q];
-    a[5 * nthr + t] = acc[ACC_VK];
-    a[6 * nthr + t] = acc[ACC_VT];
-    a[7 * nthr + t] = acc[ACC_VS1];
-    a[8 * nthr + t] = acc[ACC_VS2];
-    a[9 * nthr + t] = acc[ACC_VB];
+    for (int q = 0; q < 5; ++q) a[q * nthr + t] = acc.s[q];
+    a[5 * nthr + t] = acc.vk;
+    a[6 * nthr + t] = acc.vt;
+    a[7 * nthr + t] = acc.vs1;
+    a[8 * nthr + t] = acc.vs2;
+    a[9 * nthr + t] = acc.vb;
 }
 
 __global__ void k_wadj_b2(const __grid_constant__ bparams<double> p, double *VB, double *UB)
@@ -1545,8 +1546,8 @@ __global__ void k_wadj_gather2d(const __grid_constant__ bparams<double> p, const
     if (q == 0) {
         acc_load(acc, acc_a, nacc, pr);
     } else {
-        for (int k = 0; k < 5; ++k) acc[k] = 0.0;
-        acc[ACC_VK] = acc[ACC_VT] = acc[ACC_VS1] = acc[ACC_VS2] = acc[ACC_VB] = 0.0;
+        for (int k = 0; k < 5; ++k) acc.s[k] = 0.0;
+        acc.vk = acc.vt = acc.vs1 = acc.vs2 = acc.vb = 0.0;
     }
     adj_gather_point<KIND>(v, d, U, FB, LV, UB, Y2B, acc, tau, pr, q, lsum, hsum);
     if (q == 0) acc_store(acc, acc_a, nacc, pr);
