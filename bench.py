@@ -1008,6 +1008,9 @@ def time_genuine_mcs(lss, problems, ws_cap, stream):
     """The timed batch once more with a genuine modified Craig-Sneyd weight: zeta = 1/3 instead of
     theta = 1/2 (at zeta = theta the scheme is Craig-Sneyd's and runs its stencil), forward +
     adjoint at the same workspace cap, one timed launch after the autotuner's and a warm-up."""
+    import numpy as np
+    import torch
+
     from linear_system_solvers_gb300.batch import grid_point_steps
 
     probs = [dataclasses.replace(p, zeta=1.0 / 3.0) for p in problems]

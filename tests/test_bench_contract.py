@@ -75,3 +75,29 @@ def test_recompute_fraction():
     d = bench.per_gps(bench.DRAM_BYTES_FWD, bench.DRAM_BYTES_ADJ, 1, 0.7) - bench.per_gps(
         bench.DRAM_BYTES_FWD, bench.DRAM_BYTES_ADJ, 1, 0.2)
     assert d == pytest.approx(0.5 * bench.DRAM_BYTES_FWD)
+
+
+def test_bench_functions_only_use_names_that_exist():
+    """Every global name a function of bench.py reads is defined at module level or is a
+    builtin (bench.py imports torch and the package inside functions, so a leg that forgets its
+    own import would only fail on a GPU)."""
+    import builtins
+    import symtable
+
+    import bench
+
+    src = open(os.path.join(ROOT, "bench.py")).read()
+    missing = []
+
+    def walk(tab):
+        for child in tab.get_children():
+            if child.get_type() == "function":
+                for sym in child.get_symbols():
+                    if sym.is_global() and sym.is_referenced() and not sym.is_assigned():
+                        name = sym.get_name()
+                        if not hasattr(bench, name) and not hasattr(builtins, name):
+                            missing.append((child.get_name(), name))
+            walk(child)
+
+    walk(symtable.symtable(src, "bench.py", "exec"))
+    assert not missing, missing
