@@ -41,7 +41,7 @@ CAPTURE_RF = 0.4898
 # DRAM bytes read + written (dram__bytes_read.sum + dram__bytes_write.sum): k_batch_forward,
 # k_batch_fwdadj
 DRAM_BYTES_FWD = 339.1
-CAPTURE_DRAM_FWDADJ = 1035.8
+CAPTURE_DRAM_FWDADJ = 1026.9
 DRAM_BYTES_ADJ = CAPTURE_DRAM_FWDADJ - DRAM_BYTES_FWD * (1.0 + CAPTURE_RF)
 # FP64 instructions, thread level (smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum)
 FP64_INSTR_FWD = 32.07
