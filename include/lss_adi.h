@@ -208,7 +208,7 @@ int lss_adi_grid(const lss_adi_handle *h, void *x, void *y);
 
 /* Partitioned line solves of a LSS_ADI_ARITH_FAST single instance: every S line is cut into
  * s_chunks and every v line into v_chunks pieces solved concurrently (1 = thread per line;
- * at most 64; at least 4 rows per chunk).  0 for either picks it, with the number of lines
+ * at most 128; at least 4 rows per chunk).  0 for either picks it, with the number of lines
  * per CTA, by timing the sweeps (the autotuner lss_adi_create runs by default); a count set
  * here gets the lines per CTA that give every SM a CTA.  Neither changes the arithmetic of a
  * chunk: results depend on the chunk counts at rounding level only.  out_s / out_v (may be NULL) receive the

@@ -59,9 +59,14 @@ struct bdesc {
 constexpr int MAX_GROUP_WARPS = 4;
 
 // Most chunks per line of the partitioned line solves of one large instance (wide path): a CTA
-// holds L lines x P chunks (L * P <= 1024 threads) and composes the chunks' carries through
-// shared arrays of MAX_CHUNKS x 33 values.
-constexpr int MAX_CHUNKS = 64;
+// holds L lines x P chunks (L * P <= 1024 threads) and composes the chunks' carries through two
+// shared arrays of 1024 values, indexed [chunk][line] (carry2d).
+constexpr int MAX_CHUNKS = 128;
+template <typename T> struct carry2d {
+    T *p;
+    int L; // lines per CTA (blockDim.x)
+    __device__ __forceinline__ T *operator[](int c) const { return p + c * L; }
+};
 
 template <typename T> struct bparams {
     const bdesc *desc;
@@ -982,7 +987,8 @@ __global__ void __launch_bounds__(1024) k_wide_s_chunk(const __grid_constant__ b
                                                         const T *Y2, T *Y, const T *__restrict__ hf,
                                                         const T *__restrict__ hb)
 {
-    __shared__ T sa[MAX_CHUNKS][33], sb[MAX_CHUNKS][33];
+    __shared__ T sa_s[1024], sb_s[1024];
+    const carry2d<T> sa{sa_s, static_cast<int>(blockDim.x)}, sb{sb_s, static_cast<int>(blockDim.x)};
     const bdesc d = p.desc[0];
     const inst_view<T> v = make_view(p, d);
     const int nx = d.nx, ny = d.ny, e = nx - 2, P = blockDim.y, c = threadIdx.y, lane = threadIdx.x;
@@ -1042,7 +1048,8 @@ __global__ void __launch_bounds__(1024) k_wide_v_chunk_plain(const __grid_consta
                                                         const T *b0, T *out, const T *__restrict__ hf,
                                                         const T *__restrict__ hb)
 {
-    __shared__ T sa[MAX_CHUNKS][33], sb[MAX_CHUNKS][33];
+    __shared__ T sa_s[1024], sb_s[1024];
+    const carry2d<T> sa{sa_s, static_cast<int>(blockDim.x)}, sb{sb_s, static_cast<int>(blockDim.x)};
     const bdesc d = p.desc[0];
     const inst_view<T> v = make_view(p, d);
     const int nx = d.nx, ny = d.ny, e = ny - 2, P = blockDim.y, c = threadIdx.y, lane = threadIdx.x;
@@ -1122,7 +1129,8 @@ __global__ void __launch_bounds__(1024) k_wide_v_chunk(const __grid_constant__ b
                                                         const T *b0, T *out, const T *__restrict__ hf,
                                                         const T *__restrict__ hb)
 {
-    __shared__ T sa[MAX_CHUNKS][33], sb[MAX_CHUNKS][33];
+    __shared__ T sa_s[1024], sb_s[1024];
+    const carry2d<T> sa{sa_s, static_cast<int>(blockDim.x)}, sb{sb_s, static_cast<int>(blockDim.x)};
     extern __shared__ unsigned char vt_raw[];
     const bdesc d = p.desc[0];
     const inst_view<T> v = make_view(p, d);
@@ -1366,8 +1374,8 @@ __device__ __forceinline__ void adj_chunk_solve(double *__restrict__ TMP, long l
                                                 const double *__restrict__ XB, const double *__restrict__ G,
                                                 const double *__restrict__ LA, const double *__restrict__ hz,
                                                 const double *__restrict__ hw, long long tab, long long ts, int e,
-                                                int t0, int t1, int c, int P, int lane, bool act, double (*sa)[33],
-                                                double (*sb)[33])
+                                                int t0, int t1, int c, int P, int lane, bool act,
+                                                const carry2d<double> &sa, const carry2d<double> &sb)
 {
     double z = 0.0;
     if (act) {
@@ -1415,7 +1423,8 @@ __global__ void __launch_bounds__(1024) k_wadj_v_chunk(const __grid_constant__ b
                                                         double *TMP, double *LV, double *acc_a, long long nacc,
                                                         const double *__restrict__ hz, const double *__restrict__ hw)
 {
-    __shared__ double sa[MAX_CHUNKS][33], sb[MAX_CHUNKS][33];
+    __shared__ double sa_s[1024], sb_s[1024];
+    const carry2d<double> sa{sa_s, static_cast<int>(blockDim.x)}, sb{sb_s, static_cast<int>(blockDim.x)};
     const bdesc d = p.desc[0];
     const inst_view<double> v = make_view(p, d);
     const int nx = d.nx, ny = d.ny, e = ny - 2, P = blockDim.y, c = threadIdx.y, lane = threadIdx.x;
@@ -1460,7 +1469,8 @@ __global__ void __launch_bounds__(1024) k_wadj_s_chunk(const __grid_constant__ b
                                                         double *UB, double *Y1B, double *acc_a, long long nacc, double tau,
                                                         const double *__restrict__ hz, const double *__restrict__ hw)
 {
-    __shared__ double sa[MAX_CHUNKS][33], sb[MAX_CHUNKS][33];
+    __shared__ double sa_s[1024], sb_s[1024];
+    const carry2d<double> sa{sa_s, static_cast<int>(blockDim.x)}, sb{sb_s, static_cast<int>(blockDim.x)};
     const bdesc d = p.desc[0];
     const inst_view<double> v = make_view(p, d);
     const int nx = d.nx, ny = d.ny, e = nx - 2, P = blockDim.y, c = threadIdx.y, lane = threadIdx.x;

@@ -228,7 +228,7 @@ def test_wide_adjoint_partitioned_solves_match_line_per_thread(lss, key):
     p = lss.HestonProblem(**CASES[key])
     ref = lss.ImplicitHestonSolver(dataclasses.replace(p, line_per_thread=True), precision="f64", arith="fast")
     v0, g0, l0 = ref.adjoint()
-    for chunks in ((4, 2), (16, 8), (32, 4), (64, 2)):
+    for chunks in ((4, 2), (16, 8), (32, 4), (64, 2)):  # 64 chunks: CTAs of 16 lines
         s = lss.ImplicitHestonSolver(p, precision="f64", arith="fast")
         assert s.line_chunks(*chunks) == chunks
         v, g, lam = s.adjoint()

@@ -143,15 +143,16 @@ def test_partitioned_line_solves_match_line_per_thread(lss, oracle, scheme, chun
 
 
 @pytest.mark.parametrize("scheme", ["cs", "hv"])
-def test_sixty_four_chunks_match_line_per_thread(lss, oracle, scheme):
-    """64 chunks per line (CTAs of 16 lines x 64 chunks) on a grid with at least 4 rows per chunk
-    in both directions, against the thread-per-line solve: rounding-level differences, bounded as
-    in the test above."""
+@pytest.mark.parametrize("chunks", [(64, 64), (128, 32)])
+def test_many_chunks_match_line_per_thread(lss, oracle, scheme, chunks):
+    """64 and 128 chunks per line (CTAs of 16 lines x 64 chunks, 8 x 128) on a grid with at least 4
+    rows per chunk, against the thread-per-line solve: rounding-level differences, bounded as in
+    the test above."""
     kw = dict(model="heston", kappa=2.0, theta_v=0.05, sigma=0.4, rho=-0.3, rate=0.02, strike=100.0, maturity=0.25,
               s_lo=0.0, s_hi=200.0, v_lo=0.0, v_hi=1.2, nx=522, ny=300, nt=9, scheme=scheme, acc_point=100.0, **NU)
     p = lss.HestonProblem(**kw)
     s = lss.ImplicitHestonSolver(p, precision="f64", arith="fast")
-    assert s.line_chunks(64, 64) == (64, 64)
+    assert s.line_chunks(*chunks) == chunks
     got, val = s.solve(graph=True)
     ref, rval = lss.ImplicitHestonSolver(dataclasses.replace(p, line_per_thread=True), precision="f64",
                                          arith="fast").solve()
@@ -177,7 +178,9 @@ def test_partition_autotuner_and_limits(lss):
 
     assert s.line_chunks(64, 1) == (64, 1)  # 298 rows: 64 chunks of at least 4
     with pytest.raises(L.LssError):
-        s.line_chunks(128, 1)  # more than 64 chunks
+        s.line_chunks(128, 1)  # 298 rows: fewer than 4 per chunk
+    with pytest.raises(L.LssError):
+        s.line_chunks(256, 1)  # more than 128 chunks
     with pytest.raises(L.LssError):
         s.line_chunks(1, 32)  # 98 rows: fewer than 4 per chunk
     ref = lss.ImplicitHestonSolver(p, precision="f64", arith="reference")
