@@ -131,7 +131,7 @@ typedef struct lss_adi_problem {
 #define LSS_ADI_OPT_LINE_PER_THREAD 4
 /* WIDE_ADJOINT: lss_adi_adjoint runs the forward + adjoint of this instance as one kernel per
  *   stage over the whole GPU (partitioned line solves unless LINE_PER_THREAD) whatever its
- *   size, instead of one CTA for instances of up to 256 x 160 points. */
+ *   size, instead of one warp group of the batched kernel for instances of up to 256 x 160 points. */
 #define LSS_ADI_OPT_WIDE_ADJOINT 8
 
 /*
@@ -221,8 +221,9 @@ void lss_adi_destroy(lss_adi_handle *h);
 /* --- batched uneven instances ---------------------------------------------------------- */
 
 /* Many independent problems with their own sizes, steps and parameters, advanced by one
- * persistent kernel (one CTA per instance at a time, longest first, pulled from a device
- * work counter).  All problems share precision (FP64 or FP32); arith must be FAST. */
+ * persistent kernel per splitting scheme present (warp groups of 1-4 warps, about one thread
+ * per S line, each on one instance at a time, longest first, pulled from device work
+ * counters).  All problems share precision (FP64 or FP32); arith must be FAST. */
 int lss_adi_batch_create(const lss_adi_problem *problems, int count, lss_adi_batch **b);
 
 /* mode 0 = forward values only, 1 = forward + adjoint (values, the 5 parameter

@@ -1,11 +1,12 @@
 // adi_batched.cu -- many uneven ADI instances advanced by one persistent kernel.
 //
-// Each CTA pulls an instance index from a device counter (instances sorted longest
-// first), runs that instance's whole time loop with CTA barriers between the sweeps,
-// then pulls the next one.  The time-invariant line systems of every instance are
+// Each CTA is cut into warp groups of 1-4 warps; a group pulls an instance index from its
+// class's device counter (instances sorted longest first), runs that instance's whole time
+// loop with the group's own barrier between the sweeps, then pulls the next one.  The
+// time-invariant line systems of every instance are
 // factorised once on the device (k_setup_s_lines / k_setup_v_lines): the time loop only
 // does the pre-scaled right-hand side, one FMA of forward recurrence and one of back
-// substitution per point, because GB300's FP64 pipe (~1.2 TFLOP/s measured) and not HBM
+// substitution per point, because GB300's FP64 pipe (~1.25 TFLOP/s measured) and not HBM
 // is the binding resource.  Same time-step structure as the reference
 // (implicit_heston_time_loop::run, lss_2d_general_heston_equation_implicit_kernel.hpp:150-207).
 #include <algorithm>
