@@ -99,10 +99,12 @@ int lss_adi_create(const lss_adi_problem *p, lss_adi_handle **h)
     hh->parametric = true;
     hh->prob = *p;
     try {
-        // time-dependent coefficients (SABR, r != 0) re-evaluate their tables every step on the
-        // kernel-per-sweep path; the factorised paths precompute time-invariant line factors.
-        // The explicit Euler scheme has no line solves: kernel-per-step path as well.
-        if (p->arith == LSS_ADI_ARITH_FAST && !time_dependent(*p) && p->scheme != LSS_ADI_EXPLICIT_EULER)
+        // time-dependent coefficients (SABR, r != 0) rebuild their S-line factorisation before
+        // every step: on the factorised wide path in FP64, on the kernel-per-sweep path (which
+        // refactorises every sweep anyway) in FP32.  The explicit Euler scheme has no line
+        // solves: kernel-per-step path.
+        if (p->arith == LSS_ADI_ARITH_FAST && (!time_dependent(*p) || p->precision == LSS_ADI_FP64) &&
+            p->scheme != LSS_ADI_EXPLICIT_EULER)
             rc = make_wide_solver(*p, hh->wide);
         else
             rc = p->precision == LSS_ADI_FP64 ? make_plain<double>(*p, p->arith, p->eval_s, p->eval_v, hh->s64)

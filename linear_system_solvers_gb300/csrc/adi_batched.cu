@@ -166,6 +166,48 @@ struct setup_params {
     const double *scal;          // per instance: theta, zeta, gamma
 };
 
+// The 18 S-line slots of one point from its coefficients, 1/beta and gamma (double arithmetic).
+template <typename T>
+__device__ __forceinline__ void s_line_slots(T *s, long long slot_stride, int scheme, double th, double ze, double gm,
+                                             double M, double P, double Z, double Mt, double Pt, double W, double C,
+                                             double ib, double gam)
+{
+    const double a = -th * M, c = -th * P;
+    s[SL_LA * slot_stride] = static_cast<T>(a * ib);
+    s[SL_G * slot_stride] = static_cast<T>(gam);
+    s[SL_WG * slot_stride] = static_cast<T>(gm * C * ib);
+    s[SL_WW * slot_stride] = static_cast<T>((1.0 - th) * M * ib);
+    s[SL_WS * slot_stride] = static_cast<T>(Mt * ib);
+    s[SL_WC * slot_stride] = static_cast<T>((1.0 - W - (1.0 - th) * Z) * ib);
+    s[SL_WN * slot_stride] = static_cast<T>(Pt * ib);
+    s[SL_WE * slot_stride] = static_cast<T>((1.0 - th) * P * ib);
+    const double sc = th * Z * ib, se = c * ib;
+    if (scheme == LSS_ADI_HUNDSDORFER_VERWER) {
+        // fused HV stage: rhs4 + rhs_intermed_3 expressed in Delta = Y2 - U and Y1
+        s[SL_S2SC * slot_stride] = static_cast<T>(sc + ib);
+        s[SL_S2SE * slot_stride] = static_cast<T>(se);
+        s[SL_S2IB * slot_stride] = static_cast<T>(0.0);
+        s[SL_S2MZ * slot_stride] = static_cast<T>(ze * gm * C * ib);
+        s[SL_X1 * slot_stride] = static_cast<T>(a * ib + ze * M * ib);
+        s[SL_X2 * slot_stride] = static_cast<T>(sc - ze * (W + Z) * ib);
+        s[SL_X3 * slot_stride] = static_cast<T>(se + ze * P * ib);
+        s[SL_X4 * slot_stride] = static_cast<T>(ze * Mt * ib);
+        s[SL_X5 * slot_stride] = static_cast<T>(ze * Pt * ib);
+    } else {
+        const double zt = (scheme == LSS_ADI_MODIFIED_CRAIG_SNEYD) ? (ze - th) : 0.0;
+        s[SL_S2SC * slot_stride] = static_cast<T>(sc);
+        s[SL_S2SE * slot_stride] = static_cast<T>(se);
+        s[SL_S2IB * slot_stride] = static_cast<T>(ib);
+        s[SL_S2MZ * slot_stride] = static_cast<T>(ze * gm * C * ib);
+        s[SL_X1 * slot_stride] = static_cast<T>(zt * M * ib);
+        s[SL_X2 * slot_stride] = static_cast<T>(-zt * (Z + W) * ib);
+        s[SL_X3 * slot_stride] = static_cast<T>(-zt * P * ib);
+        s[SL_X4 * slot_stride] = static_cast<T>(zt * Mt * ib);
+        s[SL_X5 * slot_stride] = static_cast<T>(zt * Pt * ib);
+    }
+    s[SL_IB * slot_stride] = static_cast<T>(ib);
+}
+
 template <typename T>
 __global__ void k_setup_s_lines(setup_params sp, T *S0, long long slot_stride, T *chS_arena)
 {
@@ -185,50 +227,28 @@ __global__ void k_setup_s_lines(setup_params sp, T *S0, long long slot_stride, T
     const int nx = d.nx, ny = d.ny, e = nx - 2;
     const double th = sp.scal[3 * inst], ze = sp.scal[3 * inst + 1], gm = sp.scal[3 * inst + 2];
     const long long N = sp.total_n;
-    const double *bM = sp.base, *bP = sp.base + N, *bZ = sp.base + 2 * N, *bMt = sp.base + 3 * N,
-                 *bPt = sp.base + 4 * N, *bW = sp.base + 5 * N, *bC = sp.base + 6 * N;
+    const double *__restrict__ bM = sp.base, *__restrict__ bP = sp.base + N, *__restrict__ bZ = sp.base + 2 * N,
+                 *__restrict__ bMt = sp.base + 3 * N, *__restrict__ bPt = sp.base + 4 * N,
+                 *__restrict__ bW = sp.base + 5 * N, *__restrict__ bC = sp.base + 6 * N;
+    // the next point's coefficients are loaded before this point's eighteen stores, so that one
+    // DRAM latency per point overlaps the work of the point before (the loop is serial along the
+    // line: the set-up of one instance's lines runs on few threads before every step of a
+    // time-dependent instance)
+    long long o1 = d.o2 + ny + j;
+    double nM = bM[o1], nP = bP[o1], nZ = bZ[o1], nMt = bMt[o1], nPt = bPt[o1], nW = bW[o1], nC = bC[o1];
     double gam = 0.0;
     for (int t = 1; t <= e; ++t) {
         const long long o = d.o2 + (long long)t * ny + j;
-        const double M = bM[o], P = bP[o], Z = bZ[o], Mt = bMt[o], Pt = bPt[o], W = bW[o], C = bC[o];
+        const double M = nM, P = nP, Z = nZ, Mt = nMt, Pt = nPt, W = nW, C = nC;
+        if (t < e) {
+            o1 = o + ny;
+            nM = bM[o1]; nP = bP[o1]; nZ = bZ[o1]; nMt = bMt[o1]; nPt = bPt[o1]; nW = bW[o1]; nC = bC[o1];
+        }
         const double a = -th * M, b = 1.0 + th * Z, c = -th * P;
         const double beta = (t == 1) ? b : b - a * gam;
         const double ib = 1.0 / beta;
         if (t < e) gam = c / beta;
-        T *s = S0 + o;
-        s[SL_LA * slot_stride] = static_cast<T>(a * ib);
-        s[SL_G * slot_stride] = static_cast<T>(t < e ? gam : 0.0);
-        s[SL_WG * slot_stride] = static_cast<T>(gm * C * ib);
-        s[SL_WW * slot_stride] = static_cast<T>((1.0 - th) * M * ib);
-        s[SL_WS * slot_stride] = static_cast<T>(Mt * ib);
-        s[SL_WC * slot_stride] = static_cast<T>((1.0 - W - (1.0 - th) * Z) * ib);
-        s[SL_WN * slot_stride] = static_cast<T>(Pt * ib);
-        s[SL_WE * slot_stride] = static_cast<T>((1.0 - th) * P * ib);
-        const double sc = th * Z * ib, se = c * ib;
-        if (d.scheme == LSS_ADI_HUNDSDORFER_VERWER) {
-            // fused HV stage: rhs4 + rhs_intermed_3 expressed in Delta = Y2 - U and Y1
-            s[SL_S2SC * slot_stride] = static_cast<T>(sc + ib);
-            s[SL_S2SE * slot_stride] = static_cast<T>(se);
-            s[SL_S2IB * slot_stride] = static_cast<T>(0.0);
-            s[SL_S2MZ * slot_stride] = static_cast<T>(ze * gm * C * ib);
-            s[SL_X1 * slot_stride] = static_cast<T>(a * ib + ze * M * ib);
-            s[SL_X2 * slot_stride] = static_cast<T>(sc - ze * (W + Z) * ib);
-            s[SL_X3 * slot_stride] = static_cast<T>(se + ze * P * ib);
-            s[SL_X4 * slot_stride] = static_cast<T>(ze * Mt * ib);
-            s[SL_X5 * slot_stride] = static_cast<T>(ze * Pt * ib);
-        } else {
-            const double zt = (d.scheme == LSS_ADI_MODIFIED_CRAIG_SNEYD) ? (ze - th) : 0.0;
-            s[SL_S2SC * slot_stride] = static_cast<T>(sc);
-            s[SL_S2SE * slot_stride] = static_cast<T>(se);
-            s[SL_S2IB * slot_stride] = static_cast<T>(ib);
-            s[SL_S2MZ * slot_stride] = static_cast<T>(ze * gm * C * ib);
-            s[SL_X1 * slot_stride] = static_cast<T>(zt * M * ib);
-            s[SL_X2 * slot_stride] = static_cast<T>(-zt * (Z + W) * ib);
-            s[SL_X3 * slot_stride] = static_cast<T>(-zt * P * ib);
-            s[SL_X4 * slot_stride] = static_cast<T>(zt * Mt * ib);
-            s[SL_X5 * slot_stride] = static_cast<T>(zt * Pt * ib);
-        }
-        s[SL_IB * slot_stride] = static_cast<T>(ib);
+        s_line_slots<T>(S0 + o, slot_stride, d.scheme, th, ze, gm, M, P, Z, Mt, Pt, W, C, ib, t < e ? gam : 0.0);
         if (t == e) chS_arena[d.oy + j] = static_cast<T>(c * ib);
     }
 }
@@ -287,6 +307,51 @@ struct tdep_params {
     int nx, ny;
     double alpha, delta, two_alpha, half_rho_f;
 };
+
+// The S-line factorisation of the time-dependent instance in two kernels: the recurrence
+// beta_t = b_t - a_t gamma_{t-1} (serial along each line, one thread per line: only 1/beta and
+// gamma, the few FP64 operations on the serial chain), then every slot of every point in
+// parallel (s_line_slots, the same values as k_setup_s_lines).
+template <typename T>
+__global__ void k_tdep_s_factor(const double *__restrict__ base, long long n, int nx, int ny, double th, T *S0)
+{
+    const int j = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (j > ny - 2) return;
+    const int e = nx - 2;
+    const double *__restrict__ bM = base, *__restrict__ bP = base + n, *__restrict__ bZ = base + 2 * n;
+    long long o1 = (long long)ny + j;
+    double nM = bM[o1], nP = bP[o1], nZ = bZ[o1];
+    double gam = 0.0;
+    for (int t = 1; t <= e; ++t) {
+        const long long o = (long long)t * ny + j;
+        const double M = nM, P = nP, Z = nZ;
+        if (t < e) {
+            o1 = o + ny;
+            nM = bM[o1]; nP = bP[o1]; nZ = bZ[o1];
+        }
+        const double a = -th * M, b = 1.0 + th * Z, c = -th * P;
+        const double beta = (t == 1) ? b : b - a * gam;
+        S0[SL_IB * n + o] = static_cast<T>(1.0 / beta);
+        if (t < e) gam = c / beta;
+        S0[SL_G * n + o] = static_cast<T>(t < e ? gam : 0.0);
+    }
+}
+
+template <typename T>
+__global__ void k_tdep_s_slots(const double *__restrict__ base, long long n, int nx, int ny, int scheme, double th,
+                               double ze, double gm, T *S0, T *chS)
+{
+    const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const int e = nx - 2;
+    if (q >= (long long)e * (ny - 2)) return;
+    const int t = 1 + static_cast<int>(q / (ny - 2)), j = 1 + static_cast<int>(q % (ny - 2));
+    const long long o = (long long)t * ny + j;
+    const double M = base[o], P = base[n + o], Z = base[2 * n + o], Mt = base[3 * n + o], Pt = base[4 * n + o],
+                 W = base[5 * n + o], C = base[6 * n + o];
+    const double ib = static_cast<double>(S0[SL_IB * n + o]), gam = static_cast<double>(S0[SL_G * n + o]);
+    s_line_slots<T>(S0 + o, n, scheme, th, ze, gm, M, P, Z, Mt, Pt, W, C, ib, gam);
+    if (t == e) chS[j] = static_cast<T>(-th * P * ib);
+}
 
 template <typename T>
 __global__ void k_tdep_refresh(tdep_params tp, double da, double dc, T *xarena, long long total_x)
@@ -1769,10 +1834,9 @@ template <typename T> struct batch_typed {
     // before each step, forward or adjoint, the S-line tables are rebuilt at the step's time
     bool tdep = false;
     dbuf<double> td_buf;            // base tables (7 n), a_static, c_static, ab (n each), per_i (5 nx), xs (3 nx)
-    dbuf<double> td_scal;           // theta, zeta, gamma
-    dbuf<long long> td_ls;          // S-line offset of the instance (0)
     tdep_params td{};
     std::vector<double> td_da, td_dc; // D(t)^(2(1-beta)), D(t)^(1-beta) per step
+    double td_theta = 0.0, td_zeta = 0.0, td_gamma = 0.0;
     int init_tdep(const lss_adi_problem &p);
     // products: 1 = the forward chunk products of the S lines, 2 = the adjoint's
     void refresh_step(cudaStream_t s, int step, int products);
@@ -2028,12 +2092,9 @@ template <typename T> int batch_typed<T>::init_tdep(const lss_adi_problem &p)
     }
     LSS_CUDA_TRY(td_buf.alloc(total), "batch: allocating time-dependent tables");
     LSS_CUDA_TRY(td_buf.upload(h.data(), total), "batch: uploading time-dependent tables");
-    const double scal[3] = {tt.sc.theta, tt.sc.zeta, tt.sc.gamma};
-    LSS_CUDA_TRY(td_scal.alloc(3), "batch: allocating scalars");
-    LSS_CUDA_TRY(td_scal.upload(scal, 3), "batch: uploading scalars");
-    const long long zero = 0;
-    LSS_CUDA_TRY(td_ls.alloc(1), "batch: allocating line offsets");
-    LSS_CUDA_TRY(td_ls.upload(&zero, 1), "batch: uploading line offsets");
+    td_theta = tt.sc.theta;
+    td_zeta = tt.sc.zeta;
+    td_gamma = tt.sc.gamma;
     LSS_CUDA_TRY(cudaDeviceSynchronize(), "batch: time-dependent tables");
     td.base = td_buf.p;
     td.a_static = td_buf.p + off_stat;
@@ -2061,15 +2122,9 @@ template <typename T> void batch_typed<T>::refresh_step(cudaStream_t s, int step
     const bdesc &d = desc[0];
     const long long n = total_n;
     k_tdep_refresh<T><<<grid_for(n, 256), 256, 0, s>>>(td, td_da[step], td_dc[step], xarena.p, total_x);
-    setup_params sp{};
-    sp.desc = d_desc.p;
-    sp.line_start = td_ls.p;
-    sp.count = 1;
-    sp.total_lines = d.ny - 2;
-    sp.base = td.base;
-    sp.total_n = n;
-    sp.scal = td_scal.p;
-    k_setup_s_lines<T><<<grid_for(d.ny - 2, 128), 128, 0, s>>>(sp, stab.p, n, yarena.p + Y_CHS * total_y);
+    k_tdep_s_factor<T><<<grid_for(d.ny - 2, 32), 32, 0, s>>>(td.base, n, d.nx, d.ny, td_theta, stab.p);
+    k_tdep_s_slots<T><<<grid_for(static_cast<long long>(d.nx - 2) * (d.ny - 2), 256), 256, 0, s>>>(
+        td.base, n, d.nx, d.ny, d.scheme, td_theta, td_zeta, td_gamma, stab.p, yarena.p + Y_CHS * total_y);
     if (wide_ps > 1) {
         const bparams<T> p = params();
         const int g = grid_for(static_cast<long long>(d.ny - 2) * wide_ps, 128);
@@ -2568,7 +2623,7 @@ template <typename T> int batch_typed<T>::enqueue_wide(cudaStream_t s)
     LSS_CUDA_TRY(cudaMemcpyAsync(U, d_payoff.p, total_n * sizeof(T), cudaMemcpyDeviceToDevice, s), "wide: initial state");
     LSS_CUDA_TRY(cudaMemsetAsync(d_status.p, 0, sizeof(int), s), "wide: clearing the status");
     long long nl = 0;
-    const int per_refresh = 2 + (wide_ps > 1 ? 1 : 0);
+    const int per_refresh = 3 + (wide_ps > 1 ? 1 : 0);
     for (int step = 0; step < d.steps; ++step) {
         if (tdep) {
             refresh_step(s, step, 1);
@@ -2645,7 +2700,7 @@ template <typename T> int batch_typed<T>::enqueue_wide_adjoint(cudaStream_t s)
         const int per_step = d.scheme == LSS_ADI_DOUGLAS_RACHFORD ? 4 : 6;
         const double *cur = CK;
         const int n0_last = (nseg - 1) * c; // the last segment keeps its stage values: no recomputation
-        const int per_refresh = 2 + (ps > 1 ? 1 : 0);
+        const int per_refresh = 3 + (ps > 1 ? 1 : 0);
         for (int step = 0; step < d.steps; ++step) {
             if (tdep) {
                 refresh_step(s, step, 1);
