@@ -96,6 +96,8 @@ CASES = {
     "sabr_mcs_r03": dict(SABR, scheme="mcs", zeta=0.8, theta_scheme="theta80", rate=0.03, nx=40, ny=22, nt=21),
     "sabr_hv_r03": dict(SABR, scheme="hv", rate=0.05, nx=46, ny=24, nt=21),
     "wide_sabr_cs_r03": dict(SABR, scheme="cs", rate=0.03, nx=280, ny=90, nt=17, maturity=2.0),
+    # forward time stepping: D(t) at t = k, 2k, ... (the tables and the adjoint's D(t) factors)
+    "sabr_hv_fwd_r03": dict(SABR, scheme="hv", forward=True, rate=0.03, nx=44, ny=24, nt=21),
 }
 
 

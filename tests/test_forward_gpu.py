@@ -56,7 +56,7 @@ def test_fast_arith_within_1e10_of_oracle(lss, oracle, key):
     assert rel_err(got, want) < fp64_tol(want, op.s_hi)
 
 
-@pytest.mark.parametrize("key", ["config1_dr_f32", "cs_f32", "mcs_nu_f32", "hv_f32"])
+@pytest.mark.parametrize("key", ["config1_dr_f32", "cs_f32", "mcs_nu_f32", "hv_f32", "sabr_t_ds_f32"])
 def test_fast_arith_fp32_as_close_as_reference_fp32(lss, oracle, key):
     kw, fp = CASES[key]
     op, pp = problem_pair(kw)
