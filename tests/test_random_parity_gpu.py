@@ -37,7 +37,7 @@ def draw(seed):
     return kw
 
 
-@pytest.mark.parametrize("seed", range(24))
+@pytest.mark.parametrize("seed", range(64))
 def test_random_problem_parity(lss, oracle, seed):
     kw = draw(1000 + seed)
     op, pp = problem_pair(kw)
