@@ -309,34 +309,9 @@ struct tdep_params {
 };
 
 // The S-line factorisation of the time-dependent instance in two kernels: the recurrence
-// beta_t = b_t - a_t gamma_{t-1} (serial along each line, one thread per line: only 1/beta and
-// gamma, the few FP64 operations on the serial chain), then every slot of every point in
-// parallel (s_line_slots, the same values as k_setup_s_lines).
-template <typename T>
-__global__ void k_tdep_s_factor(const double *__restrict__ base, long long n, int nx, int ny, double th, T *S0)
-{
-    const int j = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-    if (j > ny - 2) return;
-    const int e = nx - 2;
-    const double *__restrict__ bM = base, *__restrict__ bP = base + n, *__restrict__ bZ = base + 2 * n;
-    long long o1 = (long long)ny + j;
-    double nM = bM[o1], nP = bP[o1], nZ = bZ[o1];
-    double gam = 0.0;
-    for (int t = 1; t <= e; ++t) {
-        const long long o = (long long)t * ny + j;
-        const double M = nM, P = nP, Z = nZ;
-        if (t < e) {
-            o1 = o + ny;
-            nM = bM[o1]; nP = bP[o1]; nZ = bZ[o1];
-        }
-        const double a = -th * M, b = 1.0 + th * Z, c = -th * P;
-        const double beta = (t == 1) ? b : b - a * gam;
-        S0[SL_IB * n + o] = static_cast<T>(1.0 / beta);
-        if (t < e) gam = c / beta;
-        S0[SL_G * n + o] = static_cast<T>(t < e ? gam : 0.0);
-    }
-}
-
+// beta_t = b_t - a_t gamma_{t-1} for 1/beta and gamma (k_tdep_s_factor, partitioned along the
+// lines), then every slot of every point in parallel (s_line_slots, the same formulas as
+// k_setup_s_lines).
 template <typename T>
 __global__ void k_tdep_s_slots(const double *__restrict__ base, long long n, int nx, int ny, int scheme, double th,
                                double ze, double gm, T *S0, T *chS)
@@ -1022,6 +997,65 @@ __device__ __forceinline__ void chunk_range(int e, int P, int c, int &t0, int &t
 {
     t0 = 1 + static_cast<int>((static_cast<long long>(c) * e) / P);
     t1 = static_cast<int>((static_cast<long long>(c + 1) * e) / P);
+}
+
+// The recurrence of the time-dependent S-line factorisation, partitioned like the line solves
+// (CTA: L lines x P chunks).  beta_t = b_t - a_t c_{t-1} / beta_{t-1} is the Moebius map of the
+// matrix [[b_t, -a_t c_{t-1}], [1, 0]] applied to beta_{t-1}: each chunk forms the product of its
+// rows' matrices (rescaled every 8 rows: only the ratio matters), a chunk composes the maps of
+// the chunks before it to get its incoming beta, then runs its own rows' recurrence from it
+// (1/beta and gamma = c/beta), so the serial chain is a chunk long instead of a line long.
+// Same values as the serial recurrence up to the rounding of the incoming beta of each chunk.
+template <typename T>
+__global__ void __launch_bounds__(1024) k_tdep_s_factor(const double *__restrict__ base, long long n, int nx, int ny,
+                                                        double th, T *S0)
+{
+    __shared__ double sm[4][1024]; // each chunk's map [[m11, m12], [m21, m22]], indexed [c * L + line]
+    const int L = blockDim.x, P = blockDim.y, lane = threadIdx.x, c = threadIdx.y;
+    const int j = 1 + blockIdx.x * L + lane;
+    const bool act = j <= ny - 2;
+    const int e = nx - 2, k = c * L + lane;
+    int t0, t1;
+    chunk_range(e, P, c, t0, t1);
+    const double *__restrict__ bM = base, *__restrict__ bP = base + n, *__restrict__ bZ = base + 2 * n;
+    if (act) {
+        double m11 = 1.0, m12 = 0.0, m21 = 0.0, m22 = 1.0;
+        double pprev = t0 > 1 ? bP[(long long)(t0 - 1) * ny + j] : 0.0; // P of row t-1 (c_{t-1} = -theta P)
+        for (int t = t0; t <= t1; ++t) {
+            const long long o = (long long)t * ny + j;
+            const double b = 1.0 + th * bZ[o];
+            const double ac = t > 1 ? (-th * bM[o]) * (-th * pprev) : 0.0; // a_t c_{t-1}
+            pprev = bP[o];
+            const double n11 = b * m11 - ac * m21, n12 = b * m12 - ac * m22;
+            m21 = m11;
+            m22 = m12;
+            m11 = n11;
+            m12 = n12;
+            if (((t - t0) & 7) == 7) {
+                const double sc = 1.0 / fmax(fabs(m11), fabs(m21));
+                m11 *= sc; m12 *= sc; m21 *= sc; m22 *= sc;
+            }
+        }
+        sm[0][k] = m11; sm[1][k] = m12; sm[2][k] = m21; sm[3][k] = m22;
+    }
+    __syncthreads();
+    if (!act) return;
+    // beta_{t0-1}: the maps of chunks 0 .. c-1 applied in order (chunk 0 starts at row 1, whose
+    // map ignores its argument: a_1 c_0 = 0)
+    double x = 1.0;
+    for (int q = 0; q < c; ++q) {
+        const int kq = q * L + lane;
+        x = (sm[0][kq] * x + sm[1][kq]) / (sm[2][kq] * x + sm[3][kq]);
+    }
+    double gam = t0 > 1 ? (-th * bP[(long long)(t0 - 1) * ny + j]) / x : 0.0;
+    for (int t = t0; t <= t1; ++t) {
+        const long long o = (long long)t * ny + j;
+        const double a = -th * bM[o], b = 1.0 + th * bZ[o], cc = -th * bP[o];
+        const double beta = (t == 1) ? b : b - a * gam;
+        S0[SL_IB * n + o] = static_cast<T>(1.0 / beta);
+        if (t < e) gam = cc / beta;
+        S0[SL_G * n + o] = static_cast<T>(t < e ? gam : 0.0);
+    }
 }
 
 // hf / hb of every chunk of every line; lines along j ([t][j] tables, S) or i ([t][i], v)
@@ -2122,7 +2156,12 @@ template <typename T> void batch_typed<T>::refresh_step(cudaStream_t s, int step
     const bdesc &d = desc[0];
     const long long n = total_n;
     k_tdep_refresh<T><<<grid_for(n, 256), 256, 0, s>>>(td, td_da[step], td_dc[step], xarena.p, total_x);
-    k_tdep_s_factor<T><<<grid_for(d.ny - 2, 32), 32, 0, s>>>(td.base, n, d.nx, d.ny, td_theta, stab.p);
+    {
+        // chunks of at least 4 rows, at most 32; 8 lines per CTA
+        int P = 1;
+        while (P < 32 && d.nx - 2 >= 8 * P) P *= 2;
+        k_tdep_s_factor<T><<<grid_for(d.ny - 2, 8), dim3(8, P), 0, s>>>(td.base, n, d.nx, d.ny, td_theta, stab.p);
+    }
     k_tdep_s_slots<T><<<grid_for(static_cast<long long>(d.nx - 2) * (d.ny - 2), 256), 256, 0, s>>>(
         td.base, n, d.nx, d.ny, d.scheme, td_theta, td_zeta, td_gamma, stab.p, yarena.p + Y_CHS * total_y);
     if (wide_ps > 1) {
