@@ -114,7 +114,7 @@ def parse():
     ap.add_argument("--max-time-steps", type=int, default=0,
                     help="cap every instance's time loop (a smaller workload for profiler captures; 0 = no cap)")
     ap.add_argument("--configs", default="", help="comma list of configurations to measure instead of the batched "
-                    "headline: c1, c2, c4, c5, c5sabr, mcsz, euler, batch32, heat1d (one JSON line each)")
+                    "headline: c1, c2, c4, c5, c5sabr, sabr_r, mcsz, euler, batch32, heat1d (one JSON line each)")
     return ap.parse_args()
 
 
@@ -651,15 +651,22 @@ def run_configs(args):
                               "nonfinite_instances": int(np.count_nonzero(status))}), flush=True)
     if "heat1d" in wanted:
         run_heat1d()
-    if "c5sabr" in wanted:
-        p = lss.HestonProblem(model="sabr", sigma=0.4, rho=-0.3, sabr_beta=0.5, rate=0.0, strike=0.05, maturity=2.0,
-                              s_lo=0.0, s_hi=0.2, v_lo=0.0, v_hi=1.0, nx=2048, ny=1024, nt=801, scheme="dr",
+    for key, rate, nt, fd_names in (("c5sabr", 0.0, 801, ("sigma", "rho")),
+                                    ("sabr_r", 0.03, 201, ("sigma", "rho", "rate"))):
+        if key not in wanted:
+            continue
+        # c5sabr: config 5's SABR problem (r unspecified there: 0, coefficients constant in time);
+        # sabr_r: the reference's own SABR rate r = 0.03, whose D(t) = exp(-r (T - t)) makes the
+        # coefficients time-dependent (the S-line tables are rebuilt before every step)
+        p = lss.HestonProblem(model="sabr", sigma=0.4, rho=-0.3, sabr_beta=0.5, rate=rate, strike=0.05, maturity=2.0,
+                              s_lo=0.0, s_hi=0.2, v_lo=0.0, v_hi=1.0, nx=2048, ny=1024, nt=nt, scheme="dr",
                               nonuniform=True, acc_point=0.05, alpha_scale=10.0, beta_scale=24.0, eval_s=0.05,
                               eval_v=0.2)
-        case("config5 SABR DR 2048x1024x800", p, "f64", 1, oracle_nt=11)
-        # forward + adjoint: dV/d(nu, rho, r) and dV/d(payoff) in one backward pass; nu and rho
-        # checked against Richardson central differences (relative bumps 1e-4, 5e-5: the
-        # sensitivities are ~1e-2 of the value) of the device forward, thread-per-line solves
+        label = f"config5 SABR DR 2048x1024x{nt - 1}" + (f" r={rate}" if rate else "")
+        case(label, p, "f64", 1, oracle_nt=11)
+        # forward + adjoint: dV/d(nu, rho, r) and dV/d(payoff) in one backward pass; checked against
+        # Richardson central differences (relative bumps 1e-4, 5e-5: the sensitivities are ~1e-2 of
+        # the value) of the device forward, thread-per-line solves
         s = lss.ImplicitHestonSolver(p, precision="f64", arith="fast")
         s.adjoint(want_payoff_grad=False)
         torch.cuda.synchronize()
@@ -673,19 +680,23 @@ def run_configs(args):
             return lss.ImplicitHestonSolver(q, precision="f64", arith="fast").solve()[1]
 
         errs = {}
-        for idx, name in ((2, "sigma"), (3, "rho")):
+        for name in fd_names:
+            idx = {"sigma": 2, "rho": 3, "rate": 4}[name]
             base = getattr(p, name)
             cd = []
-            for rel in (1e-4, 5e-5):
+            # r = 0.03: a relative bump of 1e-4 moves r by 3e-6, where the forward's rounding noise
+            # (~1e-12 of V) is ~1e-6 of the difference; 1e-3 / 5e-4 keep it below 1e-7
+            for rel in ((1e-3, 5e-4) if name == "rate" else (1e-4, 5e-5)):
                 h = rel * abs(base)
                 cd.append((fwd(dataclasses.replace(p, **{name: base + h})) -
                            fwd(dataclasses.replace(p, **{name: base - h}))) / (2 * h))
             fd = (4.0 * cd[1] - cd[0]) / 3.0
             errs[name] = abs(grads[idx] - fd) / max(abs(fd), 1e-3 * abs(val))
-        print(json.dumps({"config": "config5 SABR DR 2048x1024x800 forward + adjoint", "device_gps_fwd_adj":
+        print(json.dumps({"config": label + " forward + adjoint", "device_gps_fwd_adj":
                           p.nx * p.ny * (p.nt - 1) / secs, "device_seconds": secs, "value": val,
                           "dV_dnu": grads[2], "dV_drho": grads[3], "dV_dr": grads[4],
-                          "rel_err_vs_device_fd": errs, "fd": "Richardson central, bumps 1e-4 / 5e-5, device forward"}),
+                          "rel_err_vs_device_fd": errs,
+                          "fd": "Richardson central, relative bumps 1e-4 / 5e-5 (r: 1e-3 / 5e-4), device forward"}),
               flush=True)
 
 
