@@ -294,8 +294,8 @@ __global__ void k_setup_v_lines(setup_params sp, T *V0, long long slot_stride, T
 // a and c carry D(t)^(2(1-beta)) and D(t)^(1-beta), D(t) = exp(-r (T - t)); b, d, e, f do not.
 // Before each step the S-direction base tables M, P, Z, C are re-evaluated at the step's powers
 // da, dc (general_heston_equation_coefficients, coefficients.hpp:89-98, on the transformed data
-// of lss_heat_data_transform.hpp:174-214) and the S lines re-factorised (k_setup_s_lines); the
-// v-direction tables do not change.  The same kernel scales the S-factors of the adjoint's
+// of lss_heat_data_transform.hpp:174-214) and the S lines re-factorised (k_tdep_s_factor,
+// k_tdep_s_slots); the v-direction tables do not change.  The same kernel scales the S-factors of the adjoint's
 // D(t) terms (X_HA, X_HDD by da, X_HC by dc) and the boundary-column weights that carry d^ on
 // the v = v_lo line (XB_M, XB_P), so that the adjoint steps see this step's a^ and c^.
 struct tdep_params {
